@@ -1,0 +1,343 @@
+#!/usr/bin/env python3
+"""Benchmark: K*mumu P-wave NLL + analytic gradient evaluations per second at 1M events.
+
+One step = one evaluation of sum log p and its 8 gradient sums over the 1M
+events of one dataset: the lh_grad kernel of the reference's fitter
+(include/fitter.hh:1054-1151) lowered to CUDA on sm_103a.
+
+  value  : device throughput, FP64, the hoisted event columns resident in HBM,
+           timed with CUDA events on the backend's stream. Datasets rotate
+           over enough independent 1M-event sets that the bytes read between
+           two reads of one set exceed twice the L2 (129 MB).
+  e2e    : the same metric through the public API with HOST event buffers:
+           every step uploads the raw events (3 x 1M FP64 from pinned host
+           memory), runs the precompute kernel and the NLL+gradient kernel,
+           and reads the 9 sums back.
+  mixed  : FP32 storage/per-event arithmetic with FP64 sums (same timing as value).
+  cpu_baseline : the reference's kernel text (the same get_kernel() strings)
+           compiled with gcc, on the host cores, Kahan-summed as the
+           reference's CPU backend does (oracle/spec_kernel.py).
+
+--impl reference times only that CPU path (all host threads).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "K*mumu P-wave NLL+grad evals/s at 1M events"
+N_EVENTS = 1_000_000
+L2_BYTES = 129 * 1024 * 1024
+
+
+def _peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                r = subprocess.run(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                    "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                if r.returncode == 0 and r.stdout.strip():
+                    self.samples.append([x.strip() for x in r.stdout.strip().split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i].strip() == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def reference_arm(args):
+    """The reference's CPU path: its kernel text through the CPU backend's loop, all host threads."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import mforacle
+    from oracle.spec_kernel import SpecKernel
+    from morefit_gb300.workloads import load_spec
+    spec = load_spec("pwave")
+    ks = {k["name"]: k for k in spec["kernels"]}
+    n = args.nevents
+    ev = mforacle.generate("pwave", n)
+    cols = SpecKernel(ks["precompute_kernel"]).store(ev, [])
+    grad = SpecKernel(ks["lh_grad_kernel"])
+    from morefit_gb300.backend import eval_expressions
+    truth = np.array(spec["truth"])
+    pv = np.concatenate([truth, eval_expressions(spec["parameters"], truth, [e for _, e in spec["grad_buffers"]])])
+    nthreads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        grad.reduce(cols, pv, nthreads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        s = grad.reduce(cols, pv, nthreads)
+    dt = time.perf_counter() - t0
+    v = args.steps / dt
+    line = {"metric": METRIC, "value": v, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded accept-reject)",
+            "impl": "reference",
+            "config": {"workload": "K*mumu P-wave angular fit, 8 parameters, 1M events, FP64",
+                       "nevents": n, "inputs": "host memory"},
+            "cpu_baseline": {"value": v, "unit": "evals/s", "cores": nthreads, "kind": "port",
+                             "sample": f"{args.steps} NLL+grad evaluations over all {n} events; the reference's "
+                                       "lh_grad kernel text compiled by gcc -O3, Kahan-summed per thread chunk"},
+            "e2e": {"value": v, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "nll_check": float(-2.0 * s[0])}
+    print(json.dumps(line), flush=True)
+
+
+def ours(args):
+    import torch
+    from morefit_gb300 import _lib as L
+    from morefit_gb300.backend import CUDABackend
+    from morefit_gb300.workloads import Likelihood, generate_events, load_spec
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    backend = CUDABackend(local)
+    spec = load_spec("pwave")
+    truth = np.array(spec["truth"])
+    n = args.nevents
+    ks = {k["name"]: k for k in spec["kernels"]}
+    ncols_read = 11  # morefit_eventbuffer_3..13: the only columns the lh_grad expressions reference
+
+    def make_sets(kernelT):
+        itemsize = np.dtype(kernelT).itemsize
+        per_set = n * ncols_read * itemsize
+        nsets = max(2, math.ceil(2 * L2_BYTES / per_set) + 1)
+        sets = []
+        for r in range(nsets):
+            like = Likelihood(backend, spec, kernelT)
+            cols = generate_events(backend, spec, n, seed=229387429 + 1000 * rank + r)
+            like.set_device_data(cols)
+            sets.append(like)
+        return sets, per_stride_bytes(itemsize), nsets
+
+    def per_stride_bytes(itemsize):
+        return n * ncols_read * itemsize
+
+    stream_ptr = C_stream(backend)
+    ext = torch.cuda.ExternalStream(stream_ptr, device=torch.device("cuda", local))
+
+    def timed_device(sets, K, W):
+        """K NLL+grad launches rotating over the datasets, enqueued back to back; CUDA events on the stream."""
+        import ctypes as C
+        pv = sets[0].param_vector("lh_grad_kernel", truth)
+        kern = sets[0].blocks["lh_grad_kernel"].kernel
+        out_buf = L.c_buf()
+        L.check(L.lib.mf_buffer_alloc(backend.handle, max(K, W, 1) * kern.nout * 8, C.byref(out_buf)))
+
+        def enqueue(count):
+            ins = (L.c_buf * count)(*[sets[i % len(sets)].blocks["lh_grad_kernel"].input.buf for i in range(count)])
+            strides = np.array([sets[i % len(sets)].blocks["lh_grad_kernel"].input.stride for i in range(count)],
+                               dtype=np.uint64)
+            ns = np.full(count, n, dtype=np.uint64)
+            rows = np.ascontiguousarray(np.tile(pv, (count, 1)))
+            u64p = C.POINTER(C.c_uint64)
+            L.check(L.lib.mf_kernel_reduce_many(kern.handle, count, ins, strides.ctypes.data_as(u64p),
+                                                ns.ctypes.data_as(u64p), L.dptr(rows), len(pv), out_buf))
+
+        enqueue(W)
+        backend.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        enqueue(K)
+        e1.record(ext)
+        e1.synchronize()
+        backend.synchronize()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        res = np.zeros(kern.nout)
+        L.check(L.lib.mf_buffer_d2h(out_buf, 0, res.ctypes.data, kern.nout * 8))
+        L.lib.mf_buffer_free(out_buf)
+        return ms, res
+
+    # ---------------- FP64 device throughput (value) ----------------
+    sets64, bytes64, nsets64 = make_sets(np.float64)
+    with ClockSampler(local) as clk:
+        ms64, res64 = timed_device(sets64, args.steps, args.warmup)
+    if world > 1:
+        t = torch.tensor([ms64], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms64 = float(t.item())
+    value = world * args.steps / (ms64 / 1e3)
+    avg_launch_s = ms64 / 1e3 / args.steps
+    hbm_peak, peak_kind = _peaks()
+    achieved = bytes64 / avg_launch_s / 1e9
+
+    # ---------------- mixed precision ----------------
+    mixed = None
+    if not args.no_mixed:
+        sets32, bytes32, _ = make_sets(np.float32)
+        ms32, res32 = timed_device(sets32, args.steps, args.warmup)
+        mixed = {"value": world * args.steps / (ms32 / 1e3), "unit": "evals/s", "dtype": "f32 storage+arith, f64 sums",
+                 "speedup_vs_f64": ms64 / ms32,
+                 "roofline": {"bound": "hbm", "achieved": bytes32 / (ms32 / 1e3 / args.steps) / 1e9,
+                              "peak": hbm_peak, "unit": "GB/s",
+                              "frac": bytes32 / (ms32 / 1e3 / args.steps) / 1e9 / hbm_peak},
+                 "nll_rel_diff_vs_f64": abs(res32[0] - res64[0]) / abs(res64[0])}
+        del sets32
+
+    # ---------------- e2e through the public API, host buffers ----------------
+    if args.no_e2e:
+        args.e2e_steps = 3
+    host = sets64[0].pre.input.download()  # (3, n) FP64 raw events of set 0
+    pinned = torch.empty(host.shape, dtype=torch.float64).pin_memory()
+    pinned.numpy()[...] = host
+    host_pinned = pinned.numpy()
+    like = Likelihood(backend, spec, np.float64)
+    ke = max(3, min(args.steps, args.e2e_steps))
+    for _ in range(args.warmup):
+        like.set_data(host_pinned)
+        like.likelihood_and_gradient(truth)
+    backend.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(ke):
+        like.set_data(host_pinned)
+        nll_e2e, g_e2e = like.likelihood_and_gradient(truth)
+    e2e_s = (time.perf_counter() - t0) / ke
+    # fit-loop form: events resident, parameters in / sums out per evaluation
+    t0 = time.perf_counter()
+    for _ in range(ke * 4):
+        like.likelihood_and_gradient(truth)
+    fit_loop_s = (time.perf_counter() - t0) / (ke * 4)
+
+    # ---------------- CPU baseline (rank 0, N=1 only) ----------------
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        from oracle.spec_kernel import SpecKernel
+        cols = SpecKernel(ks["precompute_kernel"]).store(host, [])
+        gk = SpecKernel(ks["lh_grad_kernel"])
+        pvh = sets64[0].param_vector("lh_grad_kernel", truth)
+        nthreads = os.cpu_count() or 1
+        gk.reduce(cols, pvh, nthreads)
+        t0 = time.perf_counter()
+        nev = 0
+        while time.perf_counter() - t0 < args.cpu_seconds:
+            s_cpu = gk.reduce(cols, pvh, nthreads)
+            nev += 1
+        cpu_s = (time.perf_counter() - t0) / nev
+        cpu = {"value": 1.0 / cpu_s, "unit": "evals/s", "cores": nthreads, "kind": "port",
+               "sample": f"{nev} NLL+grad evaluations over all {n} events of dataset 0 "
+                         f"(~{args.cpu_seconds:.0f} s); the reference's lh_grad kernel text compiled by gcc -O3",
+               "nll_rel_diff_vs_gpu": abs(s_cpu[0] - float(like.sums('lh_grad_kernel', truth)[0])) / abs(s_cpu[0])}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms64 / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic: seeded accept-reject K*mumu P-wave events generated on the GPU",
+                "config": {"workload": "K*mumu P-wave angular fit, 8 free parameters, 1M events, FP64 (configs[1])",
+                           "nevents": n, "datasets_rotated": nsets64,
+                           "l2": f"{nsets64} x {bytes64 / 1e6:.0f} MB read in rotation (> 2x L2), no flush",
+                           "parallelism": "replicas" if world > 1 else "single GPU"},
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                             "frac": achieved / hbm_peak, "traffic": None,
+                             "peak_source": peak_kind,
+                             "algorithmic_bytes_per_launch": bytes64},
+                "e2e": {"value": world / e2e_s, "unit": "evals/s",
+                        "h2d_bytes_per_step": int(host.nbytes + 8 * 9), "d2h_bytes_per_step": 9 * 8,
+                        "what": "upload raw events (pinned host) + precompute + NLL/grad + read sums, per step"},
+                "e2e_fit_loop": {"value": world / fit_loop_s, "unit": "evals/s", "h2d_bytes_per_step": 9 * 8,
+                                 "d2h_bytes_per_step": 9 * 8,
+                                 "what": "events resident; parameters in, sums out (the fitter's per-evaluation path)"},
+                "mixed": mixed, "cpu_baseline": cpu, "clocks": clk.summary(),
+                "gpu_launches": args.steps, "nll_truth": float(-2.0 * res64[0])}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def C_stream(backend):
+    import ctypes as C
+    from morefit_gb300 import _lib as L
+    p = C.c_void_p()
+    L.check(L.lib.mf_context_stream(backend.handle, C.byref(p)))
+    return p.value
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--nevents", type=int, default=N_EVENTS)
+    ap.add_argument("--e2e-steps", type=int, default=100)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        ours(args)
+
+
+if __name__ == "__main__":
+    main()

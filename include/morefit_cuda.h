@@ -1,0 +1,240 @@
+/*
+ * morefit_cuda.h — C ABI of the GB300 (sm_103a) likelihood backend for MoreFit.
+ *
+ * Plain C: opaque handles, pointers and sizes, int status codes, no CUDA or
+ * C++ types in any signature. Every entry point returns MF_OK (0) or an
+ * MF_ERR_* code and never aborts the process; mf_last_error() returns the
+ * message of the calling thread's most recent failure.
+ *
+ * Each entry point below names the reference interface it replaces. The
+ * reference's backend interface is the abstract C++ class
+ * morefit::ComputeBlock<kernelT, evalT, seedT> (include/compute.hh:110-149)
+ * plus ComputeBackend (include/compute.hh:98-107). include/compute_cuda.hh
+ * implements those C++ classes on top of this ABI, so morefit::fitter,
+ * generator and toystudy run unchanged on it.
+ *
+ * Data layout on the device: an event buffer is structure-of-arrays, column k
+ * of a buffer with column stride S holds events [0, n) at element offset k*S
+ * (the EventVector layout of include/eventvector.hh:236-260, with the stride
+ * padded to a multiple of MF_COLUMN_ALIGN events so that every column starts
+ * on a 256-byte boundary).
+ */
+#ifndef MOREFIT_CUDA_H
+#define MOREFIT_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define MF_OK 0
+#define MF_ERR_INVALID 1      /* bad argument (null handle, size, type, layout) */
+#define MF_ERR_CUDA 2         /* a CUDA runtime call failed */
+#define MF_ERR_NVRTC 3        /* runtime compilation of a generated kernel failed */
+#define MF_ERR_PARSE 4        /* a kernel expression could not be parsed */
+#define MF_ERR_BUDGET 5       /* allocation would exceed the context's HBM budget */
+#define MF_ERR_NO_DEVICE 6    /* no CUDA device, or the device is not sm_103 */
+#define MF_ERR_UNSUPPORTED 7  /* valid request this build does not implement */
+#define MF_ERR_TIMEOUT 8      /* a bounded device wait gave up */
+
+/* ---- element types (kernelT of ComputeBlock<kernelT, evalT>) ---- */
+#define MF_F64 0
+#define MF_F32 1
+
+/* ---- kernel kinds (how MakeComputeKernel's kahan flag and MakeGenerateKernel map) ---- */
+#define MF_KERNEL_REDUCE 0    /* per-event values summed over events: MakeComputeKernel(kahan=true) */
+#define MF_KERNEL_STORE 1     /* per-event values stored as output columns: MakeComputeKernel(kahan=false) */
+#define MF_KERNEL_GENERATE 2  /* accept-reject event generation: MakeGenerateKernel */
+
+#define MF_COLUMN_ALIGN 64    /* column stride granularity, events */
+#define MF_MAX_PARAMS 512     /* parameter vector length limit per launch */
+#define MF_MAX_OUTPUTS 512    /* outputs (graphs) per kernel */
+
+typedef struct mf_context mf_context;
+typedef struct mf_buffer mf_buffer;
+typedef struct mf_kernel mf_kernel;
+
+/* Message of the calling thread's last failed call ("" if none). */
+const char* mf_last_error(void);
+
+/* Library version string. */
+const char* mf_version(void);
+
+/* Number of visible CUDA devices (0 without a GPU; never an error). */
+int mf_device_count(int* count);
+
+/* ---- context: one stream + scratch on one device ----
+ * Replaces ComputeBackend construction (include/compute.hh:98-107; the
+ * OpenCL backend's platform/device set-up, include/compute_opencl.hh:30-206).
+ * hbm_budget_bytes caps the bytes of buffers allocated through this context
+ * (0 = no cap). Calls on one context are serialised on its stream; use one
+ * context per host thread for concurrency. */
+int mf_context_create(int device, uint64_t hbm_budget_bytes, mf_context** out);
+int mf_context_destroy(mf_context* ctx);
+/* Bytes currently allocated through the context. */
+int mf_context_allocated(const mf_context* ctx, uint64_t* bytes);
+/* Blocks until all work queued on the context's stream has finished.
+ * Replaces ComputeBlock::Finish (include/compute.hh:146). */
+int mf_context_synchronize(mf_context* ctx);
+
+/* ---- device buffers ----
+ * Replace ComputeBlock::Setup{Input,Output,Parameter,Kahan,Seed}Buffer
+ * (include/compute.hh:114-126). */
+int mf_buffer_alloc(mf_context* ctx, uint64_t nbytes, mf_buffer** out);
+int mf_buffer_free(mf_buffer* buf);
+uint64_t mf_buffer_size(const mf_buffer* buf);
+/* Raw device address (for interop); the buffer keeps ownership. */
+void* mf_buffer_device_ptr(const mf_buffer* buf);
+/* Plain byte copies (synchronous with respect to the host). */
+int mf_buffer_h2d(mf_buffer* buf, uint64_t offset, const void* src, uint64_t nbytes);
+int mf_buffer_d2h(const mf_buffer* buf, uint64_t offset, void* dst, uint64_t nbytes);
+int mf_buffer_memset(mf_buffer* buf, int value);
+
+/* Column stride (events) used on the device for n events: n rounded up to a
+ * multiple of MF_COLUMN_ALIGN (at least MF_COLUMN_ALIGN). */
+uint64_t mf_column_stride(uint64_t nevents);
+
+/* Uploads an SoA event block with ncols columns of n events each, host
+ * column stride host_stride (events), into buf with device column stride
+ * dev_stride; the padding events of every column are zero-filled.
+ * elem_type: MF_F64 or MF_F32 (the host data's type; no conversion).
+ * Replaces ComputeBlock::CopyToInputBuffer (include/compute.hh:130). */
+int mf_events_upload(mf_buffer* buf, int elem_type, const void* host, uint32_t ncols, uint64_t n,
+                     uint64_t host_stride, uint64_t dev_stride);
+/* Reverse of mf_events_upload. Replaces CopyFromOutputBuffer
+ * (include/compute.hh:136). */
+int mf_events_download(const mf_buffer* buf, int elem_type, void* host, uint32_t ncols, uint64_t n,
+                       uint64_t host_stride, uint64_t dev_stride);
+/* Uploads n FP64 values converting them to FP32 on the fly when elem_type is
+ * MF_F32 (used to stage FP64 host events into an FP32 device layout). */
+int mf_events_upload_f64_as(mf_buffer* buf, int elem_type, const double* host, uint32_t ncols, uint64_t n,
+                            uint64_t host_stride, uint64_t dev_stride);
+
+/* ---- kernels ----
+ * Replaces ComputeBlock::MakeComputeKernel / MakeGenerateKernel
+ * (include/compute.hh:140-144; the reference emits C/OpenCL text around
+ * ComputeGraphNode::get_kernel() strings, include/compute_llvm.hh:535-750,
+ * include/compute_opencl.hh:646-805). The expression strings are exactly
+ * what get_kernel() prints (C syntax over input-column and parameter names,
+ * constants as "%.15e" literals). The library parses them, shares common
+ * subexpressions across all outputs, lowers them to CUDA C for the element
+ * type, and compiles the kernel with NVRTC for sm_103a (cached by source). */
+typedef struct mf_kernel_desc {
+  const char* name;                 /* kernel name (diagnostics) */
+  int kind;                         /* MF_KERNEL_REDUCE / STORE / GENERATE */
+  int elem_type;                    /* MF_F64 or MF_F32: storage and arithmetic type */
+  uint32_t n_inputs;                /* input column names, in buffer column order */
+  const char* const* input_names;
+  uint32_t n_params;                /* parameter names, in parameter-vector order */
+  const char* const* param_names;
+  uint32_t n_outputs;               /* one expression per output */
+  const char* const* exprs;
+  /* GENERATE only: n_outputs == 1 (the normalised density), the generated
+   * dimensions are the n_gen_dims names below with ranges [lo, hi). */
+  uint32_t n_gen_dims;
+  const char* const* gen_dim_names;
+  const double* gen_lo;
+  const double* gen_hi;
+  double maxprob;
+} mf_kernel_desc;
+
+int mf_kernel_build(mf_context* ctx, const mf_kernel_desc* desc, mf_kernel** out);
+int mf_kernel_free(mf_kernel* k);
+/* Copies the generated CUDA C source (NUL-terminated, truncated to len). */
+int mf_kernel_source(const mf_kernel* k, char* buf, size_t len, size_t* needed);
+/* Registers / spills / static shared memory reported by the compiler. */
+int mf_kernel_info(const mf_kernel* k, int* regs, int* spill_bytes, int* block_size, int* vec_width);
+
+/* REDUCE: sums[j] = sum over events i in [0, n) of output j, accumulated
+ * with per-thread partials, a warp/block tree and a compensated,
+ * fixed-order combine of the block partials in the last block of the grid
+ * (one launch, no host-side passes). FP64 kernels accumulate in FP64; FP32
+ * kernels keep Kahan-compensated FP32 partials per thread and promote them
+ * to FP64 at the warp level. Results are deterministic for a given n.
+ * params: n_params FP64 values (converted to the element type on the device
+ * side for FP32 kernels). input: column stride `stride` events; base and
+ * stride must satisfy the MF_COLUMN_ALIGN layout.
+ * Replaces SubmitKernel + Finish + CopyFromKahanBuffer
+ * (include/compute.hh:134-148, include/fitter.hh:1076-1096). */
+int mf_kernel_reduce(mf_kernel* k, const mf_buffer* input, uint64_t stride, uint64_t n, const double* params,
+                     uint32_t n_params, double* sums);
+
+/* Enqueues one REDUCE launch on the context's stream and returns without
+ * waiting; the n_outputs sums land in `out` at double offset
+ * out_index * n_outputs once the stream reaches them. Launches on one
+ * context run in stream order and share its scratch, so they never overlap
+ * each other. Pair with mf_context_synchronize (Finish). */
+int mf_kernel_reduce_async(mf_kernel* k, const mf_buffer* input, uint64_t stride, uint64_t n, const double* params,
+                           uint32_t n_params, mf_buffer* out, uint64_t out_index);
+
+/* Enqueues `count` REDUCE launches back to back on the context's stream
+ * without host round trips: launch i reads inputs[i] (column stride
+ * strides[i], ns[i] events) with parameter row i (params[i * n_params ...])
+ * and writes its sums to row i of `out`. Used to evaluate many datasets or
+ * parameter points per host call (several fits' requests, toy batches). */
+int mf_kernel_reduce_many(mf_kernel* k, uint32_t count, const mf_buffer* const* inputs, const uint64_t* strides,
+                          const uint64_t* ns, const double* params, uint32_t n_params, mf_buffer* out);
+
+/* The context's cudaStream_t, as an opaque pointer (interop: events, graphs). */
+int mf_context_stream(mf_context* ctx, void** stream);
+
+/* Ragged batched REDUCE over nseg independent event segments of one buffer
+ * (toy studies): segment s covers events [seg_begin[s], seg_begin[s] +
+ * seg_count[s]) of every column and uses parameter row s (params[s *
+ * n_params ...]); sums[s * n_outputs + j]. One launch for all segments. */
+int mf_kernel_reduce_segments(mf_kernel* k, const mf_buffer* input, uint64_t stride, uint32_t nseg,
+                              const uint64_t* seg_begin, const uint32_t* seg_count, const double* params,
+                              uint32_t n_params, double* sums);
+
+/* STORE: output column j of `output` (stride out_stride) receives output j
+ * for events [0, n). Replaces SubmitKernel for non-Kahan and precompute
+ * blocks (include/fitter.hh:345-375,704-712). */
+int mf_kernel_store(mf_kernel* k, const mf_buffer* input, uint64_t in_stride, uint64_t n, const double* params,
+                    uint32_t n_params, mf_buffer* output, uint64_t out_stride);
+
+/* GENERATE: accept-reject generation with one xoshiro128++ stream per
+ * generator thread, as the reference's accelerator generate kernel
+ * (include/compute_opencl.hh:425-645; seeds from include/generator.hh:115-135).
+ * seeds: SoA [4][nseeds] host array; thread t produces events
+ * [t*nper, min((t+1)*nper, n)) into output column d (stride out_stride) of
+ * `out`. Every thread gives up after max_tries proposals (returns
+ * MF_ERR_TIMEOUT) so a density that is never accepted cannot hang the GPU.
+ * Replaces SubmitKernel + Finish of a generate block. */
+int mf_kernel_generate(mf_kernel* k, const uint32_t* seeds, uint32_t nseeds, uint64_t n, uint64_t nper,
+                       const double* params, uint32_t n_params, mf_buffer* out, uint64_t out_stride,
+                       uint64_t max_tries);
+
+/* Host evaluation of parameter-only expressions (the hoisted parameter
+ * buffers "morefit_parambuffer_k" that the fitter evaluates before every
+ * launch). Replaces ComputeGraphNode::eval (include/graph.hh:193) as used by
+ * include/fitter.hh:1063-1072. out[i] = value of exprs[i]; an expression that
+ * names a variable not in `names` is an MF_ERR_PARSE error. */
+int mf_eval_expressions(uint32_t n_names, const char* const* names, const double* values, uint32_t n_exprs,
+                        const char* const* exprs, double* out);
+
+/* Seed rows for the accelerator generator (include/generator.hh:115-135):
+ * an xoshiro128++ state seeded like Xoshiro128pp::setSeed(seed)
+ * (include/random.hh:355-362), row t = the state after t jump() calls
+ * (include/random.hh:395-420). out is SoA [4][nrows]. */
+int mf_seed_rows(uint64_t seed, uint32_t nrows, uint32_t* out);
+
+/* Work partition of the reference's accelerator generator for n events with
+ * at most max_workitems generator threads (compute_opencl.hh:437-445,
+ * generator.hh:120-128; max_workitems 8192 is compute_options' default):
+ * *nper events per thread, *nseeds seed rows. */
+int mf_generate_partition(uint64_t n, uint32_t max_workitems, uint64_t* nper, uint32_t* nseeds);
+
+/* ---- diagnostics that need no GPU ----
+ * Lowers a kernel description to CUDA C without compiling it. */
+int mf_lower_source(const mf_kernel_desc* desc, char* buf, size_t len, size_t* needed);
+/* Lowers and compiles (NVRTC, sm_103a) without loading: reports registers
+ * and spill bytes per thread of the main entry. */
+int mf_compile_check(const mf_kernel_desc* desc, int* regs, int* spill_bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MOREFIT_CUDA_H */

@@ -1,0 +1,334 @@
+"""Python mirror of the reference's compute-backend interface on the CUDA C ABI.
+
+``CUDABackend`` and ``CUDABlock`` carry the method names, argument meaning
+and call order of ``morefit::ComputeBackend`` / ``morefit::ComputeBlock``
+(reference include/compute.hh:98-149), so a test or driver written against
+the reference's block interface reads the same here. Event buffers are
+numpy arrays of shape ``(ndims, nevents)`` (the SoA layout of EventVector,
+include/eventvector.hh:236-260). Kernels are the reference's
+``ComputeGraphNode::get_kernel()`` strings.
+
+Every call goes through ``libmorefit_cuda.so``; a failing call raises
+``MFError`` instead of the reference's ``assert(0)``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from typing import Sequence
+
+import numpy as np
+
+from . import _lib as L
+
+
+class CUDABackend:
+    """One device, one stream, an HBM budget (ComputeBackend, compute.hh:98-107)."""
+
+    def __init__(self, device: int = 0, hbm_budget_bytes: int = 0):
+        h = L.c_ctx()
+        L.check(L.lib.mf_context_create(device, hbm_budget_bytes, C.byref(h)))
+        self._h = h
+        self.device = device
+
+    def required_padding(self) -> int:
+        # The device layout pads each column internally; host EventVectors
+        # stay unpadded (fitter.hh:685-698 then leaves the data alone).
+        return 0
+
+    @property
+    def handle(self):
+        return self._h
+
+    def allocated(self) -> int:
+        v = C.c_uint64()
+        L.check(L.lib.mf_context_allocated(self._h, C.byref(v)))
+        return v.value
+
+    def synchronize(self) -> None:
+        L.check(L.lib.mf_context_synchronize(self._h))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            L.lib.mf_context_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class DeviceColumns:
+    """A device SoA event block: ``ncols`` columns of ``n`` events, padded stride."""
+
+    def __init__(self, backend: CUDABackend, elem: int):
+        self.backend = backend
+        self.elem = elem
+        self.buf = None
+        self.ncols = 0
+        self.n = 0
+        self.stride = 0
+
+    @property
+    def itemsize(self) -> int:
+        return 4 if self.elem == L.MF_F32 else 8
+
+    def ensure(self, ncols: int, n: int) -> None:
+        stride = int(L.lib.mf_column_stride(n))
+        need = max(1, ncols) * stride * self.itemsize
+        if self.buf is None or L.lib.mf_buffer_size(self.buf) < need:
+            self.free()
+            b = L.c_buf()
+            L.check(L.lib.mf_buffer_alloc(self.backend.handle, need, C.byref(b)))
+            self.buf = b
+        self.ncols, self.n, self.stride = ncols, n, stride
+
+    def upload(self, events: np.ndarray) -> None:
+        ev = np.ascontiguousarray(events)
+        if ev.ndim == 1:
+            ev = ev[None, :]
+        ncols, n = ev.shape
+        self.ensure(ncols, n)
+        if ev.dtype == np.float64 and self.elem == L.MF_F32:
+            L.check(L.lib.mf_events_upload_f64_as(self.buf, L.MF_F32, L.dptr(ev), ncols, n, n, self.stride))
+            return
+        want = np.float32 if self.elem == L.MF_F32 else np.float64
+        ev = np.ascontiguousarray(ev, dtype=want)
+        L.check(L.lib.mf_events_upload(self.buf, self.elem, ev.ctypes.data, ncols, n, n, self.stride))
+
+    def download(self) -> np.ndarray:
+        out = np.empty((self.ncols, self.n), dtype=np.float32 if self.elem == L.MF_F32 else np.float64)
+        L.check(L.lib.mf_events_download(self.buf, self.elem, out.ctypes.data, self.ncols, self.n, self.n,
+                                         self.stride))
+        return out
+
+    def free(self) -> None:
+        if self.buf is not None:
+            L.lib.mf_buffer_free(self.buf)
+            self.buf = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+@dataclass
+class Kernel:
+    handle: object
+    kind: int
+    nout: int
+    nparams: int
+
+    def source(self) -> str:
+        need = C.c_size_t()
+        L.check(L.lib.mf_kernel_source(self.handle, None, 0, C.byref(need)))
+        buf = C.create_string_buffer(need.value)
+        L.check(L.lib.mf_kernel_source(self.handle, buf, need.value, None))
+        return buf.value.decode()
+
+    def info(self) -> dict:
+        r, s, b, v = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        L.check(L.lib.mf_kernel_info(self.handle, C.byref(r), C.byref(s), C.byref(b), C.byref(v)))
+        return {"registers": r.value, "spill_bytes": s.value, "block": b.value, "vec": v.value}
+
+
+def make_desc(name: str, kind: int, elem: int, inputs: Sequence[str], params: Sequence[str],
+              exprs: Sequence[str], gen=None):
+    keep = {"inputs": L.cstrings(list(inputs)), "params": L.cstrings(list(params)),
+            "exprs": L.cstrings(list(exprs)), "name": name.encode()}
+    d = L.KernelDesc()
+    d.name = keep["name"]
+    d.kind = kind
+    d.elem_type = elem
+    d.n_inputs = len(inputs)
+    d.input_names = C.cast(keep["inputs"], L.c_char_pp)
+    d.n_params = len(params)
+    d.param_names = C.cast(keep["params"], L.c_char_pp)
+    d.n_outputs = len(exprs)
+    d.exprs = C.cast(keep["exprs"], L.c_char_pp)
+    if gen is not None:
+        dims, lo, hi, maxprob = gen
+        keep["gd"] = L.cstrings(list(dims))
+        keep["lo"] = np.ascontiguousarray(lo, dtype=np.float64)
+        keep["hi"] = np.ascontiguousarray(hi, dtype=np.float64)
+        d.n_gen_dims = len(dims)
+        d.gen_dim_names = C.cast(keep["gd"], L.c_char_pp)
+        d.gen_lo = L.dptr(keep["lo"])
+        d.gen_hi = L.dptr(keep["hi"])
+        d.maxprob = float(maxprob)
+    return d, keep
+
+
+def build_kernel(backend: CUDABackend, name: str, kind: int, elem: int, inputs, params, exprs, gen=None) -> Kernel:
+    d, keep = make_desc(name, kind, elem, inputs, params, exprs, gen)
+    h = L.c_ker()
+    L.check(L.lib.mf_kernel_build(backend.handle, C.byref(d), C.byref(h)))
+    del keep
+    return Kernel(h, kind, len(exprs), len(params))
+
+
+def lower_source(name: str, kind: int, elem: int, inputs, params, exprs, gen=None) -> str:
+    """CUDA C the library generates for these expressions (no GPU needed)."""
+    d, keep = make_desc(name, kind, elem, inputs, params, exprs, gen)
+    need = C.c_size_t()
+    L.check(L.lib.mf_lower_source(C.byref(d), None, 0, C.byref(need)))
+    buf = C.create_string_buffer(need.value)
+    L.check(L.lib.mf_lower_source(C.byref(d), buf, need.value, None))
+    return buf.value.decode()
+
+
+def compile_check(name: str, kind: int, elem: int, inputs, params, exprs, gen=None) -> dict:
+    """NVRTC-compiles the lowered kernel for sm_103a without a GPU."""
+    d, keep = make_desc(name, kind, elem, inputs, params, exprs, gen)
+    r, s = C.c_int(), C.c_int()
+    L.check(L.lib.mf_compile_check(C.byref(d), C.byref(r), C.byref(s)))
+    return {"registers": r.value, "spill_bytes": s.value}
+
+
+def eval_expressions(names: Sequence[str], values: Sequence[float], exprs: Sequence[str]) -> np.ndarray:
+    """Host evaluation of parameter-only expressions (ComputeGraphNode::eval)."""
+    v = np.ascontiguousarray(values, dtype=np.float64)
+    out = np.zeros(max(1, len(exprs)))
+    L.check(L.lib.mf_eval_expressions(len(names), C.cast(L.cstrings(list(names)), L.c_char_pp), L.dptr(v),
+                                      len(exprs), C.cast(L.cstrings(list(exprs)), L.c_char_pp), L.dptr(out)))
+    return out[: len(exprs)]
+
+
+class CUDABlock:
+    """ComputeBlock<kernelT, evalT> over the CUDA C ABI (compute.hh:110-149).
+
+    ``kernelT`` is ``np.float64`` (plain FP64) or ``np.float32`` (mixed
+    precision: FP32 storage and per-event arithmetic, FP64 sums).
+    """
+
+    def __init__(self, backend: CUDABackend, kernelT=np.float64):
+        self.backend = backend
+        self.elem = L.MF_F32 if np.dtype(kernelT) == np.float32 else L.MF_F64
+        self.kernelT = np.dtype(kernelT)
+        self.input = DeviceColumns(backend, self.elem)
+        self.output = DeviceColumns(backend, self.elem)
+        self.params = np.zeros(0)
+        self.nevents = 0
+        self.kernel: Kernel | None = None
+        self.kahan = False
+        self.nout = 0
+        self._sums = np.zeros(0)
+        self._seeds = None
+        self._gen = None
+
+    # --- buffers (compute.hh:114-128) ---
+    def SetupInputBuffer(self, arg, use_data_in: bool = False) -> bool:
+        if isinstance(arg, CUDABlock):  # chained: share the other block's device columns
+            self.input = arg.input if use_data_in else arg.output
+        return True
+
+    def SetupSeedBuffer(self, nbytes: int) -> bool:
+        return True
+
+    def SetupParameterBuffer(self, nbytes: int) -> bool:
+        return True
+
+    def SetupOutputBuffer(self, nbytes: int) -> bool:
+        return True
+
+    def SetupKahanBuffer(self, nbytes: int) -> bool:
+        self._sums = np.zeros(nbytes // 8)
+        return True
+
+    def SetNevents(self, nevents: int, nevents_padded: int = -1) -> bool:
+        self.nevents = int(nevents)
+        return True
+
+    # --- copies (compute.hh:130-138) ---
+    def CopyToInputBuffer(self, events: np.ndarray) -> bool:
+        self.input.upload(events)
+        self.nevents = self.input.n
+        return True
+
+    def CopyToSeedBuffer(self, seeds: np.ndarray) -> bool:
+        self._seeds = np.ascontiguousarray(seeds, dtype=np.uint32)
+        return True
+
+    def CopyToParameterBuffer(self, params) -> bool:
+        self.params = np.ascontiguousarray(params, dtype=np.float64)
+        return True
+
+    def CopyFromOutputBuffer(self) -> np.ndarray:
+        return self.output.download()
+
+    def CopyFromKahanBuffer(self) -> np.ndarray:
+        return self._sums.copy()
+
+    # --- kernels (compute.hh:140-148) ---
+    def MakeComputeKernel(self, name: str, nevents: int, input_signature: Sequence[str],
+                          output_signature: Sequence[str], params: Sequence[str], graphs: Sequence[str],
+                          kahan_summation: bool = False) -> bool:
+        if len(output_signature) != len(graphs):
+            raise ValueError("output_signature and graphs differ in length (compute_opencl.hh:707)")
+        self.kahan = bool(kahan_summation)
+        self.nout = len(graphs)
+        kind = L.MF_KERNEL_REDUCE if self.kahan else L.MF_KERNEL_STORE
+        self.kernel = build_kernel(self.backend, name, kind, self.elem, input_signature, params, graphs)
+        self._sums = np.zeros(self.nout)
+        self.nevents = int(nevents)
+        return True
+
+    def MakeGenerateKernel(self, name: str, nevents: int, input_signature, output_signature: Sequence[str],
+                           params, graphs: Sequence[str], maxprob: float = 1.0, ranges=None) -> bool:
+        dims = [d[0] if isinstance(d, tuple) else d for d in output_signature]
+        lo = [r[0] for r in ranges]
+        hi = [r[1] for r in ranges]
+        self.kernel = build_kernel(self.backend, name, L.MF_KERNEL_GENERATE, self.elem, [], params, graphs,
+                                   gen=(dims, lo, hi, maxprob))
+        self._gen = len(dims)
+        self.nevents = int(nevents)
+        return True
+
+    def SubmitKernel(self, nper: int | None = None, max_tries: int | None = None) -> bool:
+        k = self.kernel
+        if k is None:
+            raise RuntimeError("SubmitKernel before MakeComputeKernel")
+        p = self.params if self.params.size else np.zeros(1)
+        if k.kind == L.MF_KERNEL_REDUCE:
+            sums = np.zeros(k.nout)
+            L.check(L.lib.mf_kernel_reduce(k.handle, self.input.buf, self.input.stride, self.nevents, L.dptr(p),
+                                           k.nparams, L.dptr(sums)))
+            self._sums = sums
+        elif k.kind == L.MF_KERNEL_STORE:
+            self.output.ensure(k.nout, self.nevents)
+            L.check(L.lib.mf_kernel_store(k.handle, self.input.buf, self.input.stride, self.nevents, L.dptr(p),
+                                          k.nparams, self.output.buf, self.output.stride))
+        else:
+            nseeds = self._seeds.shape[-1] if self._seeds.ndim == 2 else self._seeds.size // 4
+            per = nper if nper else -(-self.nevents // nseeds)
+            if max_tries is None:  # every thread gives up after 10^4 proposals per event it owns
+                max_tries = 10000 * per
+            self.output.ensure(self._gen, self.nevents)
+            L.check(L.lib.mf_kernel_generate(k.handle, self._seeds.ctypes.data_as(C.POINTER(C.c_uint32)), nseeds,
+                                             self.nevents, per, L.dptr(p), k.nparams, self.output.buf,
+                                             self.output.stride, max_tries))
+        return True
+
+    def Finish(self) -> bool:
+        self.backend.synchronize()
+        return True
+
+    def ProvidesKahan(self) -> bool:
+        return True
+
+    # --- batched ragged segments (toy studies) ---
+    def SubmitSegments(self, seg_begin, seg_count, params_rows) -> np.ndarray:
+        k = self.kernel
+        b = np.ascontiguousarray(seg_begin, dtype=np.uint64)
+        c = np.ascontiguousarray(seg_count, dtype=np.uint32)
+        pr = np.ascontiguousarray(params_rows, dtype=np.float64).reshape(len(b), -1)
+        out = np.zeros((len(b), k.nout))
+        L.check(L.lib.mf_kernel_reduce_segments(k.handle, self.input.buf, self.input.stride, len(b),
+                                                b.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                                c.ctypes.data_as(C.POINTER(C.c_uint32)), L.dptr(pr), k.nparams,
+                                                L.dptr(out)))
+        return out

@@ -1,0 +1,97 @@
+// Lowering of MoreFit kernel expressions to CUDA C.
+//
+// Input: the C-syntax strings that ComputeGraphNode::get_kernel() prints
+// (reference include/graph.hh: Sum "(a+b)" :314-320, Prod "(a*b)" :548-554,
+// Exp/Log/Sqrt/Sin/... "f(x)" :786,987,1350,1451, Inv "1.0/(x)" :886, Neg
+// "-(x)" :1253, Pow "pow(a,b)" :1094-1099, Conditional "((x==0.0) ? a : b)"
+// :2270-2290, Constant "%.15e" :245-254, Variable name :2172).
+//
+// The strings of all outputs of one kernel are parsed into one hash-consed
+// DAG, so a subexpression that several outputs share (the density p, its
+// reciprocal, exp(...) terms) is evaluated once per event. Divisions become
+// multiplications by a shared reciprocal. Nodes that depend only on
+// parameters and constants are evaluated once per thread before the event
+// loop. Only the input columns the expressions reference are loaded.
+#ifndef MF_LOWER_H
+#define MF_LOWER_H
+
+#include <cstdint>
+#include <map>
+#include <string>
+#include <vector>
+
+namespace mf {
+
+enum class Op : uint8_t {
+  Const, Input, Param, Add, Sub, Mul, Neg, Rcp, Div, Exp, Log, Sqrt, Sin, Cos, Tan, Asin, Acos, Atan, Erf,
+  Pow, Cmp, Select
+};
+enum class CmpOp : uint8_t { Eq, Ne, Gt, Lt, Ge, Le };
+
+struct Node {
+  Op op;
+  CmpOp cmp = CmpOp::Eq;
+  double value = 0.0;  // Const
+  int index = -1;      // Input column / Param slot
+  int a = -1, b = -1, c = -1;
+  bool uniform = true;  // depends on no input column
+};
+
+class Dag {
+ public:
+  Dag(const std::vector<std::string>& inputs, const std::vector<std::string>& params);
+  // Parses one expression; returns the root node id. Throws std::runtime_error.
+  int parse(const std::string& expr);
+  const std::vector<Node>& nodes() const { return nodes_; }
+  int input_count() const { return int(inputs_.size()); }
+  const std::vector<std::string>& input_names() const { return inputs_; }
+  const std::vector<std::string>& param_names() const { return params_; }
+  // Node constructors with local simplification and hash-consing.
+  int constant(double v);
+  int unary(Op op, int a);
+  int binary(Op op, int a, int b);
+  int compare(CmpOp cmp, int a, int b);
+  int select(int cond, int a, int b);
+  // Host evaluation (parameter-only expressions, tests).
+  double eval(int id, const std::vector<double>& inputs, const std::vector<double>& params) const;
+
+ private:
+  int intern(const Node& n);
+  std::vector<Node> nodes_;
+  std::map<std::string, int> table_;
+  std::vector<std::string> inputs_, params_;
+  std::map<std::string, int> input_idx_, param_idx_;
+};
+
+struct LoweredKernel {
+  std::string source;            // complete CUDA C translation unit
+  std::string entry;             // __global__ function name
+  std::vector<int> used_inputs;  // input columns read by the kernel
+  int vec = 1;                   // events per thread per iteration
+  int block = 256;
+};
+
+enum class Elem { F64, F32 };
+enum class Kind { Reduce, Store, Generate };
+
+struct GenerateSpec {
+  std::vector<std::string> dims;
+  std::vector<double> lo, hi;
+  double maxprob = 1.0;
+};
+
+// Builds the kernel source for the given outputs.
+LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::vector<std::string>& inputs,
+                    const std::vector<std::string>& params, const std::vector<std::string>& exprs,
+                    const GenerateSpec* gen = nullptr);
+
+// Counts per-event operations of a lowered expression set (diagnostics).
+struct OpCount {
+  int nodes = 0, per_event = 0, uniform = 0, transcendental = 0, divisions = 0;
+};
+OpCount count_ops(const std::vector<std::string>& inputs, const std::vector<std::string>& params,
+                  const std::vector<std::string>& exprs);
+
+}  // namespace mf
+
+#endif

@@ -1,0 +1,865 @@
+// Runtime of the MoreFit CUDA backend: contexts, device buffers, NVRTC
+// compilation of lowered kernels, and launches (C ABI in morefit_cuda.h).
+//
+// Everything here is host code on the CUDA runtime API; the kernels are the
+// generated translation units of mf_lower.cpp, compiled by NVRTC to sm_103a
+// cubins and loaded with cudaLibraryLoadData. No entry point aborts: errors
+// become MF_ERR_* codes with a thread-local message.
+#include <cuda_runtime.h>
+#include <nvrtc.h>
+
+#include <unistd.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cctype>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <functional>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <sstream>
+#include <string>
+#include <sys/stat.h>
+#include <vector>
+
+#include "../../include/morefit_cuda.h"
+#include "mf_lower.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+#define MF_CUDA_TRY(call)                                                                                  \
+  do {                                                                                                     \
+    cudaError_t e_ = (call);                                                                               \
+    if (e_ != cudaSuccess) return fail(MF_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+// ------------------------------------------------------------ compile cache --
+struct CompiledImage {
+  std::vector<char> cubin;
+  int regs = -1, spill = -1;
+  std::string log;
+};
+
+std::mutex g_cache_mu;
+std::map<std::string, std::shared_ptr<CompiledImage>> g_cache;  // key: source
+
+uint64_t fnv1a64(const std::string& s) {
+  uint64_t h = 1469598103934665603ULL;
+  for (unsigned char c : s) {
+    h ^= c;
+    h *= 1099511628211ULL;
+  }
+  return h;
+}
+
+std::string cache_dir() {
+  const char* d = std::getenv("MOREFIT_CUDA_CACHE");
+  if (d && *d) return d;
+  const char* x = std::getenv("XDG_CACHE_HOME");
+  if (x && *x) return std::string(x) + "/morefit_gb300";
+  const char* h = std::getenv("HOME");
+  return std::string(h ? h : "/tmp") + "/.cache/morefit_gb300";
+}
+
+void parse_ptxas_log(const std::string& log, int& regs, int& spill) {
+  // "ptxas info    : Used 40 registers, ..." and "... bytes spill stores"
+  size_t p = log.find("Used ");
+  if (p != std::string::npos) regs = std::atoi(log.c_str() + p + 5);
+  size_t q = log.find(" bytes spill stores");
+  if (q != std::string::npos) {
+    size_t b = q;
+    while (b > 0 && (std::isdigit((unsigned char)log[b - 1]))) b--;
+    spill = std::atoi(log.c_str() + b);
+  }
+}
+
+int compile_source(const std::string& src, const std::string& name, std::shared_ptr<CompiledImage>& out) {
+  {
+    std::lock_guard<std::mutex> lk(g_cache_mu);
+    auto it = g_cache.find(src);
+    if (it != g_cache.end()) {
+      out = it->second;
+      return MF_OK;
+    }
+  }
+  auto img = std::make_shared<CompiledImage>();
+  char hex[32];
+  std::snprintf(hex, sizeof hex, "%016llx", (unsigned long long)fnv1a64(src));
+  const std::string dir = cache_dir();
+  const std::string base = dir + "/k" + hex + "_sm103a";
+  bool from_disk = false;
+  if (!std::getenv("MOREFIT_CUDA_NOCACHE")) {
+    std::ifstream f(base + ".cubin", std::ios::binary);
+    std::ifstream s(base + ".src", std::ios::binary);
+    if (f && s) {
+      std::string cached_src((std::istreambuf_iterator<char>(s)), std::istreambuf_iterator<char>());
+      if (cached_src == src) {
+        img->cubin.assign((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+        std::ifstream l(base + ".log");
+        if (l) img->log.assign((std::istreambuf_iterator<char>(l)), std::istreambuf_iterator<char>());
+        parse_ptxas_log(img->log, img->regs, img->spill);
+        from_disk = !img->cubin.empty();
+      }
+    }
+  }
+  if (!from_disk) {
+    nvrtcProgram prog;
+    nvrtcResult r = nvrtcCreateProgram(&prog, src.c_str(), (name + ".cu").c_str(), 0, nullptr, nullptr);
+    if (r != NVRTC_SUCCESS) return fail(MF_ERR_NVRTC, std::string("nvrtcCreateProgram: ") + nvrtcGetErrorString(r));
+    const char* opts[] = {"--gpu-architecture=sm_103a", "--std=c++17", "--generate-line-info",
+                          "--ptxas-options=-v", "--fmad=true"};
+    r = nvrtcCompileProgram(prog, int(sizeof(opts) / sizeof(opts[0])), opts);
+    size_t logsz = 0;
+    nvrtcGetProgramLogSize(prog, &logsz);
+    std::string log(logsz, '\0');
+    if (logsz) nvrtcGetProgramLog(prog, &log[0]);
+    img->log = log;
+    if (r != NVRTC_SUCCESS) {
+      nvrtcDestroyProgram(&prog);
+      return fail(MF_ERR_NVRTC, "NVRTC compile of '" + name + "' failed: " + log.substr(0, 4000));
+    }
+    size_t cubsz = 0;
+    nvrtcGetCUBINSize(prog, &cubsz);
+    img->cubin.resize(cubsz);
+    nvrtcGetCUBIN(prog, img->cubin.data());
+    nvrtcDestroyProgram(&prog);
+    parse_ptxas_log(log, img->regs, img->spill);
+    if (!std::getenv("MOREFIT_CUDA_NOCACHE")) {
+      std::string cmd_dir = dir;
+      // best effort: create the cache directory chain
+      for (size_t p = 1; p <= cmd_dir.size(); p++)
+        if (p == cmd_dir.size() || cmd_dir[p] == '/') ::mkdir(cmd_dir.substr(0, p).c_str(), 0755);
+      std::string tmp = base + ".tmp" + std::to_string(::getpid());
+      std::ofstream(tmp + ".src", std::ios::binary) << src;
+      std::ofstream(tmp + ".log", std::ios::binary) << log;
+      {
+        std::ofstream c(tmp + ".cubin", std::ios::binary);
+        c.write(img->cubin.data(), std::streamsize(img->cubin.size()));
+      }
+      std::rename((tmp + ".src").c_str(), (base + ".src").c_str());
+      std::rename((tmp + ".log").c_str(), (base + ".log").c_str());
+      std::rename((tmp + ".cubin").c_str(), (base + ".cubin").c_str());
+    }
+  }
+  std::lock_guard<std::mutex> lk(g_cache_mu);
+  g_cache[src] = img;
+  out = img;
+  return MF_OK;
+}
+
+}  // namespace
+
+// ----------------------------------------------------------------- objects --
+struct mf_context {
+  // Owner reference plus one per live buffer and kernel: the context (stream,
+  // scratch) outlives everything allocated through it, whatever order the
+  // caller releases handles in.
+  std::atomic<int> refs{1};
+  bool destroyed = false;
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  uint64_t budget = 0;
+  std::atomic<uint64_t> allocated{0};
+  // scratch for the grid-level combine of REDUCE kernels
+  double* partials = nullptr;
+  size_t partials_cap = 0;  // doubles
+  unsigned* counter = nullptr;
+  unsigned* status = nullptr;
+  // mapped pinned host memory the kernels write results into
+  double* out_host = nullptr;
+  double* out_dev = nullptr;
+  size_t out_cap = 0;  // doubles
+  // device staging for segment tables and parameter rows
+  void* stage_dev = nullptr;
+  size_t stage_cap = 0;
+};
+
+struct mf_buffer {
+  mf_context* ctx = nullptr;
+  void* ptr = nullptr;
+  uint64_t size = 0;
+};
+
+struct mf_kernel {
+  mf_context* ctx = nullptr;
+  std::string name;
+  int kind = MF_KERNEL_REDUCE;
+  int elem = MF_F64;
+  uint32_t n_inputs = 0, n_params = 0, n_outputs = 0, n_gen_dims = 0;
+  mf::LoweredKernel lowered;
+  std::shared_ptr<CompiledImage> image;
+  cudaLibrary_t lib = nullptr;
+  cudaKernel_t fn = nullptr;
+  cudaKernel_t fn_seg = nullptr;
+  int blocks_per_sm = 1;
+  int max_input = -1;
+  bool holds_ref = false;  // counted in ctx->refs
+};
+
+namespace mfi {
+int launch_reduce(mf_kernel* k, const void* data, uint64_t stride, uint64_t n, const double* params,
+                  double* partials, unsigned* counter, double* out, cudaStream_t stream, int grid_cap);
+}
+
+// ---------------------------------------------------------------- helpers --
+namespace {
+
+void release_context(mf_context* c) {
+  if (!c) return;
+  if (c->refs.fetch_sub(1) != 1) return;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  if (c->partials) cudaFree(c->partials);
+  if (c->counter) cudaFree(c->counter);
+  if (c->out_host) cudaFreeHost(c->out_host);
+  if (c->stage_dev) cudaFree(c->stage_dev);
+  cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+size_t elem_size(int e) { return e == MF_F32 ? 4 : 8; }
+
+int ensure_scratch(mf_context* c, size_t partial_doubles, size_t out_doubles) {
+  if (partial_doubles > c->partials_cap) {
+    if (c->partials) cudaFree(c->partials);
+    c->partials = nullptr;
+    size_t cap = std::max<size_t>(partial_doubles, 1 << 16);
+    MF_CUDA_TRY(cudaMalloc(&c->partials, cap * sizeof(double)));
+    c->partials_cap = cap;
+  }
+  if (out_doubles > c->out_cap) {
+    if (c->out_host) cudaFreeHost(c->out_host);
+    c->out_host = nullptr;
+    size_t cap = std::max<size_t>(out_doubles, 4096);
+    MF_CUDA_TRY(cudaHostAlloc(reinterpret_cast<void**>(&c->out_host), cap * sizeof(double), cudaHostAllocMapped));
+    MF_CUDA_TRY(cudaHostGetDevicePointer(reinterpret_cast<void**>(&c->out_dev), c->out_host, 0));
+    c->out_cap = cap;
+  }
+  return MF_OK;
+}
+
+int ensure_stage(mf_context* c, size_t bytes) {
+  if (bytes > c->stage_cap) {
+    if (c->stage_dev) cudaFree(c->stage_dev);
+    c->stage_dev = nullptr;
+    size_t cap = std::max<size_t>(bytes, 1 << 20);
+    MF_CUDA_TRY(cudaMalloc(&c->stage_dev, cap));
+    c->stage_cap = cap;
+  }
+  return MF_OK;
+}
+
+int check_layout(const mf_kernel* k, const mf_buffer* in, uint64_t stride, uint64_t n) {
+  if (!in || !in->ptr) return fail(MF_ERR_INVALID, "input buffer is null");
+  if (stride < n) return fail(MF_ERR_INVALID, "column stride smaller than the number of events");
+  if (k->kind == MF_KERNEL_REDUCE && (stride % uint64_t(std::max(1, k->lowered.vec)) != 0))
+    return fail(MF_ERR_INVALID, "column stride is not a multiple of the kernel's vector width");
+  if ((reinterpret_cast<uintptr_t>(in->ptr) & 15u) != 0) return fail(MF_ERR_INVALID, "input buffer not 16-byte aligned");
+  const uint64_t need = uint64_t(k->max_input + 1) * stride * elem_size(k->elem);
+  if (k->max_input >= 0 && need > in->size)
+    return fail(MF_ERR_INVALID, "input buffer smaller than columns x stride (" + std::to_string(need) + " > " +
+                                    std::to_string(in->size) + " bytes)");
+  return MF_OK;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ C ABI --
+extern "C" {
+
+const char* mf_last_error(void) { return g_last_error.c_str(); }
+
+const char* mf_version(void) { return "morefit_gb300 0.1 (sm_103a, NVRTC)"; }
+
+int mf_device_count(int* count) {
+  if (!count) return fail(MF_ERR_INVALID, "count is null");
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    n = 0;
+  }
+  *count = n;
+  return MF_OK;
+}
+
+int mf_context_create(int device, uint64_t hbm_budget_bytes, mf_context** out) {
+  if (!out) return fail(MF_ERR_INVALID, "out is null");
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    return fail(MF_ERR_NO_DEVICE, "no CUDA device visible");
+  }
+  if (device < 0 || device >= n) return fail(MF_ERR_INVALID, "device index out of range");
+  MF_CUDA_TRY(cudaSetDevice(device));
+  cudaDeviceProp prop;
+  MF_CUDA_TRY(cudaGetDeviceProperties(&prop, device));
+  if (prop.major != 10 || prop.minor != 3)
+    return fail(MF_ERR_NO_DEVICE, std::string("device is sm_") + std::to_string(prop.major) +
+                                      std::to_string(prop.minor) + ", this build targets sm_103a (GB300)");
+  auto c = std::make_unique<mf_context>();
+  c->device = device;
+  c->num_sms = prop.multiProcessorCount;
+  c->budget = hbm_budget_bytes;
+  MF_CUDA_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  MF_CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&c->counter), 2 * sizeof(unsigned)));
+  MF_CUDA_TRY(cudaMemset(c->counter, 0, 2 * sizeof(unsigned)));
+  c->status = c->counter + 1;
+  int rc = ensure_scratch(c.get(), size_t(c->num_sms) * 8 * 64, 4096);
+  if (rc) return rc;
+  *out = c.release();
+  return MF_OK;
+}
+
+int mf_context_destroy(mf_context* c) {
+  if (!c) return MF_OK;
+  if (c->destroyed) return fail(MF_ERR_INVALID, "context destroyed twice");
+  c->destroyed = true;
+  release_context(c);
+  return MF_OK;
+}
+
+int mf_context_allocated(const mf_context* c, uint64_t* bytes) {
+  if (!c || !bytes) return fail(MF_ERR_INVALID, "null argument");
+  *bytes = c->allocated.load();
+  return MF_OK;
+}
+
+int mf_context_synchronize(mf_context* c) {
+  if (!c) return fail(MF_ERR_INVALID, "context is null");
+  MF_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return MF_OK;
+}
+
+int mf_buffer_alloc(mf_context* c, uint64_t nbytes, mf_buffer** out) {
+  if (!c || !out) return fail(MF_ERR_INVALID, "null argument");
+  *out = nullptr;
+  const uint64_t rounded = (nbytes + 255) & ~uint64_t(255);
+  if (c->budget && c->allocated.load() + rounded > c->budget)
+    return fail(MF_ERR_BUDGET, "allocation of " + std::to_string(rounded) + " bytes exceeds the HBM budget (" +
+                                   std::to_string(c->allocated.load()) + " of " + std::to_string(c->budget) +
+                                   " bytes in use)");
+  MF_CUDA_TRY(cudaSetDevice(c->device));
+  auto b = std::make_unique<mf_buffer>();
+  b->ctx = c;
+  b->size = nbytes;
+  MF_CUDA_TRY(cudaMalloc(&b->ptr, std::max<uint64_t>(rounded, 256)));
+  c->allocated += rounded;
+  c->refs++;
+  *out = b.release();
+  return MF_OK;
+}
+
+int mf_buffer_free(mf_buffer* b) {
+  if (!b) return MF_OK;
+  mf_context* c = b->ctx;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  cudaFree(b->ptr);
+  c->allocated -= (b->size + 255) & ~uint64_t(255);
+  delete b;
+  release_context(c);
+  return MF_OK;
+}
+
+uint64_t mf_buffer_size(const mf_buffer* b) { return b ? b->size : 0; }
+
+void* mf_buffer_device_ptr(const mf_buffer* b) { return b ? b->ptr : nullptr; }
+
+int mf_buffer_h2d(mf_buffer* b, uint64_t off, const void* src, uint64_t nbytes) {
+  if (!b || (!src && nbytes)) return fail(MF_ERR_INVALID, "null argument");
+  if (off + nbytes > b->size) return fail(MF_ERR_INVALID, "copy beyond the end of the buffer");
+  MF_CUDA_TRY(cudaSetDevice(b->ctx->device));
+  MF_CUDA_TRY(cudaMemcpyAsync(static_cast<char*>(b->ptr) + off, src, nbytes, cudaMemcpyHostToDevice, b->ctx->stream));
+  MF_CUDA_TRY(cudaStreamSynchronize(b->ctx->stream));
+  return MF_OK;
+}
+
+int mf_buffer_d2h(const mf_buffer* b, uint64_t off, void* dst, uint64_t nbytes) {
+  if (!b || (!dst && nbytes)) return fail(MF_ERR_INVALID, "null argument");
+  if (off + nbytes > b->size) return fail(MF_ERR_INVALID, "copy beyond the end of the buffer");
+  MF_CUDA_TRY(cudaSetDevice(b->ctx->device));
+  MF_CUDA_TRY(cudaMemcpyAsync(dst, static_cast<const char*>(b->ptr) + off, nbytes, cudaMemcpyDeviceToHost,
+                              b->ctx->stream));
+  MF_CUDA_TRY(cudaStreamSynchronize(b->ctx->stream));
+  return MF_OK;
+}
+
+int mf_buffer_memset(mf_buffer* b, int value) {
+  if (!b) return fail(MF_ERR_INVALID, "null buffer");
+  MF_CUDA_TRY(cudaSetDevice(b->ctx->device));
+  MF_CUDA_TRY(cudaMemsetAsync(b->ptr, value, b->size, b->ctx->stream));
+  MF_CUDA_TRY(cudaStreamSynchronize(b->ctx->stream));
+  return MF_OK;
+}
+
+uint64_t mf_column_stride(uint64_t n) {
+  const uint64_t a = MF_COLUMN_ALIGN;
+  return std::max<uint64_t>(a, (n + a - 1) / a * a);
+}
+
+static int events_copy(bool up, mf_buffer* b, int elem, void* host, uint32_t ncols, uint64_t n, uint64_t hs,
+                       uint64_t ds) {
+  if (!b || (!host && n && ncols)) return fail(MF_ERR_INVALID, "null argument");
+  if (elem != MF_F64 && elem != MF_F32) return fail(MF_ERR_INVALID, "element type must be MF_F64 or MF_F32");
+  const size_t es = elem_size(elem);
+  if (hs < n || ds < n) return fail(MF_ERR_INVALID, "stride smaller than the number of events");
+  if (uint64_t(ncols) * ds * es > b->size) return fail(MF_ERR_INVALID, "buffer smaller than ncols x stride");
+  if (ncols == 0) return MF_OK;
+  MF_CUDA_TRY(cudaSetDevice(b->ctx->device));
+  if (up) {
+    if (n)
+      MF_CUDA_TRY(cudaMemcpy2DAsync(b->ptr, ds * es, host, hs * es, n * es, ncols, cudaMemcpyHostToDevice,
+                                    b->ctx->stream));
+    if (ds > n)
+      MF_CUDA_TRY(cudaMemset2DAsync(static_cast<char*>(b->ptr) + n * es, ds * es, 0, (ds - n) * es, ncols,
+                                    b->ctx->stream));
+  } else if (n) {
+    MF_CUDA_TRY(cudaMemcpy2DAsync(host, hs * es, b->ptr, ds * es, n * es, ncols, cudaMemcpyDeviceToHost,
+                                  b->ctx->stream));
+  }
+  MF_CUDA_TRY(cudaStreamSynchronize(b->ctx->stream));
+  return MF_OK;
+}
+
+int mf_events_upload(mf_buffer* b, int elem, const void* host, uint32_t ncols, uint64_t n, uint64_t hs, uint64_t ds) {
+  return events_copy(true, b, elem, const_cast<void*>(host), ncols, n, hs, ds);
+}
+
+int mf_events_download(const mf_buffer* b, int elem, void* host, uint32_t ncols, uint64_t n, uint64_t hs,
+                       uint64_t ds) {
+  return events_copy(false, const_cast<mf_buffer*>(b), elem, host, ncols, n, hs, ds);
+}
+
+int mf_events_upload_f64_as(mf_buffer* b, int elem, const double* host, uint32_t ncols, uint64_t n, uint64_t hs,
+                            uint64_t ds) {
+  if (elem == MF_F64) return mf_events_upload(b, elem, host, ncols, n, hs, ds);
+  if (elem != MF_F32) return fail(MF_ERR_INVALID, "element type must be MF_F64 or MF_F32");
+  std::vector<float> tmp(size_t(ncols) * n);
+  for (uint32_t c = 0; c < ncols; c++)
+    for (uint64_t i = 0; i < n; i++) tmp[size_t(c) * n + i] = float(host[c * hs + i]);
+  return mf_events_upload(b, MF_F32, tmp.data(), ncols, n, n, ds);
+}
+
+static int lower_desc(const mf_kernel_desc* d, mf::LoweredKernel& lk);
+
+int mf_kernel_build(mf_context* c, const mf_kernel_desc* d, mf_kernel** out) {
+  if (!c || !d || !out) return fail(MF_ERR_INVALID, "null argument");
+  *out = nullptr;
+  if (d->elem_type != MF_F64 && d->elem_type != MF_F32) return fail(MF_ERR_INVALID, "bad element type");
+  if (d->kind != MF_KERNEL_REDUCE && d->kind != MF_KERNEL_STORE && d->kind != MF_KERNEL_GENERATE)
+    return fail(MF_ERR_INVALID, "bad kernel kind");
+  if (d->n_outputs == 0 || d->n_outputs > MF_MAX_OUTPUTS) return fail(MF_ERR_INVALID, "bad number of outputs");
+  if (d->n_params > MF_MAX_PARAMS) return fail(MF_ERR_INVALID, "too many parameters");
+  auto k = std::make_unique<mf_kernel>();
+  k->ctx = c;
+  k->name = d->name ? d->name : "kernel";
+  k->kind = d->kind;
+  k->elem = d->elem_type;
+  k->n_inputs = d->n_inputs;
+  k->n_params = d->n_params;
+  k->n_outputs = d->n_outputs;
+  k->n_gen_dims = d->kind == MF_KERNEL_GENERATE ? d->n_gen_dims : 0;
+  int lrc = lower_desc(d, k->lowered);
+  if (lrc) return lrc;
+  for (int i : k->lowered.used_inputs) k->max_input = std::max(k->max_input, i);
+  int rc = compile_source(k->lowered.source, k->name, k->image);
+  if (rc) return rc;
+  MF_CUDA_TRY(cudaSetDevice(c->device));
+  MF_CUDA_TRY(cudaLibraryLoadData(&k->lib, k->image->cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0));
+  MF_CUDA_TRY(cudaLibraryGetKernel(&k->fn, k->lib, k->lowered.entry.c_str()));
+  if (d->kind == MF_KERNEL_REDUCE)
+    MF_CUDA_TRY(cudaLibraryGetKernel(&k->fn_seg, k->lib, (k->lowered.entry + "_segments").c_str()));
+  int nb = 0;
+  MF_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, reinterpret_cast<const void*>(k->fn),
+                                                            k->lowered.block, 0));
+  k->blocks_per_sm = std::max(1, nb);
+  c->refs++;
+  k->holds_ref = true;
+  *out = k.release();
+  return MF_OK;
+}
+
+static int lower_desc(const mf_kernel_desc* d, mf::LoweredKernel& lk) {
+  if (!d) return fail(MF_ERR_INVALID, "null descriptor");
+  if (d->elem_type != MF_F64 && d->elem_type != MF_F32) return fail(MF_ERR_INVALID, "bad element type");
+  if (d->kind != MF_KERNEL_REDUCE && d->kind != MF_KERNEL_STORE && d->kind != MF_KERNEL_GENERATE)
+    return fail(MF_ERR_INVALID, "bad kernel kind");
+  if (d->n_outputs == 0 || d->n_outputs > MF_MAX_OUTPUTS || !d->exprs)
+    return fail(MF_ERR_INVALID, "bad number of outputs");
+  if (d->n_params > MF_MAX_PARAMS) return fail(MF_ERR_INVALID, "too many parameters");
+  auto names = [](uint32_t n, const char* const* p) {
+    std::vector<std::string> v;
+    for (uint32_t i = 0; i < n; i++) v.push_back(p && p[i] ? p[i] : "");
+    return v;
+  };
+  mf::GenerateSpec gs;
+  if (d->kind == MF_KERNEL_GENERATE) {
+    if (d->n_outputs != 1 || d->n_gen_dims == 0 || !d->gen_lo || !d->gen_hi)
+      return fail(MF_ERR_INVALID, "generate kernel needs one density expression and its dimensions");
+    gs.dims = names(d->n_gen_dims, d->gen_dim_names);
+    gs.lo.assign(d->gen_lo, d->gen_lo + d->n_gen_dims);
+    gs.hi.assign(d->gen_hi, d->gen_hi + d->n_gen_dims);
+    gs.maxprob = d->maxprob;
+  }
+  try {
+    lk = mf::lower(d->name ? d->name : "kernel",
+                   d->kind == MF_KERNEL_REDUCE  ? mf::Kind::Reduce
+                   : d->kind == MF_KERNEL_STORE ? mf::Kind::Store
+                                                : mf::Kind::Generate,
+                   d->elem_type == MF_F32 ? mf::Elem::F32 : mf::Elem::F64, names(d->n_inputs, d->input_names),
+                   names(d->n_params, d->param_names), names(d->n_outputs, d->exprs),
+                   d->kind == MF_KERNEL_GENERATE ? &gs : nullptr);
+  } catch (const std::exception& e) {
+    return fail(MF_ERR_PARSE, e.what());
+  }
+  return MF_OK;
+}
+
+int mf_lower_source(const mf_kernel_desc* d, char* buf, size_t len, size_t* needed) {
+  mf::LoweredKernel lk;
+  int rc = lower_desc(d, lk);
+  if (rc) return rc;
+  if (needed) *needed = lk.source.size() + 1;
+  if (buf && len) {
+    size_t n = std::min(len - 1, lk.source.size());
+    std::memcpy(buf, lk.source.data(), n);
+    buf[n] = '\0';
+  }
+  return MF_OK;
+}
+
+int mf_eval_expressions(uint32_t n_names, const char* const* names, const double* values, uint32_t n_exprs,
+                        const char* const* exprs, double* out) {
+  if ((n_names && (!names || !values)) || (n_exprs && (!exprs || !out))) return fail(MF_ERR_INVALID, "null argument");
+  std::vector<std::string> nm;
+  for (uint32_t i = 0; i < n_names; i++) nm.push_back(names[i] ? names[i] : "");
+  std::vector<double> vals(values, values + n_names);
+  try {
+    mf::Dag dag({}, nm);
+    for (uint32_t i = 0; i < n_exprs; i++) out[i] = dag.eval(dag.parse(exprs[i] ? exprs[i] : ""), {}, vals);
+  } catch (const std::exception& e) {
+    return fail(MF_ERR_PARSE, e.what());
+  }
+  return MF_OK;
+}
+
+int mf_seed_rows(uint64_t seed, uint32_t nrows, uint32_t* out) {
+  if (!out && nrows) return fail(MF_ERR_INVALID, "null argument");
+  // Splitmix64 seeding of four 32-bit words (upper halves), then xoshiro128++
+  // jumps by 2^64 steps between rows (published jump polynomial).
+  uint64_t sm = seed;
+  auto splitmix = [&sm]() {
+    uint64_t z = (sm += 0x9e3779b97f4a7c15ULL);
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+    return z ^ (z >> 31);
+  };
+  uint32_t st[4];
+  for (int k = 0; k < 4; k++) st[k] = uint32_t(splitmix() >> 32);
+  auto rotl = [](uint32_t x, int k) { return (x << k) | (x >> (32 - k)); };
+  auto next = [&](uint32_t* s) {
+    const uint32_t t = s[1] << 9;
+    s[2] ^= s[0];
+    s[3] ^= s[1];
+    s[1] ^= s[2];
+    s[0] ^= s[3];
+    s[2] ^= t;
+    s[3] = rotl(s[3], 11);
+  };
+  static const uint32_t J[4] = {0x8764000bu, 0xf542d2d3u, 0x6fa035c3u, 0x77f2db5bu};
+  for (uint32_t r = 0; r < nrows; r++) {
+    for (int k = 0; k < 4; k++) out[uint64_t(k) * nrows + r] = st[k];
+    uint32_t a[4] = {0, 0, 0, 0};
+    for (int i = 0; i < 4; i++)
+      for (int b = 0; b < 32; b++) {
+        if (J[i] & (1u << b))
+          for (int k = 0; k < 4; k++) a[k] ^= st[k];
+        next(st);
+      }
+    for (int k = 0; k < 4; k++) st[k] = a[k];
+  }
+  return MF_OK;
+}
+
+int mf_generate_partition(uint64_t n, uint32_t max_workitems, uint64_t* nper, uint32_t* nseeds) {
+  if (!nper || !nseeds) return fail(MF_ERR_INVALID, "null argument");
+  if (max_workitems > 0 && n > max_workitems) {
+    *nper = n / max_workitems + 1;
+    *nseeds = uint32_t(n / *nper + 1);
+  } else {
+    *nper = 1;
+    *nseeds = uint32_t(std::max<uint64_t>(n, 1));
+  }
+  return MF_OK;
+}
+
+int mf_compile_check(const mf_kernel_desc* d, int* regs, int* spill) {
+  mf::LoweredKernel lk;
+  int rc = lower_desc(d, lk);
+  if (rc) return rc;
+  std::shared_ptr<CompiledImage> img;
+  rc = compile_source(lk.source, d->name ? d->name : "kernel", img);
+  if (rc) return rc;
+  if (regs) *regs = img->regs;
+  if (spill) *spill = img->spill;
+  return MF_OK;
+}
+
+int mf_kernel_free(mf_kernel* k) {
+  if (!k) return MF_OK;
+  mf_context* c = k->ctx;
+  if (k->lib) {
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    cudaLibraryUnload(k->lib);
+  }
+  const bool counted = k->holds_ref;
+  delete k;
+  if (counted) release_context(c);
+  return MF_OK;
+}
+
+int mf_kernel_source(const mf_kernel* k, char* buf, size_t len, size_t* needed) {
+  if (!k) return fail(MF_ERR_INVALID, "kernel is null");
+  const std::string& s = k->lowered.source;
+  if (needed) *needed = s.size() + 1;
+  if (buf && len) {
+    size_t n = std::min(len - 1, s.size());
+    std::memcpy(buf, s.data(), n);
+    buf[n] = '\0';
+  }
+  return MF_OK;
+}
+
+int mf_kernel_info(const mf_kernel* k, int* regs, int* spill, int* block, int* vec) {
+  if (!k) return fail(MF_ERR_INVALID, "kernel is null");
+  if (regs) *regs = k->image ? k->image->regs : -1;
+  if (spill) *spill = k->image ? k->image->spill : -1;
+  if (block) *block = k->lowered.block;
+  if (vec) *vec = k->lowered.vec;
+  return MF_OK;
+}
+
+}  // extern "C"
+
+namespace mfi {
+
+int grid_for(const mf_kernel* k, uint64_t n) {
+  const uint64_t per_block = uint64_t(k->lowered.block) * uint64_t(k->lowered.vec);
+  const uint64_t need = std::max<uint64_t>(1, (n + per_block - 1) / per_block);
+  const uint64_t cap = uint64_t(k->ctx->num_sms) * uint64_t(k->blocks_per_sm);
+  return int(std::min(need, cap));
+}
+
+// Launches one REDUCE kernel; `out` is a device-visible address for n_outputs doubles.
+int launch_reduce(mf_kernel* k, const void* data, uint64_t stride, uint64_t n, const double* params,
+                  double* partials, unsigned* counter, double* out, cudaStream_t stream, int grid_cap) {
+  int grid = grid_for(k, n);
+  if (grid_cap > 0) grid = std::min(grid, grid_cap);
+  std::vector<double> pv(std::max<uint32_t>(1, k->n_params), 0.0);
+  if (k->n_params) std::memcpy(pv.data(), params, k->n_params * sizeof(double));
+  void* args[] = {const_cast<void**>(&data), &stride, &n, pv.data(), &partials, &counter, &out};
+  MF_CUDA_TRY(cudaLaunchKernel(reinterpret_cast<const void*>(k->fn), dim3(grid), dim3(k->lowered.block), args, 0,
+                               stream));
+  return MF_OK;
+}
+
+}  // namespace mfi
+
+extern "C" {
+
+int mf_kernel_reduce(mf_kernel* k, const mf_buffer* in, uint64_t stride, uint64_t n, const double* params,
+                     uint32_t n_params, double* sums) {
+  if (!k || !sums) return fail(MF_ERR_INVALID, "null argument");
+  if (k->kind != MF_KERNEL_REDUCE) return fail(MF_ERR_INVALID, "kernel is not a REDUCE kernel");
+  if (n_params != k->n_params || (n_params && !params))
+    return fail(MF_ERR_INVALID, "parameter count mismatch (" + std::to_string(n_params) + " given, " +
+                                    std::to_string(k->n_params) + " expected)");
+  int rc = check_layout(k, in, stride, n);
+  if (rc) return rc;
+  mf_context* c = k->ctx;
+  if (n == 0) {
+    std::fill(sums, sums + k->n_outputs, 0.0);
+    return MF_OK;
+  }
+  MF_CUDA_TRY(cudaSetDevice(c->device));
+  const int grid = mfi::grid_for(k, n);
+  rc = ensure_scratch(c, size_t(grid) * k->n_outputs, k->n_outputs);
+  if (rc) return rc;
+  rc = mfi::launch_reduce(k, in->ptr, stride, n, params, c->partials, c->counter, c->out_dev, c->stream, 0);
+  if (rc) return rc;
+  MF_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  std::memcpy(sums, c->out_host, k->n_outputs * sizeof(double));
+  return MF_OK;
+}
+
+int mf_kernel_reduce_async(mf_kernel* k, const mf_buffer* in, uint64_t stride, uint64_t n, const double* params,
+                           uint32_t n_params, mf_buffer* out, uint64_t out_index) {
+  if (!k || !out) return fail(MF_ERR_INVALID, "null argument");
+  if (k->kind != MF_KERNEL_REDUCE) return fail(MF_ERR_INVALID, "kernel is not a REDUCE kernel");
+  if (n_params != k->n_params || (n_params && !params)) return fail(MF_ERR_INVALID, "parameter count mismatch");
+  int rc = check_layout(k, in, stride, n);
+  if (rc) return rc;
+  if ((out_index + 1) * k->n_outputs * sizeof(double) > out->size)
+    return fail(MF_ERR_INVALID, "output buffer too small for out_index");
+  if (n == 0) return fail(MF_ERR_INVALID, "no events");
+  mf_context* c = k->ctx;
+  MF_CUDA_TRY(cudaSetDevice(c->device));
+  const int grid = mfi::grid_for(k, n);
+  rc = ensure_scratch(c, size_t(grid) * k->n_outputs, k->n_outputs);
+  if (rc) return rc;
+  double* dst = static_cast<double*>(out->ptr) + out_index * k->n_outputs;
+  return mfi::launch_reduce(k, in->ptr, stride, n, params, c->partials, c->counter, dst, c->stream, 0);
+}
+
+int mf_kernel_reduce_many(mf_kernel* k, uint32_t count, const mf_buffer* const* inputs, const uint64_t* strides,
+                          const uint64_t* ns, const double* params, uint32_t n_params, mf_buffer* out) {
+  if (!k || !inputs || !strides || !ns || !out || (n_params && !params)) return fail(MF_ERR_INVALID, "null argument");
+  if (k->kind != MF_KERNEL_REDUCE) return fail(MF_ERR_INVALID, "kernel is not a REDUCE kernel");
+  if (n_params != k->n_params) return fail(MF_ERR_INVALID, "parameter count mismatch");
+  if (uint64_t(count) * k->n_outputs * sizeof(double) > out->size)
+    return fail(MF_ERR_INVALID, "output buffer smaller than count x outputs");
+  for (uint32_t i = 0; i < count; i++) {
+    int rc = check_layout(k, inputs[i], strides[i], ns[i]);
+    if (rc) return rc;
+    if (ns[i] == 0) return fail(MF_ERR_INVALID, "launch with no events");
+  }
+  mf_context* c = k->ctx;
+  MF_CUDA_TRY(cudaSetDevice(c->device));
+  int maxgrid = 1;
+  for (uint32_t i = 0; i < count; i++) maxgrid = std::max(maxgrid, mfi::grid_for(k, ns[i]));
+  int rc = ensure_scratch(c, size_t(maxgrid) * k->n_outputs, k->n_outputs);
+  if (rc) return rc;
+  for (uint32_t i = 0; i < count; i++) {
+    double* dst = static_cast<double*>(out->ptr) + uint64_t(i) * k->n_outputs;
+    rc = mfi::launch_reduce(k, inputs[i]->ptr, strides[i], ns[i], params + uint64_t(i) * n_params, c->partials,
+                            c->counter, dst, c->stream, 0);
+    if (rc) return rc;
+  }
+  return MF_OK;
+}
+
+int mf_context_stream(mf_context* c, void** stream) {
+  if (!c || !stream) return fail(MF_ERR_INVALID, "null argument");
+  *stream = c->stream;
+  return MF_OK;
+}
+
+int mf_kernel_reduce_segments(mf_kernel* k, const mf_buffer* in, uint64_t stride, uint32_t nseg,
+                              const uint64_t* seg_begin, const uint32_t* seg_count, const double* params,
+                              uint32_t n_params, double* sums) {
+  if (!k || !in || !seg_begin || !seg_count || !sums || (n_params && !params))
+    return fail(MF_ERR_INVALID, "null argument");
+  if (k->kind != MF_KERNEL_REDUCE) return fail(MF_ERR_INVALID, "kernel is not a REDUCE kernel");
+  if (n_params != k->n_params) return fail(MF_ERR_INVALID, "parameter count mismatch");
+  if (nseg == 0) return MF_OK;
+  uint64_t end = 0;
+  for (uint32_t s = 0; s < nseg; s++) end = std::max<uint64_t>(end, seg_begin[s] + seg_count[s]);
+  int rc = check_layout(k, in, stride, end);
+  if (rc) return rc;
+  mf_context* c = k->ctx;
+  MF_CUDA_TRY(cudaSetDevice(c->device));
+  const uint32_t np = std::max<uint32_t>(1, n_params);
+  const size_t bytes_begin = size_t(nseg) * 8, bytes_count = (size_t(nseg) * 4 + 7) / 8 * 8,
+               bytes_par = size_t(nseg) * np * 8;
+  rc = ensure_stage(c, bytes_begin + bytes_count + bytes_par);
+  if (rc) return rc;
+  rc = ensure_scratch(c, 0, size_t(nseg) * k->n_outputs);
+  if (rc) return rc;
+  std::vector<char> host(bytes_begin + bytes_count + bytes_par, 0);
+  std::memcpy(host.data(), seg_begin, bytes_begin);
+  std::memcpy(host.data() + bytes_begin, seg_count, size_t(nseg) * 4);
+  double* hp = reinterpret_cast<double*>(host.data() + bytes_begin + bytes_count);
+  for (uint32_t s = 0; s < nseg; s++)
+    for (uint32_t j = 0; j < n_params; j++) hp[size_t(s) * np + j] = params[size_t(s) * n_params + j];
+  MF_CUDA_TRY(cudaMemcpyAsync(c->stage_dev, host.data(), host.size(), cudaMemcpyHostToDevice, c->stream));
+  char* base = static_cast<char*>(c->stage_dev);
+  const uint64_t* d_begin = reinterpret_cast<const uint64_t*>(base);
+  const unsigned* d_count = reinterpret_cast<const unsigned*>(base + bytes_begin);
+  const double* d_par = reinterpret_cast<const double*>(base + bytes_begin + bytes_count);
+  unsigned npu = np;
+  double* outp = c->out_dev;
+  const void* data = in->ptr;
+  void* args[] = {const_cast<void**>(&data), &stride, &d_begin, &d_count, &d_par, &npu, &outp};
+  MF_CUDA_TRY(cudaLaunchKernel(reinterpret_cast<const void*>(k->fn_seg), dim3(nseg), dim3(k->lowered.block), args, 0,
+                               c->stream));
+  MF_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  std::memcpy(sums, c->out_host, size_t(nseg) * k->n_outputs * sizeof(double));
+  return MF_OK;
+}
+
+int mf_kernel_store(mf_kernel* k, const mf_buffer* in, uint64_t in_stride, uint64_t n, const double* params,
+                    uint32_t n_params, mf_buffer* out, uint64_t out_stride) {
+  if (!k || !out) return fail(MF_ERR_INVALID, "null argument");
+  if (k->kind != MF_KERNEL_STORE) return fail(MF_ERR_INVALID, "kernel is not a STORE kernel");
+  if (n_params != k->n_params || (n_params && !params)) return fail(MF_ERR_INVALID, "parameter count mismatch");
+  int rc = check_layout(k, in, in_stride, n);
+  if (rc) return rc;
+  if (out_stride < n) return fail(MF_ERR_INVALID, "output stride smaller than the number of events");
+  if (uint64_t(k->n_outputs) * out_stride * elem_size(k->elem) > out->size)
+    return fail(MF_ERR_INVALID, "output buffer smaller than outputs x stride");
+  if (n == 0) return MF_OK;
+  mf_context* c = k->ctx;
+  MF_CUDA_TRY(cudaSetDevice(c->device));
+  const uint64_t need = (n + k->lowered.block - 1) / k->lowered.block;
+  const int grid = int(std::min<uint64_t>(need, uint64_t(c->num_sms) * k->blocks_per_sm * 4));
+  std::vector<double> pv(std::max<uint32_t>(1, k->n_params), 0.0);
+  if (k->n_params) std::memcpy(pv.data(), params, k->n_params * sizeof(double));
+  const void* data = in->ptr;
+  void* outp = out->ptr;
+  void* args[] = {const_cast<void**>(&data), &in_stride, &n, pv.data(), &outp, &out_stride};
+  MF_CUDA_TRY(cudaLaunchKernel(reinterpret_cast<const void*>(k->fn), dim3(grid), dim3(k->lowered.block), args, 0,
+                               c->stream));
+  MF_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return MF_OK;
+}
+
+int mf_kernel_generate(mf_kernel* k, const uint32_t* seeds, uint32_t nseeds, uint64_t n, uint64_t nper,
+                       const double* params, uint32_t n_params, mf_buffer* out, uint64_t out_stride,
+                       uint64_t max_tries) {
+  if (!k || !seeds || !out) return fail(MF_ERR_INVALID, "null argument");
+  if (k->kind != MF_KERNEL_GENERATE) return fail(MF_ERR_INVALID, "kernel is not a GENERATE kernel");
+  if (n_params != k->n_params || (n_params && !params)) return fail(MF_ERR_INVALID, "parameter count mismatch");
+  if (nseeds == 0 || nper == 0) return fail(MF_ERR_INVALID, "no generator threads");
+  if (uint64_t(nseeds) * nper < n) return fail(MF_ERR_INVALID, "nseeds x nper does not cover n events");
+  if (out_stride < n || uint64_t(k->n_gen_dims) * out_stride * elem_size(k->elem) > out->size)
+    return fail(MF_ERR_INVALID, "output buffer smaller than dimensions x stride");
+  if (n == 0) return MF_OK;
+  mf_context* c = k->ctx;
+  MF_CUDA_TRY(cudaSetDevice(c->device));
+  int rc = ensure_stage(c, size_t(nseeds) * 4 * sizeof(uint32_t));
+  if (rc) return rc;
+  MF_CUDA_TRY(cudaMemcpyAsync(c->stage_dev, seeds, size_t(nseeds) * 4 * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                              c->stream));
+  MF_CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(unsigned), c->stream));
+  std::vector<double> pv(std::max<uint32_t>(1, k->n_params), 0.0);
+  if (k->n_params) std::memcpy(pv.data(), params, k->n_params * sizeof(double));
+  const unsigned* sd = static_cast<const unsigned*>(c->stage_dev);
+  void* outp = out->ptr;
+  unsigned* status = c->status;
+  unsigned long long mt = max_tries ? max_tries : 1000000000ULL;
+  void* args[] = {&sd, &nseeds, &n, &nper, pv.data(), &outp, &out_stride, &status, &mt};
+  const unsigned grid = (nseeds + k->lowered.block - 1) / k->lowered.block;
+  MF_CUDA_TRY(cudaLaunchKernel(reinterpret_cast<const void*>(k->fn), dim3(grid), dim3(k->lowered.block), args, 0,
+                               c->stream));
+  unsigned st = 0;
+  MF_CUDA_TRY(cudaMemcpyAsync(&st, c->status, sizeof st, cudaMemcpyDeviceToHost, c->stream));
+  MF_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  if (st) return fail(MF_ERR_TIMEOUT, "generation gave up after max_tries proposals in at least one thread");
+  return MF_OK;
+}
+
+}  // extern "C"

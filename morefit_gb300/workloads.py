@@ -1,0 +1,171 @@
+"""Likelihood evaluation on the CUDA backend for a lowered MoreFit model.
+
+A model spec (``morefit_gb300/specs/<name>.json``) holds exactly what the
+reference's ``fitter::make_kernels`` hands its compute backend
+(include/fitter.hh:321-658): the precompute kernel (event-only hoisted
+columns), the lh / lh+grad / Hessian kernels as get_kernel() strings, and the
+parameter-buffer expressions evaluated on the host before every launch.
+
+``Likelihood`` restates the fitter's evaluation calls on top of
+``CUDABlock`` with the same call sequence and the same conventions:
+``likelihood()`` returns -2 sum log p (fitter.hh:1152-1220),
+``likelihood_and_gradient()`` returns (-2 sum log p, -2 sum dlogp/dtheta)
+(fitter.hh:1054-1151) and ``hessian()`` returns the matrix of -2 sum
+d2logp/dtheta_i dtheta_j (fitter.hh:1221-1326). The event block is uploaded
+once (fitter.hh:704-757) and every evaluation moves only the parameter
+vector in and the sums out.
+"""
+from __future__ import annotations
+
+import json
+from pathlib import Path
+
+import numpy as np
+
+import ctypes as C
+
+from . import _lib as L
+from .backend import CUDABackend, CUDABlock, DeviceColumns, eval_expressions
+
+DEFAULT_SEED = 229387429
+MAX_GENERATOR_WORKITEMS = 8192  # compute_options::opencl_max_generator_workitems (compute.hh:59)
+
+SPEC_DIR = Path(__file__).resolve().parent / "specs"
+
+
+def load_spec(name: str) -> dict:
+    return json.loads((SPEC_DIR / f"{name}.json").read_text())
+
+
+class Likelihood:
+    """NLL, gradient and Hessian of one dataset, device resident."""
+
+    def __init__(self, backend: CUDABackend, spec: dict, kernelT=np.float64):
+        self.backend = backend
+        self.spec = spec
+        self.kernelT = np.dtype(kernelT)
+        self.params = list(spec["parameters"])
+        ks = {k["name"]: k for k in spec["kernels"]}
+        self.kspec = ks
+        self.has_precompute = "precompute_kernel" in ks
+        self.buffers = {"lh_kernel": spec["lh_buffers"], "lh_grad_kernel": spec["grad_buffers"],
+                        "lh_hessian_kernel": spec["hessian_buffers"]}
+        # Blocks as the fitter wires them (fitter.hh:525-657, 704-757).
+        self.pre = CUDABlock(backend, kernelT)
+        self.blocks = {}
+        for name in ("lh_kernel", "lh_grad_kernel", "lh_hessian_kernel"):
+            if name not in ks:
+                continue
+            b = CUDABlock(backend, kernelT)
+            if self.has_precompute:
+                b.SetupInputBuffer(self.pre, False)
+            else:
+                b.SetupInputBuffer(self.pre, True)
+            k = ks[name]
+            b.MakeComputeKernel(name, 0, k["inputs"], [f"r{i}" for i in range(len(k["exprs"]))], k["params"],
+                                k["exprs"], True)
+            self.blocks[name] = b
+        if self.has_precompute:
+            k = ks["precompute_kernel"]
+            self.pre.MakeComputeKernel("precompute_kernel", 0, k["inputs"], k["outputs"], [], k["exprs"], False)
+        self.nevents = 0
+
+    def set_data(self, events: np.ndarray) -> None:
+        """Uploads the raw event block (ndims, n) and runs the precompute kernel."""
+        ev = np.asarray(events)
+        if ev.ndim == 1:
+            ev = ev[None, :]
+        self.pre.CopyToInputBuffer(ev)
+        self.nevents = ev.shape[1]
+        if self.has_precompute:
+            self.pre.SetNevents(self.nevents)
+            self.pre.SubmitKernel()
+        for b in self.blocks.values():
+            b.SetNevents(self.nevents)
+
+    def set_device_data(self, cols: DeviceColumns) -> None:
+        """Uses an event block already on the device (e.g. from generate_events)."""
+        if cols.elem != self.pre.elem:
+            self.set_data(cols.download())
+            return
+        self.pre.input = cols
+        self.nevents = cols.n
+        if self.has_precompute:
+            self.pre.SetNevents(self.nevents)
+            self.pre.SubmitKernel()
+        else:
+            for b in self.blocks.values():
+                b.SetupInputBuffer(self.pre, True)
+        for b in self.blocks.values():
+            b.SetNevents(self.nevents)
+
+    def input_block(self, kernel: str = "lh_grad_kernel") -> DeviceColumns:
+        return self.blocks[kernel].input
+
+    def param_vector(self, kernel: str, theta) -> np.ndarray:
+        """[floating values..., parameter buffers...] as the fitter builds it (fitter.hh:1059-1072)."""
+        theta = np.asarray(theta, dtype=np.float64)
+        bufs = self.buffers[kernel]
+        extra = eval_expressions(self.params, theta, [e for _, e in bufs]) if bufs else np.zeros(0)
+        return np.concatenate([theta, extra])
+
+    def sums(self, kernel: str, theta=None, param_vector=None) -> np.ndarray:
+        b = self.blocks[kernel]
+        pv = self.param_vector(kernel, theta) if param_vector is None else np.asarray(param_vector, np.float64)
+        b.CopyToParameterBuffer(pv)
+        b.SubmitKernel()
+        return b.CopyFromKahanBuffer()
+
+    def likelihood(self, theta) -> float:
+        return -2.0 * float(self.sums("lh_kernel", theta)[0])
+
+    def likelihood_and_gradient(self, theta):
+        s = self.sums("lh_grad_kernel", theta)
+        return -2.0 * float(s[0]), -2.0 * s[1:]
+
+    def hessian(self, theta) -> np.ndarray:
+        s = self.sums("lh_hessian_kernel", theta)
+        npar = len(self.params)
+        h = np.zeros((npar, npar))
+        idx = 0
+        for i in range(npar):
+            for j in range(i + 1):
+                h[i, j] = h[j, i] = -2.0 * s[idx]
+                idx += 1
+        return h
+
+
+def seed_rows(nrows: int, seed: int = DEFAULT_SEED) -> np.ndarray:
+    out = np.zeros((4, nrows), dtype=np.uint32)
+    L.check(L.lib.mf_seed_rows(seed, nrows, out.ctypes.data_as(C.POINTER(C.c_uint32))))
+    return out
+
+
+def generate_partition(n: int, max_workitems: int = MAX_GENERATOR_WORKITEMS):
+    nper, nseeds = C.c_uint64(), C.c_uint32()
+    L.check(L.lib.mf_generate_partition(n, max_workitems, C.byref(nper), C.byref(nseeds)))
+    return nper.value, nseeds.value
+
+
+def generate_events(backend: CUDABackend, spec: dict, n: int, seed: int = DEFAULT_SEED,
+                    max_workitems: int = MAX_GENERATOR_WORKITEMS, kernelT=np.float64) -> DeviceColumns:
+    """Seeded accept-reject events on the GPU (generator::generate, generator.hh:71-175).
+
+    Uses the model's generate kernel (the normalised density with the truth
+    values substituted, as the reference's generator builds it) and the
+    accelerator work partition with ``max_workitems`` generator threads."""
+    gk = next(k for k in spec["kernels"] if k.get("generate"))
+    blk = CUDABlock(backend, kernelT)
+    blk.MakeGenerateKernel(gk["name"], n, [], gk["outputs"], gk["params"], gk["exprs"], gk["maxprob"],
+                           ranges=list(zip(gk["lo"], gk["hi"])))
+    nper, nseeds = generate_partition(n, max_workitems)
+    blk.CopyToSeedBuffer(seed_rows(nseeds, seed))
+    blk.SetNevents(n)
+    blk.SubmitKernel(nper=nper)
+    cols = blk.output
+    blk.output = DeviceColumns(backend, blk.elem)  # hand the columns over to the caller
+    return cols
+
+
+def elem_of(kernelT) -> int:
+    return L.MF_F32 if np.dtype(kernelT) == np.float32 else L.MF_F64

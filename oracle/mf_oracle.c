@@ -233,6 +233,40 @@ int mfo_generate(int workload, const double* th, const double* lo, const double*
   return 0;
 }
 
+int mfo_generate_partitioned(int workload, const double* th, const double* lo, const double* hi, uint64_t seed,
+                             uint32_t n, uint32_t nper, uint32_t nseeds, double* out) {
+  if (nseeds == 0 || nper == 0 || (workload != 0 && workload != 1)) return 1;
+  const int ndim = workload == 0 ? 1 : 3;
+  uint32_t* seeds = (uint32_t*)malloc(sizeof(uint32_t) * 4 * (size_t)nseeds);
+  mfo_seed_rows(seed, nseeds, seeds);
+  gen_job j;
+  memset(&j, 0, sizeof j);
+  j.workload = workload;
+  j.th = th;
+  for (int d = 0; d < ndim; d++) {
+    j.lo[d] = printed15(lo[d]);
+    j.delta[d] = printed15(hi[d] - lo[d]);
+  }
+  j.mlo = lo[0];
+  j.mhi = hi[0];
+  j.maxprob = printed15(workload == 0 ? mfo_mass_max(th, lo[0], hi[0]) : mfo_pwave_max(th));
+  j.seeds = seeds;
+  j.nthreads = nseeds;
+  j.n = n;
+  j.out = out;
+  for (uint32_t t = 0; t < nseeds; t++) {
+    uint64_t from = (uint64_t)t * nper, to = from + nper;
+    if (from >= n) break;
+    if (to > n) to = n;
+    j.tid = t;
+    j.from = (uint32_t)from;
+    j.to = (uint32_t)to;
+    gen_chunk(&j);
+  }
+  free(seeds);
+  return 0;
+}
+
 /* ---------------- compensated sums ---------------- */
 
 double mfo_kahan(const double* v, uint32_t n) {

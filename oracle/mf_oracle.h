@@ -39,6 +39,13 @@ void mfo_seed_rows(uint64_t seed, uint32_t nrows, uint32_t* seeds);
 int mfo_generate(int workload, const double* truth, const double* range_lo, const double* range_hi,
                  uint64_t seed, uint32_t n, uint32_t nthreads, double* out);
 
+/* Accept-reject generation with the accelerator work partition of the
+ * reference's OpenCL generate kernel (include/compute_opencl.hh:505-515,
+ * 541-580): generator thread t (seed row t of mfo_seed_rows) produces events
+ * [t*nper, min((t+1)*nper, n)). nseeds rows are used. */
+int mfo_generate_partitioned(int workload, const double* truth, const double* range_lo, const double* range_hi,
+                             uint64_t seed, uint32_t n, uint32_t nper, uint32_t nseeds, double* out);
+
 /* Closed-form normalised densities (restating pdf.hh:139-194,423-651 and
  * physicspdfs.hh:39-81) evaluated per event. */
 double mfo_mass_prob(double m, const double* theta, double lo, double hi);

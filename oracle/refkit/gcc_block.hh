@@ -59,6 +59,9 @@ struct RecordedKernel {
   std::string name;
   std::vector<std::string> inputs, outputs, params, exprs;
   bool kahan = false;
+  bool generate = false;
+  std::vector<double> lo, hi;
+  double maxprob = 0.0;
 };
 
 inline std::vector<RecordedKernel>& recorded_kernels() {
@@ -195,6 +198,18 @@ class LLVMBlock : public ComputeBlock<kernelT, evalT, seedT> {
     generate_ = true;
     name_ = name;
     nevents_ = nevents_padded_ = nevents;
+    RecordedKernel rec;
+    rec.name = name;
+    rec.generate = true;
+    rec.params = params;
+    for (auto& d : output_signature) {
+      rec.outputs.push_back(d.get_name());
+      rec.lo.push_back(d.get_min());
+      rec.hi.push_back(d.get_max());
+    }
+    rec.exprs.push_back(graphs.at(0)->get_kernel());
+    rec.maxprob = maxprob;
+    recorded_kernels().push_back(rec);
     std::ostringstream c;
     c << "#include <math.h>\n#include <stdint.h>\n";
     c << "static inline uint32_t rotl32(uint32_t x, int k) { return (x << k) | (x >> (32 - k)); }\n";

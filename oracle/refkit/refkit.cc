@@ -195,7 +195,9 @@ static int cmd_golden(const std::string& which, unsigned n, const std::string& o
   Xoshiro128pp rnd;
   rnd.setSeed(int64_t(229387429));
   EventVector<kT, eT> data(w.dims);
+  recorded_kernels().clear();
   generate(w, &backend, &rnd, n, data);
+  std::vector<RecordedKernel> gen_records = recorded_kernels();
   const uint64_t ev_hash = fnv1a(data.get_data(), data.buffer_size());
   if (!out_bin.empty()) {
     FILE* f = std::fopen(out_bin.c_str(), "wb");
@@ -265,11 +267,16 @@ static int cmd_golden(const std::string& which, unsigned n, const std::string& o
   pts += "]";
 
   std::string kern = "[";
-  for (size_t i = 0; i < recorded_kernels().size(); i++) {
-    auto& r = recorded_kernels()[i];
+  std::vector<RecordedKernel> all = gen_records;
+  for (auto& r : recorded_kernels()) all.push_back(r);
+  for (size_t i = 0; i < all.size(); i++) {
+    auto& r = all[i];
     kern += std::string(i ? "," : "") + "{\"name\":" + jstr(r.name) + ",\"inputs\":" + jsvec(r.inputs) +
             ",\"outputs\":" + jsvec(r.outputs) + ",\"params\":" + jsvec(r.params) + ",\"exprs\":" + jsvec(r.exprs) +
-            ",\"kahan\":" + (r.kahan ? "true" : "false") + "}";
+            ",\"kahan\":" + (r.kahan ? "true" : "false");
+    if (r.generate)
+      kern += ",\"generate\":true,\"lo\":" + jvec(r.lo) + ",\"hi\":" + jvec(r.hi) + ",\"maxprob\":" + jnum(r.maxprob);
+    kern += "}";
   }
   kern += "]";
   std::vector<std::string> dnames, pnames;

@@ -1,0 +1,69 @@
+"""Lowering of the reference's kernel text to CUDA C and its NVRTC compile for sm_103a (CPU only)."""
+import pytest
+
+from conftest import kernel_spec, load_golden
+
+
+def _src(g, name, elem, kind=0):
+    from morefit_gb300.backend import lower_source
+    k = kernel_spec(g, name)
+    return lower_source(name, kind, elem, k["inputs"], k["params"], k["exprs"])
+
+
+def test_shared_subexpressions_evaluated_once():
+    from morefit_gb300 import _lib as L
+    g = load_golden("pwave_n1000.json")
+    src = _src(g, "lh_grad_kernel", L.MF_F64)
+    body = src[src.index("mf_reduce("):src.index("mf_reduce_segments(")]
+    # one density, one log and one reciprocal per event (vector width 2)
+    assert body.count("= log(") == 2
+    assert body.count("__drcp_rn(") == 2
+    # only the 11 hoisted basis columns are read; ctl, ctk, phi are not
+    assert "data + (mf_u64)0 * stride" not in body and "data + (mf_u64)13 * stride" in body
+
+
+def test_hessian_kernel_shares_the_density():
+    from morefit_gb300 import _lib as L
+    g = load_golden("pwave_n1000.json")
+    src = _src(g, "lh_hessian_kernel", L.MF_F64)
+    body = src[src.index("mf_reduce("):src.index("mf_reduce_segments(")]
+    assert body.count("__drcp_rn(") <= 4  # 1/p and 1/p^2, twice for the two vector lanes
+
+
+def test_float_kernels_use_float_literals_and_functions():
+    from morefit_gb300 import _lib as L
+    g = load_golden("mass_n1000.json")
+    src = _src(g, "lh_grad_kernel", L.MF_F32)
+    body = src[src.index("mf_reduce("):src.index("mf_reduce_segments(")]
+    assert "expf(" in body and "logf(" in body
+    assert " exp(" not in body and " log(" not in body
+    assert "double2" not in body and "float4" in body
+
+
+@pytest.mark.parametrize("workload", ["pwave", "mass"])
+@pytest.mark.parametrize("elem", [0, 1])
+def test_all_kernels_compile_without_spills(workload, elem):
+    from morefit_gb300 import _lib as L
+    from morefit_gb300.backend import compile_check
+    g = load_golden(f"{workload}_n1000.json")
+    for k in g["kernels"]:
+        gen = None
+        if k.get("generate"):
+            kind = L.MF_KERNEL_GENERATE
+            gen = (k["outputs"], k["lo"], k["hi"], k["maxprob"])
+        elif k["name"] == "precompute_kernel":
+            kind = L.MF_KERNEL_STORE
+        else:
+            kind = L.MF_KERNEL_REDUCE
+        info = compile_check(k["name"], kind, elem, k["inputs"], k["params"], k["exprs"], gen)
+        assert info["registers"] > 0
+        assert info["spill_bytes"] == 0, (k["name"], info)
+
+
+def test_parse_error_is_reported():
+    from morefit_gb300 import _lib as L
+    from morefit_gb300.backend import lower_source
+    with pytest.raises(L.MFError, match="PARSE"):
+        lower_source("bad", 0, 0, ["x"], [], ["log(x"])
+    with pytest.raises(L.MFError, match="PARSE"):
+        lower_source("bad", 0, 0, ["x"], [], ["foo(x)"])

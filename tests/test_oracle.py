@@ -1,0 +1,93 @@
+"""The oracle against the reference's own outputs (CPU only).
+
+Golden files were written by oracle/refkit: the reference's generator,
+fitter and Minuit2 running on the reference's kernel text (make_golden.sh).
+"""
+import numpy as np
+import pytest
+
+from conftest import assert_sums_close, golden_events, kernel_spec, load_golden
+from oracle.spec_kernel import SpecKernel
+
+
+@pytest.mark.parametrize("workload,n", [("pwave", 1000), ("mass", 1000)])
+def test_generator_reproduces_reference_events(oracle_lib, workload, n):
+    ev = oracle_lib.generate(workload, n)
+    ref = golden_events(workload, n)
+    assert np.array_equal(ev, ref)
+    assert oracle_lib.fnv1a(ev) == load_golden(f"{workload}_n{n}.json")["events_fnv1a"]
+
+
+@pytest.mark.parametrize("workload,n", [("mass", 100000), ("pwave", 1000000)])
+def test_generator_hash_at_full_size(oracle_lib, workload, n):
+    ev = oracle_lib.generate(workload, n)
+    assert oracle_lib.fnv1a(ev) == load_golden(f"{workload}_n{n}.json")["events_fnv1a"]
+
+
+def test_generator_threads_partition(oracle_lib):
+    # Per-thread streams (generator.hh:102-113): thread t starts from t jumps.
+    a = oracle_lib.generate("pwave", 4000, nthreads=4)
+    b = oracle_lib.generate("pwave", 4000, nthreads=1)
+    assert np.array_equal(a[:, :1000], b[:, :1000])
+    assert not np.array_equal(a[:, 1000:2000], b[:, 1000:2000])
+
+
+def _inputs_for(g, events, spec_name):
+    """Event block a kernel reads: raw events, or the precompute output."""
+    ks = {k["name"]: k for k in g["kernels"]}
+    if "precompute_kernel" in ks:
+        return SpecKernel(ks["precompute_kernel"]).store(events, [])
+    return events
+
+
+@pytest.mark.parametrize("workload", ["pwave", "mass"])
+def test_spec_kernel_reproduces_reference_sums(oracle_lib, workload):
+    g = load_golden(f"{workload}_n1000.json")
+    ev = golden_events(workload, 1000)
+    for name in ("lh_kernel", "lh_grad_kernel", "lh_hessian_kernel"):
+        sk = SpecKernel(kernel_spec(g, name))
+        cols = _inputs_for(g, ev, name)
+        for pt in g["points"]:
+            got = sk.reduce(cols, pt["kernel_params"][name])
+            ref = np.array(pt["kernel_sums"][name])
+            np.testing.assert_allclose(got, ref, rtol=1e-13, atol=1e-13 * np.abs(ref).max())
+
+
+def test_spec_kernel_threads(oracle_lib):
+    g = load_golden("pwave_n1000.json")
+    ev = golden_events("pwave", 1000)
+    sk = SpecKernel(kernel_spec(g, "lh_grad_kernel"))
+    cols = _inputs_for(g, ev, "lh_grad_kernel")
+    p = g["points"][0]["kernel_params"]["lh_grad_kernel"]
+    a = sk.reduce(cols, p, nthreads=1)
+    b = sk.reduce(cols, p, nthreads=7)
+    np.testing.assert_allclose(a, b, rtol=1e-14, atol=1e-12)
+
+
+def test_closed_form_pwave_matches_reference(oracle_lib):
+    g = load_golden("pwave_n1000.json")
+    ev = golden_events("pwave", 1000)
+    basis = oracle_lib.pwave_basis(ev)
+    for pt in g["points"]:
+        got = oracle_lib.pwave_nll_grad(basis, pt["params"])
+        ref = np.array(pt["kernel_sums"]["lh_grad_kernel"])
+        assert_sums_close(got, ref, np.abs(ref) + 1e3, rtol=1e-11, stol=1e-13, what="pwave closed form")
+
+
+def test_closed_form_mass_matches_reference(oracle_lib):
+    g = load_golden("mass_n1000.json")
+    ev = golden_events("mass", 1000)
+    for pt in g["points"]:
+        got = oracle_lib.mass_nll_grad(ev[0], pt["params"])
+        ref = np.array(pt["kernel_sums"]["lh_grad_kernel"])
+        assert_sums_close(got, ref, np.abs(ref) + 1e3, rtol=1e-9, stol=1e-12, what="mass closed form")
+
+
+def test_closed_form_pwave_full_size(oracle_lib):
+    g = load_golden("pwave_n1000000.json")
+    ev = oracle_lib.generate("pwave", 1000000, nthreads=1)
+    basis = oracle_lib.pwave_basis(ev)
+    pt = g["points"][0]
+    got = oracle_lib.pwave_nll_grad(basis, pt["params"], nthreads=4)
+    ref = np.array(pt["kernel_sums"]["lh_grad_kernel"])
+    assert_sums_close(got, ref, np.full(9, 1e6), rtol=1e-11, stol=1e-13, what="pwave 1M closed form")
