@@ -159,13 +159,13 @@ def ours(args):
     ks = {k["name"]: k for k in spec["kernels"]}
     ncols_read = 11  # morefit_eventbuffer_3..13: the only columns the lh_grad expressions reference
 
-    def make_sets(kernelT):
+    def make_sets(kernelT, native=False):
         itemsize = np.dtype(kernelT).itemsize
         per_set = n * ncols_read * itemsize
         nsets = max(2, math.ceil(2 * L2_BYTES / per_set) + 1)
         sets = []
         for r in range(nsets):
-            like = Likelihood(backend, spec, kernelT)
+            like = Likelihood(backend, spec, kernelT, native_f64=native)
             cols = generate_events(backend, spec, n, seed=229387429 + 1000 * rank + r)
             like.set_device_data(cols)
             sets.append(like)
@@ -226,6 +226,16 @@ def ours(args):
     avg_launch_s = ms64 / 1e3 / args.steps
     hbm_peak, peak_kind = _peaks()
     achieved = bytes64 / avg_launch_s / 1e9
+
+    # ---------------- native FP64 arithmetic (reported beside the default) ----------------
+    native = None
+    if not args.no_native:
+        setsn, _, _ = make_sets(np.float64, native=True)
+        msn, resn = timed_device(setsn, max(50, args.steps // 10), args.warmup)
+        native = {"value": world * max(50, args.steps // 10) / (msn / 1e3), "unit": "evals/s",
+                  "dtype": "f64 storage, native FP64 arithmetic",
+                  "rel_diff_vs_default": float(np.max(np.abs(resn - res64) / np.maximum(np.abs(res64), 1.0)))}
+        del setsn
 
     # ---------------- mixed precision ----------------
     mixed = None
@@ -288,6 +298,8 @@ def ours(args):
         line = {"metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms64 / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "arithmetic": "FP64 storage and sums; per-event math in double-float (FP32 pairs, ~48-bit) -- "
+                              "NLL within 1e-10 rel of native FP64; native FP64 timed in native_fp64",
                 "data": "synthetic: seeded accept-reject K*mumu P-wave events generated on the GPU",
                 "config": {"workload": "K*mumu P-wave angular fit, 8 free parameters, 1M events, FP64 (configs[1])",
                            "nevents": n, "datasets_rotated": nsets64,
@@ -303,11 +315,94 @@ def ours(args):
                 "e2e_fit_loop": {"value": world / fit_loop_s, "unit": "evals/s", "h2d_bytes_per_step": 9 * 8,
                                  "d2h_bytes_per_step": 9 * 8,
                                  "what": "events resident; parameters in, sums out (the fitter's per-evaluation path)"},
-                "mixed": mixed, "cpu_baseline": cpu, "clocks": clk.summary(),
+                "native_fp64": native, "mixed": mixed, "cpu_baseline": cpu, "clocks": clk.summary(),
                 "gpu_launches": args.steps, "nll_truth": float(-2.0 * res64[0])}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+VARIANTS = {
+    # name: (kernelT, native_f64, vec, block, bulk-copy pipeline, stages); 0 = library default
+    "f64_native": (np.float64, True, 2, 256, False, 0),
+    "f64_dw": (np.float64, False, 0, 0, False, 0),
+    "f64_dw_b256": (np.float64, False, 1, 256, False, 0),
+    "f64_dw_pipe": (np.float64, False, 1, 256, True, 4),
+    "f32": (np.float32, False, 0, 0, False, 0),
+    "f32_v2": (np.float32, False, 2, 256, False, 0),
+    "f32_pipe": (np.float32, False, 2, 256, True, 4),
+}
+
+
+def variants(args):
+    """Times the NLL+grad kernel in each arithmetic mode / launch shape (one JSON line each).
+
+    Same datasets and timing as the main benchmark; used for launch-shape
+    sweeps and, with --steps 1, as the small case for ncu captures."""
+    import ctypes as C
+    import torch
+    from morefit_gb300 import _lib as L
+    from morefit_gb300.backend import CUDABackend
+    from morefit_gb300.workloads import Likelihood, generate_events, load_spec
+    torch.cuda.set_device(0)
+    backend = CUDABackend(0)
+    spec = load_spec("pwave")
+    truth = np.array(spec["truth"])
+    n = args.nevents
+    nsets = args.sets
+    raw = [generate_events(backend, spec, n, seed=229387429 + r) for r in range(nsets)]
+    ext = torch.cuda.ExternalStream(C_stream(backend))
+    names = args.variant_list.split(",") if args.variant_list else list(VARIANTS)
+    ref = None
+    for name in names:
+        kernelT, native, vec, block, pipeline, stages = VARIANTS[name]
+        sets = []
+        for r in range(nsets):
+            like = Likelihood(backend, spec, kernelT, native_f64=native, vec=vec, block=block, pipeline=pipeline,
+                              stages=stages)
+            if kernelT == np.float64:
+                like.set_device_data(raw[r])
+            else:
+                like.set_data(raw[r].download())
+            sets.append(like)
+        kern = sets[0].blocks["lh_grad_kernel"].kernel
+        pv = sets[0].param_vector("lh_grad_kernel", truth)
+        K, W = args.steps, args.warmup
+        out = L.c_buf()
+        L.check(L.lib.mf_buffer_alloc(backend.handle, max(K, W, 1) * kern.nout * 8, C.byref(out)))
+
+        def enqueue(count):
+            ins = (L.c_buf * count)(*[sets[i % nsets].blocks["lh_grad_kernel"].input.buf for i in range(count)])
+            st = np.array([sets[i % nsets].blocks["lh_grad_kernel"].input.stride for i in range(count)], np.uint64)
+            ns = np.full(count, n, dtype=np.uint64)
+            rows = np.ascontiguousarray(np.tile(pv, (count, 1)))
+            u = C.POINTER(C.c_uint64)
+            L.check(L.lib.mf_kernel_reduce_many(kern.handle, count, ins, st.ctypes.data_as(u), ns.ctypes.data_as(u),
+                                                L.dptr(rows), len(pv), out))
+
+        if W:
+            enqueue(W)
+        backend.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        enqueue(K)
+        e1.record(ext)
+        e1.synchronize()
+        backend.synchronize()
+        ms = e0.elapsed_time(e1) / K
+        res = np.zeros(kern.nout)
+        L.check(L.lib.mf_buffer_d2h(out, 0, res.ctypes.data, kern.nout * 8))
+        L.lib.mf_buffer_free(out)
+        if ref is None:
+            ref = res
+        itemsize = np.dtype(kernelT).itemsize
+        info = kern.info()
+        print(json.dumps({"variant": name, "us_per_eval": ms * 1e3, "evals_per_s": 1e3 / ms,
+                          "GBs": n * 11 * itemsize / (ms * 1e-3) / 1e9, "registers": info["registers"],
+                          "vec": info["vec"], "block": info["block"],
+                          "rel_diff_vs_first": (np.abs(res - ref) / np.maximum(np.abs(ref), 1.0)).max().item()}),
+              flush=True)
+        del sets
 
 
 def C_stream(backend):
@@ -330,11 +425,17 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-native", action="store_true")
+    ap.add_argument("--variants", action="store_true", help="time every kernel variant instead")
+    ap.add_argument("--variant-list", default="")
+    ap.add_argument("--sets", type=int, default=5)
     args = ap.parse_args()
-    if args.warmup < 3:
+    if args.warmup < 3 and not args.variants:
         args.warmup = 3
     if args.impl == "reference":
         reference_arm(args)
+    elif args.variants:
+        variants(args)
     else:
         ours(args)
 

@@ -325,6 +325,11 @@ class CUDABlock : public ComputeBlock<kernelT, evalT, seedT> {
     source_.assign(need, '\0');
     mf_lower_source(&d, &source_[0], need, nullptr);
     source_.resize(need ? need - 1 : 0);
+    print_source();
+  }
+  void print_source() const {
+    if (backend_ && backend_->opts_ && backend_->opts_->print_kernel)
+      std::cout << std::endl << "CUDA KERNEL SOURCECODE:" << std::endl << source_ << "END KERNEL SOURCECODE" << std::endl;
   }
   bool build(const std::string& name, const std::vector<std::string>& inputs, const std::vector<std::string>& params,
              const std::vector<std::string>& exprs, const std::vector<std::string>* dims,
@@ -348,8 +353,7 @@ class CUDABlock : public ComputeBlock<kernelT, evalT, seedT> {
     source_.assign(need, '\0');
     mf_kernel_source(kernel_, &source_[0], need, nullptr);
     source_.resize(need ? need - 1 : 0);
-    if (backend_->opts_ && backend_->opts_->print_kernel)
-      std::cout << std::endl << "CUDA KERNEL SOURCECODE:" << std::endl << source_ << "END KERNEL SOURCECODE" << std::endl;
+    print_source();
     return true;
   }
 

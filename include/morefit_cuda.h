@@ -139,7 +139,31 @@ typedef struct mf_kernel_desc {
   const double* gen_lo;
   const double* gen_hi;
   double maxprob;
+  /* MF_FLAG_* bits. */
+  uint32_t flags;
+  /* Launch shape of REDUCE kernels (0 = library default): events per thread
+   * per loop iteration (1, 2 or 4; vector loads of that width) and threads
+   * per block (64..1024, multiple of 32). */
+  uint32_t vec;
+  uint32_t block;
+  /* Shared-memory stages of the REDUCE input pipeline (0 = default, 2..8). */
+  uint32_t stages;
 } mf_kernel_desc;
+
+/* FP64 REDUCE kernels evaluate the per-event expressions in double-float
+ * arithmetic (pairs of FP32 values, ~48-bit significand, with FP64 sums) by
+ * default, because GB300 issues FP32 at 64x its FP64 rate; this flag selects
+ * native FP64 arithmetic instead. */
+#define MF_FLAG_NATIVE_F64 1u
+/* FP64 columns, FP32 per-event arithmetic with FP64 sums (the mixed-precision
+ * form for raw observables that need their FP64 storage, e.g. a mass with a
+ * large offset): a sum or difference of an input column and a parameter-only
+ * value is formed in FP64 before rounding, everything else in FP32. */
+#define MF_FLAG_F32_ARITH 2u
+/* REDUCE kernels stream their input columns through a ring of shared-memory
+ * stages filled by bulk asynchronous copies (cp.async.bulk + mbarrier, one
+ * persistent block set) instead of the default grid-stride vector loads. */
+#define MF_FLAG_BULK_PIPELINE 4u
 
 int mf_kernel_build(mf_context* ctx, const mf_kernel_desc* desc, mf_kernel** out);
 int mf_kernel_free(mf_kernel* k);
@@ -177,6 +201,15 @@ int mf_kernel_reduce_async(mf_kernel* k, const mf_buffer* input, uint64_t stride
  * parameter points per host call (several fits' requests, toy batches). */
 int mf_kernel_reduce_many(mf_kernel* k, uint32_t count, const mf_buffer* const* inputs, const uint64_t* strides,
                           const uint64_t* ns, const double* params, uint32_t n_params, mf_buffer* out);
+
+/* Compensated sums over events of ncols columns of an SoA event block:
+ * sums[c] = sum_{i<n} column c (element type MF_F64 or MF_F32, column stride
+ * `stride`), one launch, fixed summation order. Replaces the host-side
+ * kahan_summation(EventVector, dim) (include/utils.hh:28-41) that the fitter
+ * applies to per-event output buffers when kahan_on_accelerator is off
+ * (include/fitter.hh:1082-1108), and the OpenCL backend's multi-pass Kahan
+ * reduction kernels (include/compute_opencl.hh:807-991). */
+int mf_columns_sum(const mf_buffer* buf, int elem_type, uint32_t ncols, uint64_t n, uint64_t stride, double* sums);
 
 /* The context's cudaStream_t, as an opaque pointer (interop: events, graphs). */
 int mf_context_stream(mf_context* ctx, void** stream);

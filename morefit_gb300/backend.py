@@ -137,7 +137,8 @@ class Kernel:
 
 
 def make_desc(name: str, kind: int, elem: int, inputs: Sequence[str], params: Sequence[str],
-              exprs: Sequence[str], gen=None):
+              exprs: Sequence[str], gen=None, native_f64: bool = False, vec: int = 0, block: int = 0,
+              f32_arith: bool = False, pipeline: bool = False, stages: int = 0):
     keep = {"inputs": L.cstrings(list(inputs)), "params": L.cstrings(list(params)),
             "exprs": L.cstrings(list(exprs)), "name": name.encode()}
     d = L.KernelDesc()
@@ -150,6 +151,11 @@ def make_desc(name: str, kind: int, elem: int, inputs: Sequence[str], params: Se
     d.param_names = C.cast(keep["params"], L.c_char_pp)
     d.n_outputs = len(exprs)
     d.exprs = C.cast(keep["exprs"], L.c_char_pp)
+    d.flags = ((L.MF_FLAG_NATIVE_F64 if native_f64 else 0) | (L.MF_FLAG_F32_ARITH if f32_arith else 0)
+               | (L.MF_FLAG_BULK_PIPELINE if pipeline else 0))
+    d.vec = vec
+    d.block = block
+    d.stages = stages
     if gen is not None:
         dims, lo, hi, maxprob = gen
         keep["gd"] = L.cstrings(list(dims))
@@ -163,17 +169,20 @@ def make_desc(name: str, kind: int, elem: int, inputs: Sequence[str], params: Se
     return d, keep
 
 
-def build_kernel(backend: CUDABackend, name: str, kind: int, elem: int, inputs, params, exprs, gen=None) -> Kernel:
-    d, keep = make_desc(name, kind, elem, inputs, params, exprs, gen)
+def build_kernel(backend: CUDABackend, name: str, kind: int, elem: int, inputs, params, exprs, gen=None,
+                 native_f64: bool = False, vec: int = 0, block: int = 0, f32_arith: bool = False,
+                 pipeline: bool = False, stages: int = 0) -> Kernel:
+    d, keep = make_desc(name, kind, elem, inputs, params, exprs, gen, native_f64, vec, block, f32_arith, pipeline, stages)
     h = L.c_ker()
     L.check(L.lib.mf_kernel_build(backend.handle, C.byref(d), C.byref(h)))
     del keep
     return Kernel(h, kind, len(exprs), len(params))
 
 
-def lower_source(name: str, kind: int, elem: int, inputs, params, exprs, gen=None) -> str:
+def lower_source(name: str, kind: int, elem: int, inputs, params, exprs, gen=None, native_f64: bool = False,
+                 vec: int = 0, block: int = 0, f32_arith: bool = False, pipeline: bool = False, stages: int = 0) -> str:
     """CUDA C the library generates for these expressions (no GPU needed)."""
-    d, keep = make_desc(name, kind, elem, inputs, params, exprs, gen)
+    d, keep = make_desc(name, kind, elem, inputs, params, exprs, gen, native_f64, vec, block, f32_arith, pipeline, stages)
     need = C.c_size_t()
     L.check(L.lib.mf_lower_source(C.byref(d), None, 0, C.byref(need)))
     buf = C.create_string_buffer(need.value)
@@ -181,9 +190,10 @@ def lower_source(name: str, kind: int, elem: int, inputs, params, exprs, gen=Non
     return buf.value.decode()
 
 
-def compile_check(name: str, kind: int, elem: int, inputs, params, exprs, gen=None) -> dict:
+def compile_check(name: str, kind: int, elem: int, inputs, params, exprs, gen=None, native_f64: bool = False,
+                  vec: int = 0, block: int = 0, f32_arith: bool = False, pipeline: bool = False, stages: int = 0) -> dict:
     """NVRTC-compiles the lowered kernel for sm_103a without a GPU."""
-    d, keep = make_desc(name, kind, elem, inputs, params, exprs, gen)
+    d, keep = make_desc(name, kind, elem, inputs, params, exprs, gen, native_f64, vec, block, f32_arith, pipeline, stages)
     r, s = C.c_int(), C.c_int()
     L.check(L.lib.mf_compile_check(C.byref(d), C.byref(r), C.byref(s)))
     return {"registers": r.value, "spill_bytes": s.value}
@@ -205,9 +215,15 @@ class CUDABlock:
     precision: FP32 storage and per-event arithmetic, FP64 sums).
     """
 
-    def __init__(self, backend: CUDABackend, kernelT=np.float64):
+    def __init__(self, backend: CUDABackend, kernelT=np.float64, native_f64: bool = False, vec: int = 0,
+                 block: int = 0, f32_arith: bool = False, pipeline: bool = False, stages: int = 0):
         self.backend = backend
-        self.elem = L.MF_F32 if np.dtype(kernelT) == np.float32 else L.MF_F64
+        self.native_f64 = native_f64
+        self.f32_arith = f32_arith
+        self.pipeline = pipeline
+        self.shape = (vec, block, stages)
+        # FP32 arithmetic over FP64 columns keeps FP64 storage
+        self.elem = L.MF_F32 if (np.dtype(kernelT) == np.float32 and not f32_arith) else L.MF_F64
         self.kernelT = np.dtype(kernelT)
         self.input = DeviceColumns(backend, self.elem)
         self.output = DeviceColumns(backend, self.elem)
@@ -272,7 +288,10 @@ class CUDABlock:
         self.kahan = bool(kahan_summation)
         self.nout = len(graphs)
         kind = L.MF_KERNEL_REDUCE if self.kahan else L.MF_KERNEL_STORE
-        self.kernel = build_kernel(self.backend, name, kind, self.elem, input_signature, params, graphs)
+        self.kernel = build_kernel(self.backend, name, kind, self.elem, input_signature, params, graphs,
+                                   native_f64=self.native_f64, vec=self.shape[0], block=self.shape[1],
+                                   f32_arith=self.f32_arith and kind == L.MF_KERNEL_REDUCE, pipeline=self.pipeline,
+                                   stages=self.shape[2])
         self._sums = np.zeros(self.nout)
         self.nevents = int(nevents)
         return True

@@ -1,0 +1,129 @@
+// Compensated sums of per-event columns on the device.
+//
+// Replaces the host-side Kahan summation of a block's per-event output
+// buffer (reference include/utils.hh:28-41, used by include/fitter.hh:1082-1108
+// when kahan_on_accelerator is off) and the OpenCL backend's separate
+// multi-pass Kahan reduction kernels (include/compute_opencl.hh:807-991):
+// one launch sums every column of an SoA block. Each thread keeps a
+// double-float partial per column (FP32 pipe; GB300 issues FP64 at 1/64 of
+// the FP32 rate), the block reduces them in a fixed order, every block
+// writes its partials, and the last block to finish combines them in block
+// order, so the result is reproducible for a given n.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstring>
+#include <string>
+
+#include "../../include/morefit_cuda.h"
+#include "mf_internal.h"
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kMaxGrid = 1024;  // partial rows per launch
+
+struct dw {
+  float h, l;
+};
+__device__ __forceinline__ dw two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ dw fast_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ dw dw_add(dw a, dw b) {
+  const dw s = two_sum(a.h, b.h);
+  return fast_two_sum(s.h, __fadd_rn(__fadd_rn(a.l, b.l), s.l));
+}
+// Exact-to-48-bits split of an FP64 value (one conversion; the column kernel
+// is memory bound, so the FP64 pipe is not the limit here).
+__device__ __forceinline__ dw split(double x) {
+  const float h = __double2float_rn(x);
+  return {h, __double2float_rn(x - (double)h)};
+}
+__device__ __forceinline__ dw split(float x) { return {x, 0.0f}; }
+__device__ __forceinline__ dw shfl_xor(dw a, int o) {
+  return {__shfl_xor_sync(0xffffffffu, a.h, o), __shfl_xor_sync(0xffffffffu, a.l, o)};
+}
+
+// One column at a time: grid-stride partial per thread, warp tree, block pass.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) columns_sum_kernel(const T* __restrict__ data, uint64_t stride, uint64_t n,
+                                                                uint32_t ncols, float2* __restrict__ partials,
+                                                                unsigned* __restrict__ counter, double* __restrict__ out) {
+  __shared__ float2 red[kThreads / 32];
+  __shared__ bool am_last;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (uint32_t c = 0; c < ncols; c++) {
+    const T* __restrict__ col = data + (uint64_t)c * stride;
+    dw acc = {0.0f, 0.0f};
+    for (uint64_t i = (uint64_t)blockIdx.x * kThreads + threadIdx.x; i < n; i += (uint64_t)gridDim.x * kThreads)
+      acc = dw_add(acc, split(col[i]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc = dw_add(acc, shfl_xor(acc, o));
+    if (lane == 0) red[warp] = make_float2(acc.h, acc.l);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      dw b = {red[0].x, red[0].y};
+      for (int w = 1; w < kThreads / 32; w++) b = dw_add(b, dw{red[w].x, red[w].y});
+      partials[(uint64_t)blockIdx.x * ncols + c] = make_float2(b.h, b.l);
+    }
+    __syncthreads();
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) am_last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+  __syncthreads();
+  if (!am_last) return;
+  __threadfence();
+  for (uint32_t c = 0; c < ncols; c++) {
+    dw acc = {0.0f, 0.0f};
+    for (unsigned b = threadIdx.x; b < gridDim.x; b += kThreads) {
+      const float2 p = __ldcg(partials + (uint64_t)b * ncols + c);
+      acc = dw_add(acc, dw{p.x, p.y});
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc = dw_add(acc, shfl_xor(acc, o));
+    if (lane == 0) red[warp] = make_float2(acc.h, acc.l);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      dw b = {red[0].x, red[0].y};
+      for (int w = 1; w < kThreads / 32; w++) b = dw_add(b, dw{red[w].x, red[w].y});
+      out[c] = (double)b.h + (double)b.l;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *counter = 0u;
+}
+
+int grid_for(uint64_t n, int num_sms) {
+  const uint64_t need = (n + kThreads - 1) / kThreads;
+  const uint64_t cap = std::min<uint64_t>(kMaxGrid, uint64_t(num_sms) * 4);
+  return int(std::max<uint64_t>(1, std::min(need, cap)));
+}
+
+}  // namespace
+
+namespace mfi {
+
+int columns_sum_launch(const void* data, int elem, uint64_t stride, uint64_t n, uint32_t ncols, void* partials,
+                       unsigned* counter, double* out, cudaStream_t stream, int num_sms) {
+  const int grid = grid_for(n, num_sms);
+  if (elem == MF_F32)
+    columns_sum_kernel<float><<<grid, kThreads, 0, stream>>>(static_cast<const float*>(data), stride, n, ncols,
+                                                             static_cast<float2*>(partials), counter, out);
+  else
+    columns_sum_kernel<double><<<grid, kThreads, 0, stream>>>(static_cast<const double*>(data), stride, n, ncols,
+                                                              static_cast<float2*>(partials), counter, out);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return set_error(MF_ERR_CUDA, std::string("columns_sum launch: ") + cudaGetErrorString(e));
+  return MF_OK;
+}
+
+int columns_sum_partials(uint64_t n, int num_sms) { return grid_for(n, num_sms); }
+
+}  // namespace mfi

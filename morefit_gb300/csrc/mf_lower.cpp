@@ -476,6 +476,166 @@ __device__ __forceinline__ void mf_kahan_f32(float& s, float& c, float x) {
 }
 )CUDA";
 
+// Double-float ("double-word") arithmetic on pairs of FP32 values, used by
+// FP64 REDUCE kernels. GB300 issues FP32 at 64x its FP64 rate; a value is
+// kept as an unevaluated sum h + l of two floats (|l| <= ulp(h)/2, ~48
+// significant bits) and combined with error-free transforms: TwoSum (Knuth),
+// FastTwoSum (Dekker 1971) and the FMA-based TwoProd; addition and
+// multiplication follow the double-word algorithms analysed by Joldes, Muller
+// and Popescu (ACM TOMS 44, 2017). The logarithm is table driven in the manner
+// of Tang (ACM TOMS 16, 1990): log y = E ln2 + ln c_j + ln(1+t) with c_j the
+// centre of one of 128 mantissa intervals, |t| <= 2^-8 and a short series.
+// Operations without a double-float form fall back to FP64 on the value.
+const char* kDwPrelude = R"CUDA(
+struct mf_dw { float h, l; };
+__device__ __forceinline__ mf_dw mf_dw_make(float h, float l) { mf_dw r; r.h = h; r.l = l; return r; }
+__device__ __forceinline__ mf_dw mf_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  return mf_dw_make(s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb)));
+}
+__device__ __forceinline__ mf_dw mf_fast_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  return mf_dw_make(s, __fsub_rn(b, __fsub_rn(s, a)));
+}
+__device__ __forceinline__ mf_dw mf_dw_add(mf_dw a, mf_dw b) {
+  const mf_dw s = mf_two_sum(a.h, b.h);
+  return mf_fast_two_sum(s.h, __fadd_rn(__fadd_rn(a.l, b.l), s.l));
+}
+__device__ __forceinline__ mf_dw mf_dw_neg(mf_dw a) { return mf_dw_make(-a.h, -a.l); }
+__device__ __forceinline__ mf_dw mf_dw_sub(mf_dw a, mf_dw b) { return mf_dw_add(a, mf_dw_neg(b)); }
+__device__ __forceinline__ mf_dw mf_dw_mul(mf_dw a, mf_dw b) {
+  const float p = __fmul_rn(a.h, b.h);
+  const float e = __fmaf_rn(a.h, b.l, __fmaf_rn(a.l, b.h, __fmaf_rn(a.h, b.h, -p)));
+  return mf_fast_two_sum(p, e);
+}
+__device__ __forceinline__ mf_dw mf_dw_rcp(mf_dw a) {
+  // r = 1/a.h, then one Newton correction with the residual 1 - a*r formed exactly to first order.
+  const float r = __frcp_rn(a.h);
+  const float p = __fmul_rn(a.h, r);
+  const float pe = __fmaf_rn(a.h, r, -p);
+  const float e = __fsub_rn(__fsub_rn(__fsub_rn(1.0f, p), pe), __fmul_rn(a.l, r));
+  return mf_fast_two_sum(r, __fmul_rn(r, e));
+}
+__device__ __forceinline__ double mf_dw_to_double(mf_dw a) { return (double)a.h + (double)a.l; }
+__device__ __forceinline__ mf_dw mf_dw_from_double(double x) {
+  const float h = __double2float_rn(x);
+  return mf_dw_make(h, __double2float_rn(x - (double)h));
+}
+// Splits an FP64 value into h + l with integer and FP32 operations only (no
+// FP64 pipe, no conversion instructions, no branch): h keeps the top 24
+// significand bits (truncated), l the next 23. Magnitudes below 2^-126 give
+// h = l = 0 (an absolute error below 1.2e-38), l underflows to 0 below
+// 2^-81, magnitudes from 2^128 on give +-inf, NaN stays NaN.
+__device__ __forceinline__ mf_dw mf_dw_split(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned hi32 = (unsigned)(b >> 32), lo32 = (unsigned)b;
+  const unsigned e = (hi32 >> 20) & 0x7ffu;
+  const unsigned sign = hi32 & 0x80000000u;
+  const unsigned hnorm = sign | ((e - 896u) << 23) | ((hi32 & 0xfffffu) << 3) | (lo32 >> 29);
+  const unsigned hbig = sign | 0x7f800000u | ((e == 2047u && ((hi32 & 0xfffffu) | lo32)) ? 0x400000u : 0u);
+  const unsigned hb = e > 1150u ? hbig : (e >= 897u ? hnorm : sign);
+  // top 23 of the 29 remaining bits as an exact float (exponent-field trick), scaled by 2^(e - 1069)
+  const float r23 = __fsub_rn(__uint_as_float(0x4b000000u | ((lo32 & 0x1fffffffu) >> 6)), 8388608.0f);
+  const unsigned sb = (e >= 943u && e <= 1150u) ? ((e - 942u) << 23) : 0u;
+  const float l = __fmul_rn(r23, __uint_as_float(sb));
+  return mf_dw_make(__uint_as_float(hb), __uint_as_float(__float_as_uint(l) | sign));
+}
+// ln of a positive double-float (see above); zero gives -inf, negative or
+// NaN gives NaN, +inf gives +inf, subnormal h is rescaled by 2^64 first.
+__device__ __forceinline__ mf_dw mf_dw_log(mf_dw a, const float4* __restrict__ tab) {
+  const bool sub = a.h > 0.0f && a.h < 1.17549435e-38f;
+  const float ah = sub ? __fmul_rn(a.h, 18446744073709551616.0f) : a.h;
+  const float al = sub ? __fmul_rn(a.l, 18446744073709551616.0f) : a.l;
+  const unsigned bits = __float_as_uint(ah);
+  const int E = (int)((bits >> 23) & 0xffu) - 127;
+  const float m = __uint_as_float((bits & 0x007fffffu) | 0x3f800000u);
+  const float4 T = tab[(bits >> 16) & 0x7fu];  // {ln c hi, ln c lo, 1/c, c}
+  const unsigned se = (unsigned)(127 - E);
+  const float yl = __fmul_rn(al, __uint_as_float(se >= 1u && se <= 254u ? (se << 23) : 0u));
+  const mf_dw N = mf_two_sum(__fsub_rn(m, T.w), yl);
+  const float th = __fmul_rn(N.h, T.z);
+  const float tl = __fmul_rn(__fadd_rn(__fmaf_rn(-th, T.w, N.h), N.l), T.z);
+  const float sh = __fmul_rn(th, th);
+  const float sl = __fmaf_rn(2.0f * th, tl, __fmaf_rn(th, th, -sh));
+  mf_dw lt = mf_dw_sub(mf_dw_make(th, tl), mf_dw_make(0.5f * sh, 0.5f * sl));
+  const float P = __fmaf_rn(th, __fmaf_rn(th, __fmaf_rn(th, __fmaf_rn(th, 0.142857143f, -0.166666667f), 0.2f), -0.25f),
+                            0.333333333f);
+  lt = mf_dw_add(lt, mf_dw_make(__fmul_rn(__fmul_rn(sh, th), P), 0.0f));
+  const int Et = E - (sub ? 64 : 0);
+  const float Ef = __fsub_rn(__int_as_float(0x4b400000 + Et), 12582912.0f);  // (float)Et without a conversion
+  const float eh = __fmul_rn(Ef, MF_LN2_HI);
+  const mf_dw el = mf_fast_two_sum(eh, __fmaf_rn(Ef, MF_LN2_LO, __fmaf_rn(Ef, MF_LN2_HI, -eh)));
+  mf_dw r = mf_dw_add(mf_dw_add(el, mf_dw_make(T.x, T.y)), lt);
+  const float inf = __uint_as_float(0x7f800000u);
+  if (a.h == 0.0f) r = mf_dw_make(-inf, 0.0f);
+  if (!(a.h >= 0.0f)) r = mf_dw_make(__uint_as_float(0x7fc00000u), 0.0f);
+  if (a.h == inf) r = mf_dw_make(inf, 0.0f);
+  return r;
+}
+__device__ __forceinline__ mf_dw mf_dw_shfl_xor(mf_dw a, int o) {
+  return mf_dw_make(__shfl_xor_sync(0xffffffffu, a.h, o), __shfl_xor_sync(0xffffffffu, a.l, o));
+}
+)CUDA";
+
+// Bulk asynchronous global->shared copies completed on an mbarrier (sm_90+
+// PTX: cp.async.bulk, mbarrier.*). Both addresses 16-byte aligned, sizes a
+// multiple of 16 bytes.
+const char* kBulkPrelude = R"CUDA(
+__device__ __forceinline__ unsigned mf_smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mf_mbar_init(unsigned long long* b, unsigned cnt) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mf_smem_u32(b)), "r"(cnt) : "memory");
+}
+__device__ __forceinline__ void mf_fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void mf_fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void mf_mbar_expect_tx(unsigned long long* b, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mf_smem_u32(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mf_bulk_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* b) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+               ::"r"(mf_smem_u32(dst)), "l"(src), "r"(bytes), "r"(mf_smem_u32(b)) : "memory");
+}
+__device__ __forceinline__ unsigned mf_mbar_try_wait(unsigned long long* b, unsigned parity) {
+  unsigned ok;
+  asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+               : "=r"(ok) : "r"(mf_smem_u32(b)), "r"(parity) : "memory");
+  return ok;
+}
+// Bounded wait: false after MF_SPIN_LIMIT unsuccessful polls.
+#define MF_SPIN_LIMIT (1u << 22)
+__device__ __forceinline__ bool mf_mbar_wait_bounded(unsigned long long* b, unsigned parity) {
+  for (unsigned i = 0; i < MF_SPIN_LIMIT; i++)
+    if (mf_mbar_try_wait(b, parity)) return true;
+  return false;
+}
+)CUDA";
+
+// The 128-entry table of mf_dw_log: for c_j = 1 + (2j+1)/256,
+// {hi(ln c_j), lo(ln c_j), 1/c_j, c_j} as exact float literals.
+std::string dw_log_table() {
+  std::ostringstream o;
+  {
+    const double ln2 = std::log(2.0);
+    const float hi = float(ln2), lo = float(ln2 - double(hi));
+    char b[160];
+    std::snprintf(b, sizeof b, "#define MF_LN2_HI %af\n#define MF_LN2_LO %af\n", double(hi), double(lo));
+    o << b;
+  }
+  o << "__device__ const float4 mf_dw_logtab_g[128] = {\n";
+  for (int j = 0; j < 128; j++) {
+    const double c = 1.0 + (2.0 * j + 1.0) / 256.0;
+    const double L = std::log(c);
+    const float lh = float(L);
+    const float ll = float(L - double(lh));
+    const float ic = float(1.0 / c);
+    char b[200];
+    std::snprintf(b, sizeof b, "  {%af, %af, %af, %af},\n", double(lh), double(ll), double(ic), c);
+    o << b;
+  }
+  o << "};\n";
+  return o.str();
+}
+
 }  // namespace
 
 OpCount count_ops(const std::vector<std::string>& inputs, const std::vector<std::string>& params,
@@ -503,7 +663,8 @@ OpCount count_ops(const std::vector<std::string>& inputs, const std::vector<std:
 
 LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::vector<std::string>& inputs,
                     const std::vector<std::string>& params, const std::vector<std::string>& exprs,
-                    const GenerateSpec* gen) {
+                    const GenerateSpec* gen, bool native_f64, int vec_req, int block_req, bool f32_arith,
+                    bool direct_loads, int stages_req) {
   std::vector<std::string> in_names = inputs;
   if (kind == Kind::Generate) {
     if (!gen) throw std::runtime_error("generate kernel without generate spec");
@@ -529,6 +690,22 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
   out.entry = "mf_" + std::string(kind == Kind::Reduce ? "reduce" : kind == Kind::Store ? "store" : "generate");
   out.block = 256;
   out.vec = (kind == Kind::Generate) ? 1 : (st32 ? 4 : 2);
+  if (kind == Kind::Reduce) {
+    out.pipelined = !direct_loads;
+    // double-float bodies: one event per thread per iteration, 512 threads
+    // (measured fastest on GB300 for the K*mumu gradient kernel)
+    const bool dw_default = !st32 && !native_f64 && !f32_arith;
+    if (dw_default) {
+      out.vec = 1;
+      // 512 threads (<= 128 registers) for gradient-sized kernels; many-output
+      // kernels (Hessians) keep 256 threads so their accumulators stay in registers
+      if (!out.pipelined && exprs.size() <= 16) out.block = 512;
+    }
+    if (vec_req == 1 || vec_req == 2 || (vec_req == 4 && st32)) out.vec = vec_req;
+    if (block_req >= 64 && block_req <= 1024 && block_req % 32 == 0) out.block = block_req;
+    out.stages = stages_req >= 2 && stages_req <= 8 ? stages_req : (dw_default ? 3 : 4);
+    out.tile = out.block * out.vec;
+  }
   const int V = out.vec;
   const int M = int(exprs.size());
   const int NP = std::max<int>(1, int(params.size()));
@@ -542,11 +719,14 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
   s << "// MoreFit CUDA backend: generated kernel '" << name << "' (" << (kind == Kind::Reduce ? "reduce"
                                                                           : kind == Kind::Store ? "store"
                                                                                                 : "generate")
-    << ", " << ST << " storage, " << AT << " arithmetic)\n";
+    << ", " << ST << " storage, "
+    << (kind == Kind::Reduce && !st32 && !native_f64 ? std::string("double-float") : AT) << " arithmetic)\n";
   s << "// outputs:\n";
   for (size_t j = 0; j < exprs.size(); j++) s << "//   [" << j << "] " << exprs[j].substr(0, 160) << "\n";
   s << kPrelude;
   s << "#define MF_BLOCK " << out.block << "\n#define MF_NOUT " << M << "\n#define MF_NPAR " << NP << "\n";
+  // partial blocks each last-block thread loads per round (bounded register use)
+  s << "#define MF_Q " << std::max(1, 32 / std::max(1, M)) << "\n";
   s << "struct mf_par { double v[MF_NPAR]; };\n";
 
   // Parameter-only prologue (u*), emitted once per thread.
@@ -574,56 +754,319 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
   };
 
   if (kind == Kind::Reduce) {
-    const std::string ACC = ar32 ? "float" : "double";
+    // Arithmetic of the per-event body: FP32 (mixed precision), FP64, or
+    // double-float on FP32 pairs (the default for FP64 storage).
+    // F32S: FP64 storage, FP32 arithmetic, except that a sum or difference of
+    // an input column and a parameter-only value is formed in FP64 before it
+    // is rounded (keeps m - mu exact for observables with a large offset).
+    enum class Ar { F32, F64, DW, F32S } ar =
+        st32 ? Ar::F32 : (f32_arith ? Ar::F32S : (native_f64 ? Ar::F64 : Ar::DW));
+    auto is_leafish = [&](int k) {
+      const Op o = ns[k].op;
+      return o == Op::Input || ns[k].uniform;
+    };
+    // per-event nodes evaluated in FP64 under F32S
+    std::vector<char> dnode(ns.size(), 0);
+    if (ar == Ar::F32S)
+      for (size_t i = 0; i < ns.size(); i++) {
+        const Node& n = ns[i];
+        if (!live[i] || n.uniform || (n.op != Op::Add && n.op != Op::Sub)) continue;
+        if (is_leafish(n.a) && is_leafish(n.b) && (ns[n.a].op == Op::Input || ns[n.b].op == Op::Input)) dnode[i] = 1;
+      }
+    bool has_log = false;
+    for (size_t i = 0; i < ns.size(); i++)
+      if (live[i] && !ns[i].uniform && ns[i].op == Op::Log) has_log = true;
+    // The double-float library is always present: every cross-thread sum
+    // (warp, block, grid) runs in double-float on the FP32 pipe.
+    s << dw_log_table() << kDwPrelude << kBulkPrelude;
+    // ---- leaves and statements of the per-event body ----
+    auto eref = [&](int id) -> std::string {
+      const Node& n = ns[id];
+      if (ar == Ar::F32S) {  // float view of any node
+        if (n.op == Op::Const) return fmt_const(n.value, true);
+        if (n.op == Op::Input) return "(float)x" + std::to_string(n.index);
+        if (n.op == Op::Param) return "pf" + std::to_string(n.index);
+        if (n.uniform) return "uf" + std::to_string(id);
+        if (dnode[id]) return "(float)e" + std::to_string(id);
+        return "e" + std::to_string(id);
+      }
+      if (n.op == Op::Const) {
+        if (ar == Ar::F32) return fmt_const(n.value, true);
+        if (ar == Ar::F64) return fmt_const(n.value, false);
+        const float h = float(n.value);
+        const float l = float(n.value - double(h));
+        char b[96];
+        std::snprintf(b, sizeof b, "mf_dw_make(%af, %af)", double(h), double(l));
+        return b;
+      }
+      if (n.op == Op::Input) return "x" + std::to_string(n.index);
+      const std::string sfx = ar == Ar::F32 ? "f" : ar == Ar::DW ? "w" : "";
+      if (n.op == Op::Param) return "p" + sfx + std::to_string(n.index);
+      if (n.uniform) return "u" + sfx + std::to_string(id);
+      return "e" + std::to_string(id);
+    };
+    auto dref = [&](int k) -> std::string {  // FP64 view of an input / uniform / constant (F32S only)
+      const Node& n = ns[k];
+      if (n.op == Op::Const) return fmt_const(n.value, false);
+      if (n.op == Op::Input) return "x" + std::to_string(n.index);
+      if (n.op == Op::Param) return "p" + std::to_string(n.index);
+      return "u" + std::to_string(k);
+    };
+    auto estmt = [&](int id) -> std::string {
+      const Node& n = ns[id];
+      if (ar == Ar::F32S && dnode[id])
+        return "const double e" + std::to_string(id) + " = " + dref(n.a) + (n.op == Op::Add ? " + " : " - ") + dref(n.b) +
+               ";";
+      const std::string T = ar == Ar::F32 || ar == Ar::F32S ? "float" : ar == Ar::F64 ? "double" : "mf_dw";
+      const std::string lhs = "const " + std::string(n.op == Op::Cmp ? "bool" : T) + " e" + std::to_string(id) + " = ";
+      const std::string A = n.a >= 0 ? eref(n.a) : "", B = n.b >= 0 ? eref(n.b) : "", Cc = n.c >= 0 ? eref(n.c) : "";
+      if (ar != Ar::DW) {
+        const bool f = ar == Ar::F32 || ar == Ar::F32S;
+        switch (n.op) {
+          case Op::Add: return lhs + A + " + " + B + ";";
+          case Op::Sub: return lhs + A + " - " + B + ";";
+          case Op::Mul: return lhs + A + " * " + B + ";";
+          case Op::Div: return lhs + A + " / " + B + ";";
+          case Op::Neg: return lhs + "-" + A + ";";
+          case Op::Rcp: return lhs + fn_name(Op::Rcp, f) + "(" + A + ");";
+          case Op::Pow: return lhs + fn_name(Op::Pow, f) + "(" + A + ", " + B + ");";
+          case Op::Cmp: return lhs + "(" + A + " " + cmp_str(n.cmp) + " " + B + ");";
+          case Op::Select: return lhs + "(" + A + " ? " + B + " : " + Cc + ");";
+          default:
+            if (is_unary_fn(n.op)) return lhs + fn_name(n.op, f) + "(" + A + ");";
+        }
+        throw std::runtime_error("emit: unexpected node");
+      }
+      auto D = [](const std::string& v) { return "mf_dw_to_double(" + v + ")"; };
+      switch (n.op) {
+        case Op::Add: return lhs + "mf_dw_add(" + A + ", " + B + ");";
+        case Op::Sub: return lhs + "mf_dw_sub(" + A + ", " + B + ");";
+        case Op::Mul: return lhs + "mf_dw_mul(" + A + ", " + B + ");";
+        case Op::Div: return lhs + "mf_dw_mul(" + A + ", mf_dw_rcp(" + B + "));";
+        case Op::Neg: return lhs + "mf_dw_neg(" + A + ");";
+        case Op::Rcp: return lhs + "mf_dw_rcp(" + A + ");";
+        case Op::Log: return lhs + "mf_dw_log(" + A + ", mf_logtab);";
+        case Op::Pow: return lhs + "mf_dw_from_double(pow(" + D(A) + ", " + D(B) + "));";
+        case Op::Cmp: return lhs + "(" + D(A) + " " + cmp_str(n.cmp) + " " + D(B) + ");";
+        case Op::Select: return lhs + "(" + A + " ? " + B + " : " + Cc + ");";
+        default:
+          if (is_unary_fn(n.op)) return lhs + "mf_dw_from_double(" + fn_name(n.op, false) + "(" + D(A) + "));";
+      }
+      throw std::runtime_error("emit: unexpected node");
+    };
+    // Uniform (parameter-only) values referenced by the per-event body or by an output.
+    std::set<int> uni_used;
+    auto note_uniform = [&](int k) {
+      if (k >= 0 && ns[k].uniform && ns[k].op != Op::Const) uni_used.insert(k);
+    };
+    for (size_t i = 0; i < ns.size(); i++) {
+      if (!live[i] || ns[i].uniform || ns[i].op == Op::Input || dnode[i]) continue;
+      note_uniform(ns[i].a);
+      note_uniform(ns[i].b);
+      note_uniform(ns[i].c);
+    }
+    for (int r : roots) note_uniform(r);
+    // Parameter-only values: evaluated once per launch on the host and passed
+    // pre-rounded in the argument struct (no FP64 work in the kernel, where
+    // FP64 issues at 1/64 of the FP32 rate).
+    std::map<int, std::string> slot_names;  // node -> C name in the body
+    {
+      std::vector<UniformSlot> slots;
+      int nd = 0, nf = 0;
+      auto add_slot = [&](int k, int kind) {
+        UniformSlot sl{k, kind, kind == UniformSlot::Double ? nd : nf};
+        if (kind == UniformSlot::Double)
+          nd++;
+        else
+          nf += kind == UniformSlot::DwPair ? 2 : 1;
+        slots.push_back(sl);
+      };
+      std::set<int> dslots;  // nodes needed as doubles
+      if (ar == Ar::F64) dslots = uni_used;
+      if (ar == Ar::F32S)
+        for (size_t i = 0; i < ns.size(); i++)
+          if (dnode[i]) {
+            if (ns[ns[i].a].uniform && ns[ns[i].a].op != Op::Const) dslots.insert(ns[i].a);
+            if (ns[ns[i].b].uniform && ns[ns[i].b].op != Op::Const) dslots.insert(ns[i].b);
+          }
+      for (int k : dslots) {
+        add_slot(k, UniformSlot::Double);
+        slot_names[k] = ns[k].op == Op::Param ? "p" + std::to_string(ns[k].index) : "u" + std::to_string(k);
+      }
+      if (ar != Ar::F64)
+        for (int k : uni_used)
+          add_slot(k, ns[k].op == Op::Cmp ? UniformSlot::Bool : ar == Ar::DW ? UniformSlot::DwPair : UniformSlot::Float);
+      out.host_args = true;
+      out.nodes = ns;
+      out.slots = slots;
+      out.nd = std::max(1, nd);
+      out.nf = std::max(1, nf);
+    }
+    auto prologue = [&](std::ostringstream& o, const std::string& P) {
+      for (const auto& sl : out.slots) {
+        const int k = sl.node;
+        const std::string off = std::to_string(sl.offset);
+        switch (sl.kind) {
+          case UniformSlot::Double: o << "  const double " << slot_names[k] << " = " << P << "d[" << off << "];\n"; break;
+          case UniformSlot::Float: o << "  const float " << eref(k) << " = " << P << "f[" << off << "];\n"; break;
+          case UniformSlot::Bool: o << "  const bool " << eref(k) << " = " << P << "f[" << off << "] != 0.0f;\n"; break;
+          case UniformSlot::DwPair:
+            o << "  const mf_dw " << eref(k) << " = mf_dw_make(" << P << "f[" << off << "], " << P << "f["
+              << sl.offset + 1 << "]);\n";
+            break;
+        }
+      }
+    };
+    auto body = [&](std::ostringstream& o, const std::string& ind) {
+      for (size_t i = 0; i < ns.size(); i++) {
+        if (!live[i] || ns[i].uniform || ns[i].op == Op::Input) continue;
+        o << ind << estmt(int(i)) << "\n";
+      }
+    };
+    // Accumulation of output j from the body's value (per thread).
+    auto acc_decl = [&](std::ostringstream& o) {
+      if (ar == Ar::F32 || ar == Ar::F32S)
+        o << "  float acc[MF_NOUT], cmp[MF_NOUT];\n#pragma unroll\n  for (int j = 0; j < MF_NOUT; j++) { acc[j] = 0.0f; cmp[j] = 0.0f; }\n";
+      else if (ar == Ar::F64)
+        o << "  double acc[MF_NOUT];\n#pragma unroll\n  for (int j = 0; j < MF_NOUT; j++) acc[j] = 0.0;\n";
+      else
+        o << "  mf_dw acc[MF_NOUT];\n#pragma unroll\n  for (int j = 0; j < MF_NOUT; j++) acc[j] = mf_dw_make(0.0f, 0.0f);\n";
+    };
+    auto acc_add = [&](std::ostringstream& o, const std::string& ind) {
+      for (int j = 0; j < M; j++) {
+        const std::string r = eref(roots[j]);
+        if (ar == Ar::F32 || ar == Ar::F32S)
+          o << ind << "mf_kahan_f32(acc[" << j << "], cmp[" << j << "], " << r << ");\n";
+        else if (ar == Ar::F64)
+          o << ind << "acc[" << j << "] += " << r << ";\n";
+        else
+          o << ind << "acc[" << j << "] = mf_dw_add(acc[" << j << "], " << r << ");\n";
+      }
+    };
+    // Per-thread accumulator of output j as a double-float value, summed over
+    // the warp (lane 0 holds the result).
+    auto warp_sum = [&](std::ostringstream& o) {
+      if (ar == Ar::F32 || ar == Ar::F32S)
+        o << "    mf_dw a = mf_two_sum(acc[j], -cmp[j]);\n";
+      else if (ar == Ar::F64)
+        o << "    mf_dw a = mf_dw_split(acc[j]);\n";
+      else
+        o << "    mf_dw a = acc[j];\n";
+      o << "#pragma unroll\n    for (int o = 16; o > 0; o >>= 1) a = mf_dw_add(a, mf_dw_shfl_xor(a, o));\n";
+    };
+    auto load_table = [&](std::ostringstream& o) {
+      if (ar != Ar::DW || !has_log) return;
+      o << "  __shared__ float4 mf_logtab[128];\n"
+        << "  for (int q = threadIdx.x; q < 128; q += MF_BLOCK) mf_logtab[q] = mf_dw_logtab_g[q];\n"
+        << "  __syncthreads();\n";
+    };
+    auto input_value = [&](const std::string& raw) {
+      if (ar == Ar::DW) return "mf_dw_split(" + raw + ")";
+      return raw;
+    };
+    const std::string XT = ar == Ar::F32 ? "float" : (ar == Ar::F64 || ar == Ar::F32S) ? "double" : "mf_dw";
+
+    s << "struct mf_args { double d[" << out.nd << "]; float f[" << out.nf << "]; };\n";
     // ---- single-dataset reduce ----
     s << "extern \"C\" __global__ void __launch_bounds__(MF_BLOCK) " << out.entry << "(const " << ST
-      << "* __restrict__ data, mf_u64 stride, mf_u64 n, mf_par P, double* __restrict__ partials,"
-      << " unsigned* __restrict__ counter, double* __restrict__ out) {\n";
-    emit_params_and_uniform(s, "P.v");
-    s << "  " << ACC << " acc[MF_NOUT];\n";
-    if (ar32) s << "  float cmp[MF_NOUT];\n";
-    s << "#pragma unroll\n  for (int j = 0; j < MF_NOUT; j++) { acc[j] = 0; " << (ar32 ? "cmp[j] = 0; " : "") << "}\n";
-    s << "  const mf_u64 step = (mf_u64)gridDim.x * MF_BLOCK * " << V << ";\n";
-    s << "  for (mf_u64 base = ((mf_u64)blockIdx.x * MF_BLOCK + threadIdx.x) * " << V
-      << "; base < n; base += step) {\n";
-    const std::string VT = st32 ? "float4" : "double2";
-    for (int k : out.used_inputs)
-      s << "    const " << VT << " l" << k << " = __ldg(reinterpret_cast<const " << VT << "*>(data + (mf_u64)" << k
-        << " * stride + base));\n";
+      << "* __restrict__ data, mf_u64 stride, mf_u64 n, mf_args P, float2* __restrict__ partials,"
+      << " unsigned* __restrict__ counter, double* __restrict__ out, unsigned* __restrict__ status) {\n";
+    load_table(s);
+    prologue(s, "P.");
+    acc_decl(s);
+    const std::string VT = V == 1 ? ST : st32 ? (V == 4 ? "float4" : "float2") : "double2";
     const char* comp[4] = {"x", "y", "z", "w"};
-    for (int v = 0; v < V; v++) {
-      s << "    {\n";
-      for (int k : out.used_inputs) s << "      const " << AT << " x" << k << " = l" << k << "." << comp[v] << ";\n";
-      emit_body(s, "      ");
-      s << "      if (base + " << v << " < n) {\n";
-      for (int j = 0; j < M; j++) {
-        if (ar32)
-          s << "        mf_kahan_f32(acc[" << j << "], cmp[" << j << "], r" << j << ");\n";
-        else
-          s << "        acc[" << j << "] += r" << j << ";\n";
+    auto emit_events = [&](const std::string& ind, const std::string& idx0, const std::string& valid_base,
+                           const std::function<std::string(int)>& src) {
+      for (int k : out.used_inputs) s << ind << "const " << VT << " l" << k << " = " << src(k) << ";\n";
+      for (int v = 0; v < V; v++) {
+        s << ind << "{\n";
+        for (int k : out.used_inputs)
+          s << ind << "  const " << XT << " x" << k << " = "
+            << input_value("l" + std::to_string(k) + (V == 1 ? std::string("") : std::string(".") + comp[v])) << ";\n";
+        body(s, ind + "  ");
+        s << ind << "  if (" << valid_base << " + " << v << " < n) {\n";
+        acc_add(s, ind + "    ");
+        s << ind << "  }\n" << ind << "}\n";
       }
-      s << "      }\n    }\n";
+      (void)idx0;
+    };
+    const int NC = int(out.used_inputs.size());
+    if (out.pipelined && NC > 0) {
+      // Persistent blocks; tile t (events [t*MF_TILE, (t+1)*MF_TILE) of every
+      // column read by the body) goes to block t % gridDim.x. Thread 0 keeps
+      // MF_STAGES - 1 tiles in flight with bulk asynchronous copies into a
+      // ring of shared-memory stages; all threads wait on the stage's
+      // mbarrier (bounded), compute from shared memory and release the stage.
+      const size_t es = st32 ? 4 : 8;
+      out.smem_bytes = size_t(out.stages) * NC * out.tile * es;
+      s << "#define MF_TILE " << out.tile << "\n#define MF_STAGES " << out.stages << "\n#define MF_NC " << NC << "\n";
+      s << "  extern __shared__ __align__(128) unsigned char mf_dyn[];\n";
+      s << "  " << ST << "* __restrict__ stage = reinterpret_cast<" << ST << "*>(mf_dyn);\n";
+      s << "  __shared__ __align__(8) unsigned long long mf_bar[MF_STAGES];\n";
+      s << "  const mf_u64 ntiles = (n + MF_TILE - 1) / MF_TILE;\n";
+      s << "  if (threadIdx.x == 0) {\n    for (int q = 0; q < MF_STAGES; q++) mf_mbar_init(&mf_bar[q], 1u);\n"
+        << "    mf_fence_mbar_init();\n  }\n  __syncthreads();\n";
+      // issue lambda as a macro-like block
+      std::ostringstream issue;
+      issue << "{ const mf_u64 t0 = (TL) * (mf_u64)MF_TILE; mf_u64 cnt = stride - t0; if (cnt > MF_TILE) cnt = MF_TILE;\n"
+            << "          const unsigned bytes = (unsigned)(cnt * sizeof(" << ST << "));\n"
+            << "          mf_mbar_expect_tx(&mf_bar[SL], bytes * MF_NC);\n";
+      for (int ci = 0; ci < NC; ci++)
+        issue << "          mf_bulk_g2s(stage + ((mf_u64)(SL) * MF_NC + " << ci << ") * MF_TILE, data + (mf_u64)"
+              << out.used_inputs[ci] << " * stride + t0, bytes, &mf_bar[SL]);\n";
+      issue << "        }";
+      auto issue_code = [&](const std::string& tl, const std::string& sl) {
+        std::string c = issue.str();
+        for (size_t p; (p = c.find("(TL)")) != std::string::npos;) c.replace(p, 4, "(" + tl + ")");
+        for (size_t p; (p = c.find("SL")) != std::string::npos;) c.replace(p, 2, sl);
+        return c;
+      };
+      s << "  unsigned issued = 0;  // tiles issued by thread 0 (valid in thread 0)\n";
+      s << "  if (threadIdx.x == 0)\n    for (int q = 0; q < MF_STAGES - 1; q++) {\n"
+        << "      const mf_u64 tl = blockIdx.x + (mf_u64)q * gridDim.x;\n      if (tl < ntiles) {\n        "
+        << issue_code("tl", "q") << "\n        issued++;\n      }\n    }\n";
+      s << "  unsigned it = 0;\n  bool aborted = false;\n";
+      s << "  for (mf_u64 tile = blockIdx.x; tile < ntiles; tile += gridDim.x, it++) {\n";
+      s << "    const unsigned sl = it % MF_STAGES, par = (it / MF_STAGES) & 1u;\n";
+      s << "    if (threadIdx.x == 0) {\n      const mf_u64 nt = tile + (mf_u64)(MF_STAGES - 1) * gridDim.x;\n"
+        << "      if (nt < ntiles) {\n        const unsigned ns = (it + MF_STAGES - 1) % MF_STAGES;\n"
+        << "        mf_fence_proxy_async();\n        " << issue_code("nt", "ns") << "\n        issued++;\n      }\n    }\n";
+      s << "    const bool ok = mf_mbar_wait_bounded(&mf_bar[sl], par);\n";
+      s << "    if (__syncthreads_or(!ok)) { aborted = true; break; }\n";
+      s << "    const " << ST << "* __restrict__ sb = stage + (mf_u64)sl * MF_NC * MF_TILE;\n";
+      s << "    const mf_u64 tbase = tile * (mf_u64)MF_TILE;\n";
+      s << "    {\n      const int e0 = threadIdx.x * " << V << ";\n";
+      std::map<int, int> colpos;
+      for (int ci = 0; ci < NC; ci++) colpos[out.used_inputs[ci]] = ci;
+      emit_events("      ", "e0", "tbase + e0", [&](int k) {
+        return "*reinterpret_cast<const " + VT + "*>(sb + " + std::to_string(colpos[k]) + " * MF_TILE + e0)";
+      });
+      s << "    }\n    __syncthreads();\n  }\n";
+      // abort: report, drain this block's copies still in flight (bounded), continue to the reduction
+      s << "  if (aborted && threadIdx.x == 0) {\n    atomicOr(status, 1u);\n"
+        << "    for (unsigned k = it; k < issued; k++) mf_mbar_wait_bounded(&mf_bar[k % MF_STAGES], (k / MF_STAGES) & 1u);\n"
+        << "  }\n";
+    } else {
+      s << "  const mf_u64 step = (mf_u64)gridDim.x * MF_BLOCK * " << V << ";\n";
+      s << "  for (mf_u64 base = ((mf_u64)blockIdx.x * MF_BLOCK + threadIdx.x) * " << V
+        << "; base < n; base += step) {\n";
+      emit_events("    ", "base", "base", [&](int k) {
+        return "__ldg(reinterpret_cast<const " + VT + "*>(data + (mf_u64)" + std::to_string(k) + " * stride + base))";
+      });
+      s << "  }\n";
     }
-    s << "  }\n";
-    // warp -> block -> grid, last block combines in fixed order
-    s << R"CUDA(  __shared__ double red[MF_NOUT][MF_BLOCK / 32];
-  __shared__ bool am_last;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-  for (int j = 0; j < MF_NOUT; j++) {
-)CUDA";
-    if (ar32)
-      s << "    const double w = mf_warp_sum((double)acc[j] - (double)cmp[j]);\n";
-    else
-      s << "    const double w = mf_warp_sum(acc[j]);\n";
-    s << R"CUDA(    if (lane == 0) red[j][warp] = w;
+    s << "  __shared__ float2 red[MF_NOUT][MF_BLOCK / 32];\n  __shared__ bool am_last;\n"
+      << "  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;\n#pragma unroll\n"
+      << "  for (int j = 0; j < MF_NOUT; j++) {\n";
+    warp_sum(s);
+    s << R"CUDA(    if (lane == 0) red[j][warp] = make_float2(a.h, a.l);
   }
   __syncthreads();
   for (int j = threadIdx.x; j < MF_NOUT; j += MF_BLOCK) {
-    double b = 0.0;
-#pragma unroll
-    for (int w = 0; w < MF_BLOCK / 32; w++) b += red[j][w];
-    partials[(mf_u64)blockIdx.x * MF_NOUT + j] = b;
+    mf_dw b = mf_dw_make(red[j][0].x, red[j][0].y);
+    for (int w = 1; w < MF_BLOCK / 32; w++) b = mf_dw_add(b, mf_dw_make(red[j][w].x, red[j][w].y));
+    partials[(mf_u64)blockIdx.x * MF_NOUT + j] = make_float2(b.h, b.l);
   }
   __threadfence();
   __syncthreads();
@@ -631,12 +1074,41 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
   __syncthreads();
   if (!am_last) return;
   __threadfence();
-  for (int j = warp; j < MF_NOUT; j += MF_BLOCK / 32) {
-    double s = 0.0, c = 0.0;
-    for (unsigned b = lane; b < gridDim.x; b += 32) mf_neumaier(s, c, __ldcg(partials + (mf_u64)b * MF_NOUT + j));
-    double t = mf_warp_sum(s);
-    double tc = mf_warp_sum(c);
-    if (lane == 0) out[j] = t + tc;
+  // Fixed-order double-float combine of the block partials by the whole last
+  // block: thread t takes blocks t, t + MF_BLOCK, ... for every output (all
+  // loads of a round issued before the adds), then a warp tree and a pass
+  // over the warps in order. The order depends only on the grid size.
+  {
+    mf_dw s[MF_NOUT];
+#pragma unroll
+    for (int j = 0; j < MF_NOUT; j++) s[j] = mf_dw_make(0.0f, 0.0f);
+    for (unsigned b0 = 0; b0 < gridDim.x; b0 += MF_Q * MF_BLOCK) {
+      float2 v[MF_Q][MF_NOUT];
+#pragma unroll
+      for (int q = 0; q < MF_Q; q++) {
+        const unsigned b = b0 + q * MF_BLOCK + threadIdx.x;
+#pragma unroll
+        for (int j = 0; j < MF_NOUT; j++)
+          v[q][j] = b < gridDim.x ? __ldcg(partials + (mf_u64)b * MF_NOUT + j) : make_float2(0.0f, 0.0f);
+      }
+#pragma unroll
+      for (int q = 0; q < MF_Q; q++)
+#pragma unroll
+        for (int j = 0; j < MF_NOUT; j++) s[j] = mf_dw_add(s[j], mf_dw_make(v[q][j].x, v[q][j].y));
+    }
+#pragma unroll
+    for (int j = 0; j < MF_NOUT; j++) {
+      mf_dw a = s[j];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) a = mf_dw_add(a, mf_dw_shfl_xor(a, o));
+      if (lane == 0) red[j][warp] = make_float2(a.h, a.l);
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < MF_NOUT; j += MF_BLOCK) {
+      mf_dw b = mf_dw_make(red[j][0].x, red[j][0].y);
+      for (int w = 1; w < MF_BLOCK / 32; w++) b = mf_dw_add(b, mf_dw_make(red[j][w].x, red[j][w].y));
+      out[j] = mf_dw_to_double(b);
+    }
   }
   if (threadIdx.x == 0) *counter = 0u;
 }
@@ -645,42 +1117,32 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
     // ---- ragged segments: one block per segment ----
     s << "extern \"C\" __global__ void __launch_bounds__(MF_BLOCK) " << out.entry << "_segments(const " << ST
       << "* __restrict__ data, mf_u64 stride, const mf_u64* __restrict__ seg_begin,"
-      << " const unsigned* __restrict__ seg_count, const double* __restrict__ params, unsigned nparams,"
+      << " const unsigned* __restrict__ seg_count, const mf_args* __restrict__ args,"
       << " double* __restrict__ out) {\n";
+    load_table(s);
     s << "  const unsigned seg = blockIdx.x;\n  const mf_u64 first = seg_begin[seg];\n"
-      << "  const mf_u64 cnt = seg_count[seg];\n  const double* __restrict__ Pv = params + (mf_u64)seg * nparams;\n";
-    emit_params_and_uniform(s, "Pv");
-    s << "  " << ACC << " acc[MF_NOUT];\n";
-    if (ar32) s << "  float cmp[MF_NOUT];\n";
-    s << "#pragma unroll\n  for (int j = 0; j < MF_NOUT; j++) { acc[j] = 0; " << (ar32 ? "cmp[j] = 0; " : "") << "}\n";
+      << "  const mf_u64 cnt = seg_count[seg];\n  const mf_args& P = args[seg];\n";
+    prologue(s, "P.");
+    acc_decl(s);
     s << "  for (mf_u64 i = threadIdx.x; i < cnt; i += MF_BLOCK) {\n";
     for (int k : out.used_inputs)
-      s << "    const " << AT << " x" << k << " = (" << AT << ")__ldg(data + (mf_u64)" << k
-        << " * stride + first + i);\n";
-    emit_body(s, "    ");
-    for (int j = 0; j < M; j++) {
-      if (ar32)
-        s << "    mf_kahan_f32(acc[" << j << "], cmp[" << j << "], r" << j << ");\n";
-      else
-        s << "    acc[" << j << "] += r" << j << ";\n";
-    }
+      s << "    const " << XT << " x" << k << " = " << input_value("__ldg(data + (mf_u64)" + std::to_string(k) +
+                                                                   " * stride + first + i)")
+        << ";\n";
+    body(s, "    ");
+    acc_add(s, "    ");
     s << "  }\n";
-    s << R"CUDA(  __shared__ double red[MF_NOUT][MF_BLOCK / 32];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-  for (int j = 0; j < MF_NOUT; j++) {
-)CUDA";
-    if (ar32)
-      s << "    const double w = mf_warp_sum((double)acc[j] - (double)cmp[j]);\n";
-    else
-      s << "    const double w = mf_warp_sum(acc[j]);\n";
-    s << R"CUDA(    if (lane == 0) red[j][warp] = w;
+    s << "  __shared__ float2 red[MF_NOUT][MF_BLOCK / 32];\n"
+      << "  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;\n#pragma unroll\n"
+      << "  for (int j = 0; j < MF_NOUT; j++) {\n";
+    warp_sum(s);
+    s << R"CUDA(    if (lane == 0) red[j][warp] = make_float2(a.h, a.l);
   }
   __syncthreads();
   for (int j = threadIdx.x; j < MF_NOUT; j += MF_BLOCK) {
-    double b = 0.0, c = 0.0;
-    for (int w = 0; w < MF_BLOCK / 32; w++) mf_neumaier(b, c, red[j][w]);
-    out[(mf_u64)seg * MF_NOUT + j] = b + c;
+    mf_dw b = mf_dw_make(red[j][0].x, red[j][0].y);
+    for (int w = 1; w < MF_BLOCK / 32; w++) b = mf_dw_add(b, mf_dw_make(red[j][w].x, red[j][w].y));
+    out[(mf_u64)seg * MF_NOUT + j] = mf_dw_to_double(b);
   }
 }
 )CUDA";
@@ -743,6 +1205,57 @@ __device__ __forceinline__ unsigned mf_xoshiro(unsigned* s) {
   }
   out.source = s.str();
   return out;
+}
+
+namespace {
+double eval_memo(const std::vector<Node>& ns, int id, const double* params, size_t np, std::vector<double>& memo,
+                 std::vector<char>& done) {
+  if (done[id]) return memo[id];
+  const Node& n = ns[id];
+  double v = 0.0;
+  switch (n.op) {
+    case Op::Const: v = n.value; break;
+    case Op::Param: v = size_t(n.index) < np ? params[n.index] : 0.0; break;
+    case Op::Input: throw std::runtime_error("input column in a parameter-only value");
+    case Op::Add: case Op::Sub: case Op::Mul: case Op::Div: case Op::Pow:
+      v = apply_binary(n.op, eval_memo(ns, n.a, params, np, memo, done), eval_memo(ns, n.b, params, np, memo, done));
+      break;
+    case Op::Cmp:
+      v = apply_cmp(n.cmp, eval_memo(ns, n.a, params, np, memo, done), eval_memo(ns, n.b, params, np, memo, done)) ? 1.0
+                                                                                                                 : 0.0;
+      break;
+    case Op::Select:
+      v = eval_memo(ns, n.a, params, np, memo, done) != 0.0 ? eval_memo(ns, n.b, params, np, memo, done)
+                                                            : eval_memo(ns, n.c, params, np, memo, done);
+      break;
+    default: v = apply_unary(n.op, eval_memo(ns, n.a, params, np, memo, done)); break;
+  }
+  memo[id] = v;
+  done[id] = 1;
+  return v;
+}
+}  // namespace
+
+void LoweredKernel::fill_args(const double* params, size_t np, unsigned char* out) const {
+  std::memset(out, 0, args_bytes());
+  double* d = reinterpret_cast<double*>(out);
+  float* f = reinterpret_cast<float*>(out + size_t(nd) * 8);
+  std::vector<double> memo(nodes.size(), 0.0);
+  std::vector<char> done(nodes.size(), 0);
+  for (const auto& sl : slots) {
+    const double v = eval_memo(nodes, sl.node, params, np, memo, done);
+    switch (sl.kind) {
+      case UniformSlot::Double: d[sl.offset] = v; break;
+      case UniformSlot::Float: f[sl.offset] = float(v); break;
+      case UniformSlot::Bool: f[sl.offset] = v != 0.0 ? 1.0f : 0.0f; break;
+      case UniformSlot::DwPair: {
+        const float h = float(v);
+        f[sl.offset] = h;
+        f[sl.offset + 1] = float(v - double(h));
+        break;
+      }
+    }
+  }
 }
 
 }  // namespace mf

@@ -63,12 +63,36 @@ class Dag {
   std::map<std::string, int> input_idx_, param_idx_;
 };
 
+// A parameter-only value the REDUCE body needs, evaluated on the host at
+// launch and passed in the kernel's argument struct
+// { double d[nd]; float f[nf]; }.
+struct UniformSlot {
+  enum Kind { Double = 0, Float = 1, DwPair = 2, Bool = 3 };
+  int node;    // DAG node (a Param or a uniform node)
+  int kind;
+  int offset;  // index into d[] (Double) or f[] (others)
+};
+
 struct LoweredKernel {
   std::string source;            // complete CUDA C translation unit
   std::string entry;             // __global__ function name
   std::vector<int> used_inputs;  // input columns read by the kernel
   int vec = 1;                   // events per thread per iteration
   int block = 256;
+  // REDUCE kernels stream tiles of `tile` events through `stages` shared-memory
+  // buffers with bulk asynchronous copies (pipelined = true) or read global
+  // memory directly (pipelined = false).
+  bool pipelined = false;
+  int tile = 0, stages = 0;
+  size_t smem_bytes = 0;  // dynamic shared memory of the main entry
+  // REDUCE kernels: host-evaluated argument struct
+  bool host_args = false;
+  std::vector<Node> nodes;         // the DAG, for host evaluation of the slots
+  std::vector<UniformSlot> slots;
+  int nd = 1, nf = 1;              // array lengths in the struct (>= 1)
+  size_t args_bytes() const { return (size_t(nd) * 8 + size_t(nf) * 4 + 7) / 8 * 8; }
+  // Fills the argument struct for one parameter vector (params: n_params doubles).
+  void fill_args(const double* params, size_t n_params, unsigned char* out) const;
 };
 
 enum class Elem { F64, F32 };
@@ -83,7 +107,8 @@ struct GenerateSpec {
 // Builds the kernel source for the given outputs.
 LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::vector<std::string>& inputs,
                     const std::vector<std::string>& params, const std::vector<std::string>& exprs,
-                    const GenerateSpec* gen = nullptr);
+                    const GenerateSpec* gen = nullptr, bool native_f64 = false, int vec = 0, int block = 0,
+                    bool f32_arith = false, bool direct_loads = false, int stages = 0);
 
 // Counts per-event operations of a lowered expression set (diagnostics).
 struct OpCount {

@@ -27,6 +27,7 @@
 #include <vector>
 
 #include "../../include/morefit_cuda.h"
+#include "mf_internal.h"
 #include "mf_lower.h"
 
 namespace {
@@ -37,6 +38,12 @@ int fail(int code, const std::string& msg) {
   g_last_error = msg;
   return code;
 }
+
+}  // namespace
+
+int set_error(int code, const std::string& msg) { return fail(code, msg); }
+
+namespace {
 
 #define MF_CUDA_TRY(call)                                                                                  \
   do {                                                                                                     \
@@ -72,11 +79,16 @@ std::string cache_dir() {
   return std::string(h ? h : "/tmp") + "/.cache/morefit_gb300";
 }
 
-void parse_ptxas_log(const std::string& log, int& regs, int& spill) {
-  // "ptxas info    : Used 40 registers, ..." and "... bytes spill stores"
-  size_t p = log.find("Used ");
+void parse_ptxas_log(const std::string& log, int& regs, int& spill, const std::string& entry = "") {
+  // "Compiling entry function 'NAME'" ... "Used 40 registers" ... "N bytes spill stores"
+  size_t start = 0;
+  if (!entry.empty()) {
+    size_t e = log.find("entry function '" + entry + "'");
+    if (e != std::string::npos) start = e;
+  }
+  size_t p = log.find("Used ", start);
   if (p != std::string::npos) regs = std::atoi(log.c_str() + p + 5);
-  size_t q = log.find(" bytes spill stores");
+  size_t q = log.find(" bytes spill stores", start);
   if (q != std::string::npos) {
     size_t b = q;
     while (b > 0 && (std::isdigit((unsigned char)log[b - 1]))) b--;
@@ -84,7 +96,8 @@ void parse_ptxas_log(const std::string& log, int& regs, int& spill) {
   }
 }
 
-int compile_source(const std::string& src, const std::string& name, std::shared_ptr<CompiledImage>& out) {
+int compile_source(const std::string& src, const std::string& name, std::shared_ptr<CompiledImage>& out,
+                   const std::string& entry) {
   {
     std::lock_guard<std::mutex> lk(g_cache_mu);
     auto it = g_cache.find(src);
@@ -108,7 +121,7 @@ int compile_source(const std::string& src, const std::string& name, std::shared_
         img->cubin.assign((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
         std::ifstream l(base + ".log");
         if (l) img->log.assign((std::istreambuf_iterator<char>(l)), std::istreambuf_iterator<char>());
-        parse_ptxas_log(img->log, img->regs, img->spill);
+        parse_ptxas_log(img->log, img->regs, img->spill, entry);
         from_disk = !img->cubin.empty();
       }
     }
@@ -134,7 +147,7 @@ int compile_source(const std::string& src, const std::string& name, std::shared_
     img->cubin.resize(cubsz);
     nvrtcGetCUBIN(prog, img->cubin.data());
     nvrtcDestroyProgram(&prog);
-    parse_ptxas_log(log, img->regs, img->spill);
+    parse_ptxas_log(log, img->regs, img->spill, entry);
     if (!std::getenv("MOREFIT_CUDA_NOCACHE")) {
       std::string cmd_dir = dir;
       // best effort: create the cache directory chain
@@ -176,7 +189,8 @@ struct mf_context {
   double* partials = nullptr;
   size_t partials_cap = 0;  // doubles
   unsigned* counter = nullptr;
-  unsigned* status = nullptr;
+  unsigned* status = nullptr;       // device-visible alias of status_host
+  unsigned* status_host = nullptr;  // mapped pinned host word: kernel error flags
   // mapped pinned host memory the kernels write results into
   double* out_host = nullptr;
   double* out_dev = nullptr;
@@ -224,12 +238,24 @@ void release_context(mf_context* c) {
   if (c->partials) cudaFree(c->partials);
   if (c->counter) cudaFree(c->counter);
   if (c->out_host) cudaFreeHost(c->out_host);
+  if (c->status_host) cudaFreeHost(c->status_host);
   if (c->stage_dev) cudaFree(c->stage_dev);
   cudaStreamDestroy(c->stream);
   delete c;
 }
 
+
 size_t elem_size(int e) { return e == MF_F32 ? 4 : 8; }
+
+// Reads (and clears) the kernels' error word after the stream has drained.
+int check_status(mf_context* c) {
+  const unsigned st = *c->status_host;
+  if (!st) return MF_OK;
+  *c->status_host = 0u;
+  cudaMemsetAsync(c->counter, 0, sizeof(unsigned), c->stream);  // a block that gave up may have left it set
+  cudaStreamSynchronize(c->stream);
+  return fail(MF_ERR_TIMEOUT, "a kernel gave up waiting for its input tiles (status " + std::to_string(st) + ")");
+}
 
 int ensure_scratch(mf_context* c, size_t partial_doubles, size_t out_doubles) {
   if (partial_doubles > c->partials_cap) {
@@ -314,9 +340,11 @@ int mf_context_create(int device, uint64_t hbm_budget_bytes, mf_context** out) {
   c->num_sms = prop.multiProcessorCount;
   c->budget = hbm_budget_bytes;
   MF_CUDA_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
-  MF_CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&c->counter), 2 * sizeof(unsigned)));
-  MF_CUDA_TRY(cudaMemset(c->counter, 0, 2 * sizeof(unsigned)));
-  c->status = c->counter + 1;
+  MF_CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&c->counter), sizeof(unsigned)));
+  MF_CUDA_TRY(cudaMemset(c->counter, 0, sizeof(unsigned)));
+  MF_CUDA_TRY(cudaHostAlloc(reinterpret_cast<void**>(&c->status_host), 64, cudaHostAllocMapped));
+  MF_CUDA_TRY(cudaHostGetDevicePointer(reinterpret_cast<void**>(&c->status), c->status_host, 0));
+  *c->status_host = 0u;
   int rc = ensure_scratch(c.get(), size_t(c->num_sms) * 8 * 64, 4096);
   if (rc) return rc;
   *out = c.release();
@@ -340,7 +368,7 @@ int mf_context_allocated(const mf_context* c, uint64_t* bytes) {
 int mf_context_synchronize(mf_context* c) {
   if (!c) return fail(MF_ERR_INVALID, "context is null");
   MF_CUDA_TRY(cudaStreamSynchronize(c->stream));
-  return MF_OK;
+  return check_status(c);
 }
 
 int mf_buffer_alloc(mf_context* c, uint64_t nbytes, mf_buffer** out) {
@@ -458,11 +486,6 @@ static int lower_desc(const mf_kernel_desc* d, mf::LoweredKernel& lk);
 int mf_kernel_build(mf_context* c, const mf_kernel_desc* d, mf_kernel** out) {
   if (!c || !d || !out) return fail(MF_ERR_INVALID, "null argument");
   *out = nullptr;
-  if (d->elem_type != MF_F64 && d->elem_type != MF_F32) return fail(MF_ERR_INVALID, "bad element type");
-  if (d->kind != MF_KERNEL_REDUCE && d->kind != MF_KERNEL_STORE && d->kind != MF_KERNEL_GENERATE)
-    return fail(MF_ERR_INVALID, "bad kernel kind");
-  if (d->n_outputs == 0 || d->n_outputs > MF_MAX_OUTPUTS) return fail(MF_ERR_INVALID, "bad number of outputs");
-  if (d->n_params > MF_MAX_PARAMS) return fail(MF_ERR_INVALID, "too many parameters");
   auto k = std::make_unique<mf_kernel>();
   k->ctx = c;
   k->name = d->name ? d->name : "kernel";
@@ -475,16 +498,22 @@ int mf_kernel_build(mf_context* c, const mf_kernel_desc* d, mf_kernel** out) {
   int lrc = lower_desc(d, k->lowered);
   if (lrc) return lrc;
   for (int i : k->lowered.used_inputs) k->max_input = std::max(k->max_input, i);
-  int rc = compile_source(k->lowered.source, k->name, k->image);
+  int rc = compile_source(k->lowered.source, k->name, k->image, k->lowered.entry);
   if (rc) return rc;
   MF_CUDA_TRY(cudaSetDevice(c->device));
   MF_CUDA_TRY(cudaLibraryLoadData(&k->lib, k->image->cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0));
   MF_CUDA_TRY(cudaLibraryGetKernel(&k->fn, k->lib, k->lowered.entry.c_str()));
   if (d->kind == MF_KERNEL_REDUCE)
     MF_CUDA_TRY(cudaLibraryGetKernel(&k->fn_seg, k->lib, (k->lowered.entry + "_segments").c_str()));
+  if (k->lowered.smem_bytes > 48 * 1024)
+    MF_CUDA_TRY(cudaFuncSetAttribute(reinterpret_cast<const void*>(k->fn), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     int(k->lowered.smem_bytes)));
   int nb = 0;
   MF_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, reinterpret_cast<const void*>(k->fn),
-                                                            k->lowered.block, 0));
+                                                            k->lowered.block, k->lowered.smem_bytes));
+  if (nb == 0)
+    return fail(MF_ERR_UNSUPPORTED, "kernel '" + k->name + "' does not fit on an SM (" +
+                                        std::to_string(k->lowered.smem_bytes) + " B shared memory)");
   k->blocks_per_sm = std::max(1, nb);
   c->refs++;
   k->holds_ref = true;
@@ -521,7 +550,9 @@ static int lower_desc(const mf_kernel_desc* d, mf::LoweredKernel& lk) {
                                                 : mf::Kind::Generate,
                    d->elem_type == MF_F32 ? mf::Elem::F32 : mf::Elem::F64, names(d->n_inputs, d->input_names),
                    names(d->n_params, d->param_names), names(d->n_outputs, d->exprs),
-                   d->kind == MF_KERNEL_GENERATE ? &gs : nullptr);
+                   d->kind == MF_KERNEL_GENERATE ? &gs : nullptr, (d->flags & MF_FLAG_NATIVE_F64) != 0, int(d->vec),
+                   int(d->block), d->elem_type == MF_F64 && (d->flags & MF_FLAG_F32_ARITH) != 0,
+                   (d->flags & MF_FLAG_BULK_PIPELINE) == 0, int(d->stages));
   } catch (const std::exception& e) {
     return fail(MF_ERR_PARSE, e.what());
   }
@@ -611,7 +642,7 @@ int mf_compile_check(const mf_kernel_desc* d, int* regs, int* spill) {
   int rc = lower_desc(d, lk);
   if (rc) return rc;
   std::shared_ptr<CompiledImage> img;
-  rc = compile_source(lk.source, d->name ? d->name : "kernel", img);
+  rc = compile_source(lk.source, d->name ? d->name : "kernel", img, lk.entry);
   if (rc) return rc;
   if (regs) *regs = img->regs;
   if (spill) *spill = img->spill;
@@ -658,7 +689,8 @@ int mf_kernel_info(const mf_kernel* k, int* regs, int* spill, int* block, int* v
 namespace mfi {
 
 int grid_for(const mf_kernel* k, uint64_t n) {
-  const uint64_t per_block = uint64_t(k->lowered.block) * uint64_t(k->lowered.vec);
+  const uint64_t per_block =
+      k->lowered.pipelined ? uint64_t(k->lowered.tile) : uint64_t(k->lowered.block) * uint64_t(k->lowered.vec);
   const uint64_t need = std::max<uint64_t>(1, (n + per_block - 1) / per_block);
   const uint64_t cap = uint64_t(k->ctx->num_sms) * uint64_t(k->blocks_per_sm);
   return int(std::min(need, cap));
@@ -669,11 +701,17 @@ int launch_reduce(mf_kernel* k, const void* data, uint64_t stride, uint64_t n, c
                   double* partials, unsigned* counter, double* out, cudaStream_t stream, int grid_cap) {
   int grid = grid_for(k, n);
   if (grid_cap > 0) grid = std::min(grid, grid_cap);
-  std::vector<double> pv(std::max<uint32_t>(1, k->n_params), 0.0);
-  if (k->n_params) std::memcpy(pv.data(), params, k->n_params * sizeof(double));
-  void* args[] = {const_cast<void**>(&data), &stride, &n, pv.data(), &partials, &counter, &out};
-  MF_CUDA_TRY(cudaLaunchKernel(reinterpret_cast<const void*>(k->fn), dim3(grid), dim3(k->lowered.block), args, 0,
-                               stream));
+  // argument struct: parameter-only values evaluated here, pre-rounded for the kernel's arithmetic
+  std::vector<unsigned char> pv(k->lowered.args_bytes(), 0);
+  try {
+    k->lowered.fill_args(params, k->n_params, pv.data());
+  } catch (const std::exception& e) {
+    return fail(MF_ERR_INVALID, std::string("parameter evaluation: ") + e.what());
+  }
+  unsigned* status = k->ctx->status;
+  void* args[] = {const_cast<void**>(&data), &stride, &n, pv.data(), &partials, &counter, &out, &status};
+  MF_CUDA_TRY(cudaLaunchKernel(reinterpret_cast<const void*>(k->fn), dim3(grid), dim3(k->lowered.block), args,
+                               k->lowered.smem_bytes, stream));
   return MF_OK;
 }
 
@@ -699,11 +737,12 @@ int mf_kernel_reduce(mf_kernel* k, const mf_buffer* in, uint64_t stride, uint64_
   const int grid = mfi::grid_for(k, n);
   rc = ensure_scratch(c, size_t(grid) * k->n_outputs, k->n_outputs);
   if (rc) return rc;
+  *c->status_host = 0u;
   rc = mfi::launch_reduce(k, in->ptr, stride, n, params, c->partials, c->counter, c->out_dev, c->stream, 0);
   if (rc) return rc;
   MF_CUDA_TRY(cudaStreamSynchronize(c->stream));
   std::memcpy(sums, c->out_host, k->n_outputs * sizeof(double));
-  return MF_OK;
+  return check_status(c);
 }
 
 int mf_kernel_reduce_async(mf_kernel* k, const mf_buffer* in, uint64_t stride, uint64_t n, const double* params,
@@ -752,6 +791,30 @@ int mf_kernel_reduce_many(mf_kernel* k, uint32_t count, const mf_buffer* const* 
   return MF_OK;
 }
 
+int mf_columns_sum(const mf_buffer* buf, int elem, uint32_t ncols, uint64_t n, uint64_t stride, double* sums) {
+  if (!buf || !buf->ptr || (!sums && ncols)) return fail(MF_ERR_INVALID, "null argument");
+  if (elem != MF_F64 && elem != MF_F32) return fail(MF_ERR_INVALID, "element type must be MF_F64 or MF_F32");
+  if (ncols == 0) return MF_OK;
+  if (stride < n) return fail(MF_ERR_INVALID, "column stride smaller than the number of events");
+  if (uint64_t(ncols) * stride * elem_size(elem) > buf->size)
+    return fail(MF_ERR_INVALID, "buffer smaller than ncols x stride");
+  if (n == 0) {
+    std::fill(sums, sums + ncols, 0.0);
+    return MF_OK;
+  }
+  mf_context* c = buf->ctx;
+  MF_CUDA_TRY(cudaSetDevice(c->device));
+  const int rows = mfi::columns_sum_partials(n, c->num_sms);
+  int rc = ensure_scratch(c, size_t(rows) * ncols, ncols);
+  if (rc) return rc;
+  rc = mfi::columns_sum_launch(buf->ptr, elem, stride, n, ncols, c->partials, c->counter, c->out_dev, c->stream,
+                               c->num_sms);
+  if (rc) return rc;
+  MF_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  std::memcpy(sums, c->out_host, ncols * sizeof(double));
+  return MF_OK;
+}
+
 int mf_context_stream(mf_context* c, void** stream) {
   if (!c || !stream) return fail(MF_ERR_INVALID, "null argument");
   *stream = c->stream;
@@ -772,28 +835,30 @@ int mf_kernel_reduce_segments(mf_kernel* k, const mf_buffer* in, uint64_t stride
   if (rc) return rc;
   mf_context* c = k->ctx;
   MF_CUDA_TRY(cudaSetDevice(c->device));
-  const uint32_t np = std::max<uint32_t>(1, n_params);
-  const size_t bytes_begin = size_t(nseg) * 8, bytes_count = (size_t(nseg) * 4 + 7) / 8 * 8,
-               bytes_par = size_t(nseg) * np * 8;
+  const size_t ab = k->lowered.args_bytes();
+  const size_t bytes_begin = size_t(nseg) * 8, bytes_count = (size_t(nseg) * 4 + 15) / 16 * 16,
+               bytes_par = size_t(nseg) * ab;
   rc = ensure_stage(c, bytes_begin + bytes_count + bytes_par);
   if (rc) return rc;
   rc = ensure_scratch(c, 0, size_t(nseg) * k->n_outputs);
   if (rc) return rc;
-  std::vector<char> host(bytes_begin + bytes_count + bytes_par, 0);
+  std::vector<unsigned char> host(bytes_begin + bytes_count + bytes_par, 0);
   std::memcpy(host.data(), seg_begin, bytes_begin);
   std::memcpy(host.data() + bytes_begin, seg_count, size_t(nseg) * 4);
-  double* hp = reinterpret_cast<double*>(host.data() + bytes_begin + bytes_count);
-  for (uint32_t s = 0; s < nseg; s++)
-    for (uint32_t j = 0; j < n_params; j++) hp[size_t(s) * np + j] = params[size_t(s) * n_params + j];
+  try {
+    for (uint32_t s = 0; s < nseg; s++)
+      k->lowered.fill_args(params + size_t(s) * n_params, n_params, host.data() + bytes_begin + bytes_count + s * ab);
+  } catch (const std::exception& e) {
+    return fail(MF_ERR_INVALID, std::string("parameter evaluation: ") + e.what());
+  }
   MF_CUDA_TRY(cudaMemcpyAsync(c->stage_dev, host.data(), host.size(), cudaMemcpyHostToDevice, c->stream));
   char* base = static_cast<char*>(c->stage_dev);
   const uint64_t* d_begin = reinterpret_cast<const uint64_t*>(base);
   const unsigned* d_count = reinterpret_cast<const unsigned*>(base + bytes_begin);
-  const double* d_par = reinterpret_cast<const double*>(base + bytes_begin + bytes_count);
-  unsigned npu = np;
+  const void* d_par = base + bytes_begin + bytes_count;
   double* outp = c->out_dev;
   const void* data = in->ptr;
-  void* args[] = {const_cast<void**>(&data), &stride, &d_begin, &d_count, &d_par, &npu, &outp};
+  void* args[] = {const_cast<void**>(&data), &stride, &d_begin, &d_count, const_cast<void**>(&d_par), &outp};
   MF_CUDA_TRY(cudaLaunchKernel(reinterpret_cast<const void*>(k->fn_seg), dim3(nseg), dim3(k->lowered.block), args, 0,
                                c->stream));
   MF_CUDA_TRY(cudaStreamSynchronize(c->stream));
@@ -844,7 +909,7 @@ int mf_kernel_generate(mf_kernel* k, const uint32_t* seeds, uint32_t nseeds, uin
   if (rc) return rc;
   MF_CUDA_TRY(cudaMemcpyAsync(c->stage_dev, seeds, size_t(nseeds) * 4 * sizeof(uint32_t), cudaMemcpyHostToDevice,
                               c->stream));
-  MF_CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(unsigned), c->stream));
+  *c->status_host = 0u;
   std::vector<double> pv(std::max<uint32_t>(1, k->n_params), 0.0);
   if (k->n_params) std::memcpy(pv.data(), params, k->n_params * sizeof(double));
   const unsigned* sd = static_cast<const unsigned*>(c->stage_dev);
@@ -855,9 +920,9 @@ int mf_kernel_generate(mf_kernel* k, const uint32_t* seeds, uint32_t nseeds, uin
   const unsigned grid = (nseeds + k->lowered.block - 1) / k->lowered.block;
   MF_CUDA_TRY(cudaLaunchKernel(reinterpret_cast<const void*>(k->fn), dim3(grid), dim3(k->lowered.block), args, 0,
                                c->stream));
-  unsigned st = 0;
-  MF_CUDA_TRY(cudaMemcpyAsync(&st, c->status, sizeof st, cudaMemcpyDeviceToHost, c->stream));
   MF_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  const unsigned st = *c->status_host;
+  *c->status_host = 0u;
   if (st) return fail(MF_ERR_TIMEOUT, "generation gave up after max_tries proposals in at least one thread");
   return MF_OK;
 }

@@ -40,7 +40,8 @@ def load_spec(name: str) -> dict:
 class Likelihood:
     """NLL, gradient and Hessian of one dataset, device resident."""
 
-    def __init__(self, backend: CUDABackend, spec: dict, kernelT=np.float64):
+    def __init__(self, backend: CUDABackend, spec: dict, kernelT=np.float64, native_f64: bool = False, vec: int = 0,
+                 block: int = 0, pipeline: bool = False, stages: int = 0):
         self.backend = backend
         self.spec = spec
         self.kernelT = np.dtype(kernelT)
@@ -50,13 +51,18 @@ class Likelihood:
         self.has_precompute = "precompute_kernel" in ks
         self.buffers = {"lh_kernel": spec["lh_buffers"], "lh_grad_kernel": spec["grad_buffers"],
                         "lh_hessian_kernel": spec["hessian_buffers"]}
-        # Blocks as the fitter wires them (fitter.hh:525-657, 704-757).
-        self.pre = CUDABlock(backend, kernelT)
+        # Blocks as the fitter wires them (fitter.hh:525-657, 704-757). In
+        # mixed precision the hoisted basis columns are stored in FP32; a model
+        # without them reads its raw observables, which keep FP64 storage with
+        # FP32 arithmetic (MF_FLAG_F32_ARITH).
+        mixed_raw = self.kernelT == np.float32 and not self.has_precompute
+        self.pre = CUDABlock(backend, np.float64 if mixed_raw else kernelT)
         self.blocks = {}
         for name in ("lh_kernel", "lh_grad_kernel", "lh_hessian_kernel"):
             if name not in ks:
                 continue
-            b = CUDABlock(backend, kernelT)
+            b = CUDABlock(backend, kernelT, native_f64=native_f64, vec=vec, block=block, f32_arith=mixed_raw,
+                          pipeline=pipeline, stages=stages)
             if self.has_precompute:
                 b.SetupInputBuffer(self.pre, False)
             else:

@@ -201,3 +201,27 @@ def test_gpu_generator_matches_oracle(backend, oracle_lib, workload, n):
     assert same.mean() > 0.999, f"only {same.mean():.4f} of events identical"
     # any difference is a rare accept flip at the threshold; then the stream shifts within one thread only
     assert np.allclose(np.sort(got[0]), np.sort(ref[0]), atol=0.05) or same.all()
+
+
+@pytest.mark.parametrize("elem,n,ncols", [(0, 1, 1), (0, 1000, 3), (0, 1000003, 5), (1, 777777, 4)])
+def test_columns_sum(backend, elem, n, ncols):
+    """Device column sums equal exact sums (math.fsum) to double-float accuracy."""
+    import ctypes as C
+    import math
+    from morefit_gb300 import _lib as L
+    from morefit_gb300.backend import DeviceColumns
+    rng = np.random.default_rng(n + ncols)
+    host = rng.normal(0.3, 2.0, size=(ncols, n))
+    if elem == L.MF_F32:
+        host = host.astype(np.float32)
+    cols = DeviceColumns(backend, elem)
+    cols.upload(host)
+    sums = np.zeros(ncols)
+    L.check(L.lib.mf_columns_sum(cols.buf, elem, ncols, n, cols.stride, L.dptr(sums)))
+    for c in range(ncols):
+        exact = math.fsum(host[c].astype(np.float64))
+        scale = np.abs(host[c].astype(np.float64)).sum()
+        assert abs(sums[c] - exact) <= 1e-13 * scale, (c, sums[c], exact)
+    again = np.zeros(ncols)
+    L.check(L.lib.mf_columns_sum(cols.buf, elem, ncols, n, cols.stride, L.dptr(again)))
+    assert np.array_equal(sums, again)
