@@ -211,6 +211,31 @@ int mf_kernel_reduce_many(mf_kernel* k, uint32_t count, const mf_buffer* const* 
  * reduction kernels (include/compute_opencl.hh:807-991). */
 int mf_columns_sum(const mf_buffer* buf, int elem_type, uint32_t ncols, uint64_t n, uint64_t stride, double* sums);
 
+/* mf_columns_sum without any allocation. No counterpart in the reference:
+ * it is for callers that cannot allocate device memory where they need the
+ * sums -- code that hands out every device byte from its own arena or another
+ * framework's allocator, a process whose allocation budget is spent, or a
+ * latency-critical loop where cudaMalloc/cudaFree would synchronize the
+ * device. It takes no context: `data` is a device pointer to ncols columns
+ * (column stride `stride` elements, n events, element type MF_F64/MF_F32),
+ * `sums` a device pointer to ncols doubles, `stream` a cudaStream_t (NULL for
+ * the default stream). The call enqueues the work on that stream and
+ * returns; the sums are valid once the stream has reached it. Results equal
+ * mf_columns_sum's for the same data.
+ *
+ * Its scratch is a fixed 512 KiB + 256 B array in the library's device image
+ * (held by every GPU that loads the library until the process exits): at
+ * most 64 columns (MF_ERR_INVALID beyond that), any n. All calls on one GPU
+ * share it and it keeps the last call's contents, so calls whose work
+ * overlaps on the same GPU (two streams, two host threads) race and give
+ * wrong sums: serialize them. Each GPU has its own copy. The first
+ * call on a device looks up the array's device address on that device (a
+ * one-time set-up); make that first call before any stream capture. The
+ * call allocates nothing (no cudaMalloc/cudaFree, no allocating library
+ * routine); it clears its completion counter with cudaMemsetAsync. */
+int mf_columns_sum_noalloc(const void* data, int elem_type, uint32_t ncols, uint64_t n, uint64_t stride,
+                           double* sums, void* stream);
+
 /* The context's cudaStream_t, as an opaque pointer (interop: events, graphs). */
 int mf_context_stream(mf_context* ctx, void** stream);
 

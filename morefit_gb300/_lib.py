@@ -118,6 +118,8 @@ _proto("mf_kernel_reduce_async", C.c_int, c_ker, c_buf, C.c_uint64, C.c_uint64, 
 _proto("mf_kernel_reduce_many", C.c_int, c_ker, C.c_uint32, C.POINTER(c_buf), C.POINTER(C.c_uint64),
        C.POINTER(C.c_uint64), c_dbl_p, C.c_uint32, c_buf)
 _proto("mf_columns_sum", C.c_int, c_buf, C.c_int, C.c_uint32, C.c_uint64, C.c_uint64, c_dbl_p)
+_proto("mf_columns_sum_noalloc", C.c_int, C.c_void_p, C.c_int, C.c_uint32, C.c_uint64, C.c_uint64, C.c_void_p,
+       C.c_void_p)
 _proto("mf_context_stream", C.c_int, c_ctx, C.POINTER(C.c_void_p))
 _proto("mf_kernel_reduce_segments", C.c_int, c_ker, c_buf, C.c_uint64, C.c_uint32, C.POINTER(C.c_uint64),
        C.POINTER(C.c_uint32), c_dbl_p, C.c_uint32, c_dbl_p)
@@ -155,7 +157,7 @@ def exported_symbols() -> list[str]:
         "mf_buffer_device_ptr", "mf_buffer_h2d", "mf_buffer_d2h", "mf_buffer_memset", "mf_column_stride",
         "mf_events_upload", "mf_events_download", "mf_events_upload_f64_as", "mf_kernel_build", "mf_kernel_free",
         "mf_kernel_source", "mf_kernel_info", "mf_kernel_reduce", "mf_kernel_reduce_async", "mf_kernel_reduce_many",
-        "mf_columns_sum", "mf_context_stream", "mf_kernel_reduce_segments", "mf_kernel_store",
+        "mf_columns_sum", "mf_columns_sum_noalloc", "mf_context_stream", "mf_kernel_reduce_segments", "mf_kernel_store",
         "mf_kernel_generate", "mf_eval_expressions", "mf_seed_rows", "mf_generate_partition", "mf_lower_source",
         "mf_compile_check",
     ]

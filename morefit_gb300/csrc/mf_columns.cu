@@ -11,8 +11,10 @@
 // order, so the result is reproducible for a given n.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <cstring>
+#include <mutex>
 #include <string>
 
 #include "../../include/morefit_cuda.h"
@@ -127,3 +129,85 @@ int columns_sum_launch(const void* data, int elem, uint64_t stride, uint64_t n, 
 int columns_sum_partials(uint64_t n, int num_sms) { return grid_for(n, num_sms); }
 
 }  // namespace mfi
+
+// ---------------------------------------------------------------------------
+// Column sums without any allocation.
+//
+// Some callers cannot allocate device memory at the point where they need
+// these sums: code that hands every device byte out of its own arena or
+// another framework's allocator, a process that has spent its allocation
+// budget, or a latency-critical loop where cudaMalloc/cudaFree would
+// synchronize the whole device. mf_columns_sum_noalloc serves them with the
+// same kernel as mf_columns_sum, whose scratch (one partial row per block and
+// a completion counter) lives in the file-scope arrays below instead of a
+// context. Every GPU that loads this library holds these 512 KiB + 256 bytes
+// until the process exits.
+namespace {
+
+constexpr uint32_t kNoAllocMaxCols = 64;  // largest ncols the entry point accepts
+static __device__ __align__(256) float2 g_noalloc_partials[kMaxGrid * kNoAllocMaxCols];
+static __device__ __align__(256) unsigned g_noalloc_counter;
+
+constexpr int kMaxDevices = 64;
+struct NoAllocScratch {
+  bool ready = false;
+  float2* partials = nullptr;  // device address of g_noalloc_partials on that device
+  unsigned* counter = nullptr;
+  int num_sms = 0;
+};
+NoAllocScratch g_noalloc[kMaxDevices];
+std::mutex g_noalloc_mu;
+
+// Once per device, with that device current: the device addresses of the
+// scratch arrays (the names above are host-side stand-ins, not device
+// addresses) and the SM count.
+int noalloc_setup(int dev, NoAllocScratch** out) {
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  NoAllocScratch& s = g_noalloc[dev];
+  if (!s.ready) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_partials);
+    if (e != cudaSuccess) return set_error(MF_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    s.partials = static_cast<float2*>(p);
+    e = cudaGetSymbolAddress(&p, g_noalloc_counter);
+    if (e != cudaSuccess) return set_error(MF_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    s.counter = static_cast<unsigned*>(p);
+    e = cudaDeviceGetAttribute(&s.num_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return set_error(MF_ERR_CUDA, std::string("cudaDeviceGetAttribute: ") + cudaGetErrorString(e));
+    s.ready = true;
+  }
+  *out = &s;
+  return MF_OK;
+}
+
+}  // namespace
+
+extern "C" int mf_columns_sum_noalloc(const void* data, int elem_type, uint32_t ncols, uint64_t n, uint64_t stride,
+                                      double* sums, void* stream) {
+  if (!data || !sums) return set_error(MF_ERR_INVALID, "null argument");
+  if (elem_type != MF_F64 && elem_type != MF_F32)
+    return set_error(MF_ERR_INVALID, "element type must be MF_F64 or MF_F32");
+  if (ncols == 0 || ncols > kNoAllocMaxCols)
+    return set_error(MF_ERR_INVALID, "mf_columns_sum_noalloc: ncols must be 1.." + std::to_string(kNoAllocMaxCols) +
+                                         " (its static scratch holds " + std::to_string(kNoAllocMaxCols) +
+                                         " columns), got " + std::to_string(ncols));
+  if (stride < n) return set_error(MF_ERR_INVALID, "column stride smaller than the number of events");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (n == 0) {
+    const cudaError_t e = cudaMemsetAsync(sums, 0, ncols * sizeof(double), st);
+    if (e != cudaSuccess) return set_error(MF_ERR_CUDA, std::string("cudaMemsetAsync: ") + cudaGetErrorString(e));
+    return MF_OK;
+  }
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return set_error(MF_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+  if (dev < 0 || dev >= kMaxDevices) return set_error(MF_ERR_INVALID, "device index beyond the supported range");
+  NoAllocScratch* s = nullptr;
+  int rc = noalloc_setup(dev, &s);
+  if (rc) return rc;
+  // The counter must start at zero; a previous call normally leaves it at
+  // zero, clearing it on the caller's stream makes that unconditional.
+  e = cudaMemsetAsync(s->counter, 0, sizeof(unsigned), st);
+  if (e != cudaSuccess) return set_error(MF_ERR_CUDA, std::string("cudaMemsetAsync: ") + cudaGetErrorString(e));
+  return mfi::columns_sum_launch(data, elem_type, stride, n, ncols, s->partials, s->counter, sums, st, s->num_sms);
+}
