@@ -23,6 +23,7 @@ events of one dataset: the lh_grad kernel of the reference's fitter
 from __future__ import annotations
 
 import argparse
+import datetime
 import json
 import math
 import os
@@ -51,48 +52,84 @@ def _peaks():
     return 6800.0, "fallback"
 
 
-class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+# dram__bytes_read.sum + dram__bytes_write.sum of one lh_grad launch (FP64
+# storage, double-float arithmetic, 1M events) from the full ncu capture
+# summarised in profiles/mf_reduce_lh_grad_pwave_1M.md.
+NCU_TRAFFIC_F64 = 88.056832e6 + 2.425088e6
+NCU_TRAFFIC_SOURCE = "ncu --set full, one launch, profiles/mf_reduce_lh_grad_pwave_1M.md"
 
-    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled every 50 ms by one
+    background nvidia-smi process; summary() keeps the samples stamped inside
+    the timed region (mark_start/mark_end)."""
+
+    Q = ("timestamp,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
 
     def __init__(self, device: int):
         self.device = device
-        self.samples = []
-        self._stop = threading.Event()
-        self._t = None
-
-    def _run(self):
-        while not self._stop.is_set():
-            try:
-                r = subprocess.run(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
-                                    "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
-                if r.returncode == 0 and r.stdout.strip():
-                    self.samples.append([x.strip() for x in r.stdout.strip().split(",")])
-            except Exception:
-                pass
-            self._stop.wait(0.2)
+        self._proc = None
+        self._file = None
+        self.t0 = self.t1 = None
 
     def __enter__(self):
-        self._t = threading.Thread(target=self._run, daemon=True)
-        self._t.start()
+        import tempfile
+        self._file = tempfile.TemporaryFile(mode="w+")
+        try:
+            self._proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                           "--format=csv,noheader,nounits", "-lms", "50"],
+                                          stdout=self._file, stderr=subprocess.DEVNULL)
+            time.sleep(0.5)  # first sample before the timed region starts
+        except Exception:
+            self._proc = None
         return self
 
+    def mark_start(self):
+        self.t0 = datetime.datetime.now()
+
+    def mark_end(self):
+        self.t1 = datetime.datetime.now()
+
     def __exit__(self, *a):
-        self._stop.set()
-        self._t.join(timeout=10)
+        if self._proc is not None:
+            time.sleep(0.1)
+            self._proc.terminate()
+            try:
+                self._proc.wait(timeout=5)
+            except Exception:
+                self._proc.kill()
 
     def summary(self):
-        if not self.samples:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
-        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        rows = []
+        if self._file is not None:
+            self._file.seek(0)
+            for line in self._file:
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 8:
+                    continue
+                try:
+                    ts = datetime.datetime.strptime(f[0], "%Y/%m/%d %H:%M:%S.%f")
+                except ValueError:
+                    continue
+                rows.append((ts, f[1:]))
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        inside = [r for ts, r in rows if self.t0 and self.t1 and self.t0 <= ts <= self.t1]
+        window = "timed region"
+        if not inside:  # region shorter than the sampling period: nearest samples
+            inside = [r for _, r in rows]
+            window = "whole run (timed region shorter than a sample)"
+        num = lambda v: v.replace(".", "", 1).isdigit()
+        sm = [float(s[0]) for s in inside if num(s[0])]
+        mx = [float(s[1]) for s in inside if num(s[1])]
+        pw = [float(s[2]) for s in inside if num(s[2])]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i].strip() == "Active"})
+        reasons = sorted({names[i] for s in inside for i in range(4) if s[3 + i] == "Active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.samples)}
+                "power_w": statistics.median(pw) if pw else None, "reasons": reasons,
+                "samples": len(inside), "window": window}
 
 
 def dist_env():
@@ -120,21 +157,25 @@ def reference_arm(args):
     truth = np.array(spec["truth"])
     pv = np.concatenate([truth, eval_expressions(spec["parameters"], truth, [e for _, e in spec["grad_buffers"]])])
     nthreads = os.cpu_count() or 1
-    for _ in range(args.warmup):
+    for _ in range(min(args.warmup, 3)):
         grad.reduce(cols, pv, nthreads)
+    # Bounded sample: K evaluations or --cpu-seconds of them, whichever ends first.
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    done = 0
+    while done < args.steps and (done == 0 or time.perf_counter() - t0 < args.cpu_seconds):
         s = grad.reduce(cols, pv, nthreads)
+        done += 1
     dt = time.perf_counter() - t0
-    v = args.steps / dt
+    v = done / dt
     line = {"metric": METRIC, "value": v, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
+            "steps_timed": done, "warmup": args.warmup, "ms_per_step": 1e3 * dt / done, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded accept-reject)",
             "impl": "reference",
             "config": {"workload": "K*mumu P-wave angular fit, 8 parameters, 1M events, FP64",
                        "nevents": n, "inputs": "host memory"},
             "cpu_baseline": {"value": v, "unit": "evals/s", "cores": nthreads, "kind": "port",
-                             "sample": f"{args.steps} NLL+grad evaluations over all {n} events; the reference's "
+                             "sample": f"{done} NLL+grad evaluations over all {n} events (at most K or "
+                                       f"{args.cpu_seconds:.0f} s); the reference's "
                                        "lh_grad kernel text compiled by gcc -O3, Kahan-summed per thread chunk"},
             "e2e": {"value": v, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "nll_check": float(-2.0 * s[0])}
@@ -177,7 +218,7 @@ def ours(args):
     stream_ptr = C_stream(backend)
     ext = torch.cuda.ExternalStream(stream_ptr, device=torch.device("cuda", local))
 
-    def timed_device(sets, K, W):
+    def timed_device(sets, K, W, clk=None):
         """K NLL+grad launches rotating over the datasets, enqueued back to back; CUDA events on the stream."""
         import ctypes as C
         pv = sets[0].param_vector("lh_grad_kernel", truth)
@@ -202,10 +243,14 @@ def ours(args):
         torch.cuda.synchronize()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
+        if clk is not None:
+            clk.mark_start()
         e0.record(ext)
         enqueue(K)
         e1.record(ext)
         e1.synchronize()
+        if clk is not None:
+            clk.mark_end()
         backend.synchronize()
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1)
@@ -217,7 +262,7 @@ def ours(args):
     # ---------------- FP64 device throughput (value) ----------------
     sets64, bytes64, nsets64 = make_sets(np.float64)
     with ClockSampler(local) as clk:
-        ms64, res64 = timed_device(sets64, args.steps, args.warmup)
+        ms64, res64 = timed_device(sets64, args.steps, args.warmup, clk)
     if world > 1:
         t = torch.tensor([ms64], dtype=torch.float64, device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -306,7 +351,8 @@ def ours(args):
                            "l2": f"{nsets64} x {bytes64 / 1e6:.0f} MB read in rotation (> 2x L2), no flush",
                            "parallelism": "replicas" if world > 1 else "single GPU"},
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                             "frac": achieved / hbm_peak, "traffic": None,
+                             "frac": achieved / hbm_peak, "traffic": NCU_TRAFFIC_F64,
+                             "traffic_source": NCU_TRAFFIC_SOURCE,
                              "peak_source": peak_kind,
                              "algorithmic_bytes_per_launch": bytes64},
                 "e2e": {"value": world / e2e_s, "unit": "evals/s",
@@ -384,10 +430,14 @@ def variants(args):
             enqueue(W)
         backend.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        if clk is not None:
+            clk.mark_start()
         e0.record(ext)
         enqueue(K)
         e1.record(ext)
         e1.synchronize()
+        if clk is not None:
+            clk.mark_end()
         backend.synchronize()
         ms = e0.elapsed_time(e1) / K
         res = np.zeros(kern.nout)
@@ -416,7 +466,7 @@ def C_stream(backend):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3000)
+    ap.add_argument("--steps", type=int, default=25000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--nevents", type=int, default=N_EVENTS)
