@@ -86,8 +86,16 @@ int mf_context_synchronize(mf_context* ctx);
 int mf_buffer_alloc(mf_context* ctx, uint64_t nbytes, mf_buffer** out);
 int mf_buffer_free(mf_buffer* buf);
 uint64_t mf_buffer_size(const mf_buffer* buf);
-/* Raw device address (for interop); the buffer keeps ownership. */
+/* Raw device address (for interop); the buffer keeps ownership. Data written
+ * through it is invisible to the prepared copies REDUCE kernels keep (see
+ * mf_kernel_read_layout) until mf_buffer_mark_modified is called. */
 void* mf_buffer_device_ptr(const mf_buffer* buf);
+/* Declares that the buffer's contents changed outside the library (device
+ * writes through mf_buffer_device_ptr, another library's kernels). Every
+ * write made through this API (copies, memsets, uploads, STORE/GENERATE
+ * outputs) does this by itself. No counterpart in the reference, whose
+ * buffers are read as they are on every submit. */
+int mf_buffer_mark_modified(mf_buffer* buf);
 /* Plain byte copies (synchronous with respect to the host). */
 int mf_buffer_h2d(mf_buffer* buf, uint64_t offset, const void* src, uint64_t nbytes);
 int mf_buffer_d2h(const mf_buffer* buf, uint64_t offset, void* dst, uint64_t nbytes);
@@ -171,6 +179,19 @@ int mf_kernel_free(mf_kernel* k);
 int mf_kernel_source(const mf_kernel* k, char* buf, size_t len, size_t* needed);
 /* Registers / spills / static shared memory reported by the compiler. */
 int mf_kernel_info(const mf_kernel* k, int* regs, int* spill_bytes, int* block_size, int* vec_width);
+/* What a kernel reads per event. A REDUCE kernel may read prepared columns
+ * instead of its input buffer's: the lowering folds input columns that enter
+ * every output only through the same parameter-weighted combinations (the
+ * K*mumu P-wave's 11 hoisted angular columns fold to 9), and double-float
+ * kernels read FP64 values pre-split into float pairs. The prepared copy is
+ * made on the context's stream by the kernel's first launch on an input
+ * buffer, kept beside that buffer (counted in the HBM budget, shared by the
+ * kernels that prepare alike, freed with the buffer) and remade after the
+ * buffer is written. columns / bytes_per_event: what the event loop reads;
+ * source_columns: input columns the kernel uses. No counterpart in the
+ * reference (its kernels read the hoisted columns as printed). */
+int mf_kernel_read_layout(const mf_kernel* k, uint32_t* columns, uint32_t* bytes_per_event,
+                          uint32_t* source_columns);
 
 /* REDUCE: sums[j] = sum over events i in [0, n) of output j, accumulated
  * with per-thread partials, a warp/block tree and a compensated,

@@ -135,6 +135,12 @@ class Kernel:
         L.check(L.lib.mf_kernel_info(self.handle, C.byref(r), C.byref(s), C.byref(b), C.byref(v)))
         return {"registers": r.value, "spill_bytes": s.value, "block": b.value, "vec": v.value}
 
+    def read_layout(self) -> dict:
+        """Columns and bytes per event the event loop reads (prepared or source columns)."""
+        c, b, sc = C.c_uint32(), C.c_uint32(), C.c_uint32()
+        L.check(L.lib.mf_kernel_read_layout(self.handle, C.byref(c), C.byref(b), C.byref(sc)))
+        return {"columns": c.value, "bytes_per_event": b.value, "source_columns": sc.value}
+
 
 def make_desc(name: str, kind: int, elem: int, inputs: Sequence[str], params: Sequence[str],
               exprs: Sequence[str], gen=None, native_f64: bool = False, vec: int = 0, block: int = 0,

@@ -541,6 +541,7 @@ __device__ __forceinline__ mf_dw mf_dw_split(double x) {
   const float l = __fmul_rn(r23, __uint_as_float(sb));
   return mf_dw_make(__uint_as_float(hb), __uint_as_float(__float_as_uint(l) | sign));
 }
+__device__ __forceinline__ mf_dw mf_dw_pair(float2 t) { return mf_dw_make(t.x, t.y); }
 // ln of a positive double-float (see above); zero gives -inf, negative or
 // NaN gives NaN, +inf gives +inf, subnormal h is rescaled by 2^64 first.
 __device__ __forceinline__ mf_dw mf_dw_log(mf_dw a, const float4* __restrict__ tab) {
@@ -671,12 +672,35 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
     in_names = gen->dims;
   }
   Dag dag(in_names, params);
-  std::vector<int> roots;
-  for (auto& e : exprs) roots.push_back(dag.parse(e));
-  const auto& ns = dag.nodes();
+  std::vector<int> roots0;
+  for (auto& e : exprs) roots0.push_back(dag.parse(e));
+  std::vector<int> source_inputs;
+  {
+    const auto& n0 = dag.nodes();
+    const auto l0 = reachable(n0, roots0);
+    std::set<int> u;
+    for (size_t i = 0; i < n0.size(); i++)
+      if (l0[i] && n0[i].op == Op::Input) u.insert(n0[i].index);
+    source_inputs.assign(u.begin(), u.end());
+  }
+  const bool st32 = (elem == Elem::F32);
+  // REDUCE kernels read prepared columns when that pays: double-float
+  // kernels always (FP64 values stored pre-split as float pairs, so the event
+  // loop does no splitting), FP32 and native FP64 kernels when linearly
+  // dependent columns fold. FP32-over-FP64 kernels read the source columns.
+  FoldResult fold;
+  int prep = LoweredKernel::PrepNone;
+  if (kind == Kind::Reduce && !f32_arith) {
+    fold = fold_columns(dag, roots0);
+    const bool dw = !st32 && !native_f64;
+    if (fold.rewritten && (dw || fold.folded))
+      prep = dw ? LoweredKernel::PrepPair : st32 ? LoweredKernel::PrepF32 : LoweredKernel::PrepF64;
+  }
+  const Dag& G = prep ? *fold.dag : dag;
+  const std::vector<int>& roots = prep ? fold.roots : roots0;
+  const auto& ns = G.nodes();
   auto live = reachable(ns, roots);
 
-  const bool st32 = (elem == Elem::F32);
   // Arithmetic type: REDUCE kernels compute in the element type (the FP32
   // variant is the mixed-precision path); STORE kernels (event-only
   // precompute) compute in FP64 and round once on store; GENERATE kernels
@@ -696,10 +720,11 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
     // (measured fastest on GB300 for the K*mumu gradient kernel)
     const bool dw_default = !st32 && !native_f64 && !f32_arith;
     if (dw_default) {
-      out.vec = 1;
-      // 512 threads (<= 128 registers) for gradient-sized kernels; many-output
-      // kernels (Hessians) keep 256 threads so their accumulators stay in registers
-      if (!out.pipelined && exprs.size() <= 16) out.block = 512;
+      // two events per thread (one 16-byte load per prepared column) for
+      // gradient-sized kernels, measured fastest on GB300 for the K*mumu
+      // gradient; many-output kernels (Hessians) take one event per thread so
+      // their accumulators stay in registers
+      out.vec = (!out.pipelined && exprs.size() <= 16) ? 2 : 1;
     }
     if (vec_req == 1 || vec_req == 2 || (vec_req == 4 && st32)) out.vec = vec_req;
     if (block_req >= 64 && block_req <= 1024 && block_req % 32 == 0) out.block = block_req;
@@ -714,6 +739,11 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
   for (size_t i = 0; i < ns.size(); i++)
     if (live[i] && ns[i].op == Op::Input) used.insert(ns[i].index);
   out.used_inputs.assign(used.begin(), used.end());
+  out.source_inputs = source_inputs;
+  out.prep = prep;
+  if (prep) out.prep_cols = fold.cols;
+  const bool pair = prep == LoweredKernel::PrepPair;
+  if (pair && V != 1 && V != 2) throw std::runtime_error("double-float kernels take 1 or 2 events per thread");
 
   std::ostringstream s;
   s << "// MoreFit CUDA backend: generated kernel '" << name << "' (" << (kind == Kind::Reduce ? "reduce"
@@ -721,6 +751,15 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
                                                                                                 : "generate")
     << ", " << ST << " storage, "
     << (kind == Kind::Reduce && !st32 && !native_f64 ? std::string("double-float") : AT) << " arithmetic)\n";
+  if (prep) {
+    s << "// reads " << fold.cols.size() << " prepared columns (" << (pair ? "FP64 as float pairs" : st32 ? "FP32" : "FP64")
+      << ") derived from " << fold.source_columns << " source columns:\n";
+    for (size_t m = 0; m < fold.cols.size(); m++) {
+      s << "//   y" << m << " =";
+      for (auto& [col, c] : fold.cols[m]) s << " + " << c << "*" << in_names[col];
+      s << "\n";
+    }
+  }
   s << "// outputs:\n";
   for (size_t j = 0; j < exprs.size(); j++) s << "//   [" << j << "] " << exprs[j].substr(0, 160) << "\n";
   s << kPrelude;
@@ -961,29 +1000,35 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
         << "  __syncthreads();\n";
     };
     auto input_value = [&](const std::string& raw) {
-      if (ar == Ar::DW) return "mf_dw_split(" + raw + ")";
+      if (ar == Ar::DW) return (pair ? "mf_dw_pair(" : "mf_dw_split(") + raw + ")";
       return raw;
     };
+    const std::string DT = pair ? "float2" : ST;  // element type the REDUCE entries read
     const std::string XT = ar == Ar::F32 ? "float" : (ar == Ar::F64 || ar == Ar::F32S) ? "double" : "mf_dw";
 
     s << "struct mf_args { double d[" << out.nd << "]; float f[" << out.nf << "]; };\n";
     // ---- single-dataset reduce ----
-    s << "extern \"C\" __global__ void __launch_bounds__(MF_BLOCK) " << out.entry << "(const " << ST
+    s << "extern \"C\" __global__ void __launch_bounds__(MF_BLOCK) " << out.entry << "(const " << DT
       << "* __restrict__ data, mf_u64 stride, mf_u64 n, mf_args P, float2* __restrict__ partials,"
       << " unsigned* __restrict__ counter, double* __restrict__ out, unsigned* __restrict__ status) {\n";
     load_table(s);
     prologue(s, "P.");
     acc_decl(s);
-    const std::string VT = V == 1 ? ST : st32 ? (V == 4 ? "float4" : "float2") : "double2";
+    const std::string VT = V == 1 ? DT : pair ? "float4" : st32 ? (V == 4 ? "float4" : "float2") : "double2";
     const char* comp[4] = {"x", "y", "z", "w"};
+    // event v of the vector loaded into l<k>
+    auto lane_of = [&](int k, int v) -> std::string {
+      const std::string l = "l" + std::to_string(k);
+      if (pair) return V == 1 ? l : "make_float2(" + l + "." + comp[2 * v] + ", " + l + "." + comp[2 * v + 1] + ")";
+      return V == 1 ? l : l + "." + comp[v];
+    };
     auto emit_events = [&](const std::string& ind, const std::string& idx0, const std::string& valid_base,
                            const std::function<std::string(int)>& src) {
       for (int k : out.used_inputs) s << ind << "const " << VT << " l" << k << " = " << src(k) << ";\n";
       for (int v = 0; v < V; v++) {
         s << ind << "{\n";
         for (int k : out.used_inputs)
-          s << ind << "  const " << XT << " x" << k << " = "
-            << input_value("l" + std::to_string(k) + (V == 1 ? std::string("") : std::string(".") + comp[v])) << ";\n";
+          s << ind << "  const " << XT << " x" << k << " = " << input_value(lane_of(k, v)) << ";\n";
         body(s, ind + "  ");
         s << ind << "  if (" << valid_base << " + " << v << " < n) {\n";
         acc_add(s, ind + "    ");
@@ -998,11 +1043,11 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
       // MF_STAGES - 1 tiles in flight with bulk asynchronous copies into a
       // ring of shared-memory stages; all threads wait on the stage's
       // mbarrier (bounded), compute from shared memory and release the stage.
-      const size_t es = st32 ? 4 : 8;
+      const size_t es = st32 ? 4 : 8;  // float pairs are 8 bytes too
       out.smem_bytes = size_t(out.stages) * NC * out.tile * es;
       s << "#define MF_TILE " << out.tile << "\n#define MF_STAGES " << out.stages << "\n#define MF_NC " << NC << "\n";
       s << "  extern __shared__ __align__(128) unsigned char mf_dyn[];\n";
-      s << "  " << ST << "* __restrict__ stage = reinterpret_cast<" << ST << "*>(mf_dyn);\n";
+      s << "  " << DT << "* __restrict__ stage = reinterpret_cast<" << DT << "*>(mf_dyn);\n";
       s << "  __shared__ __align__(8) unsigned long long mf_bar[MF_STAGES];\n";
       s << "  const mf_u64 ntiles = (n + MF_TILE - 1) / MF_TILE;\n";
       s << "  if (threadIdx.x == 0) {\n    for (int q = 0; q < MF_STAGES; q++) mf_mbar_init(&mf_bar[q], 1u);\n"
@@ -1010,7 +1055,7 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
       // issue lambda as a macro-like block
       std::ostringstream issue;
       issue << "{ const mf_u64 t0 = (TL) * (mf_u64)MF_TILE; mf_u64 cnt = stride - t0; if (cnt > MF_TILE) cnt = MF_TILE;\n"
-            << "          const unsigned bytes = (unsigned)(cnt * sizeof(" << ST << "));\n"
+            << "          const unsigned bytes = (unsigned)(cnt * sizeof(" << DT << "));\n"
             << "          mf_mbar_expect_tx(&mf_bar[SL], bytes * MF_NC);\n";
       for (int ci = 0; ci < NC; ci++)
         issue << "          mf_bulk_g2s(stage + ((mf_u64)(SL) * MF_NC + " << ci << ") * MF_TILE, data + (mf_u64)"
@@ -1034,7 +1079,7 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
         << "        mf_fence_proxy_async();\n        " << issue_code("nt", "ns") << "\n        issued++;\n      }\n    }\n";
       s << "    const bool ok = mf_mbar_wait_bounded(&mf_bar[sl], par);\n";
       s << "    if (__syncthreads_or(!ok)) { aborted = true; break; }\n";
-      s << "    const " << ST << "* __restrict__ sb = stage + (mf_u64)sl * MF_NC * MF_TILE;\n";
+      s << "    const " << DT << "* __restrict__ sb = stage + (mf_u64)sl * MF_NC * MF_TILE;\n";
       s << "    const mf_u64 tbase = tile * (mf_u64)MF_TILE;\n";
       s << "    {\n      const int e0 = threadIdx.x * " << V << ";\n";
       std::map<int, int> colpos;
@@ -1115,7 +1160,7 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
 )CUDA";
 
     // ---- ragged segments: one block per segment ----
-    s << "extern \"C\" __global__ void __launch_bounds__(MF_BLOCK) " << out.entry << "_segments(const " << ST
+    s << "extern \"C\" __global__ void __launch_bounds__(MF_BLOCK) " << out.entry << "_segments(const " << DT
       << "* __restrict__ data, mf_u64 stride, const mf_u64* __restrict__ seg_begin,"
       << " const unsigned* __restrict__ seg_count, const mf_args* __restrict__ args,"
       << " double* __restrict__ out) {\n";
@@ -1146,6 +1191,37 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
   }
 }
 )CUDA";
+    // ---- per-dataset preparation of the columns the entries above read ----
+    if (prep) {
+      const std::string PT = pair ? "float2" : ST;
+      s << "extern \"C\" __global__ void __launch_bounds__(256) " << out.entry << "_prep(const " << ST
+        << "* __restrict__ data, mf_u64 stride, mf_u64 n, " << PT << "* __restrict__ outp) {\n"
+        << "  for (mf_u64 i = (mf_u64)blockIdx.x * 256 + threadIdx.x; i < stride; i += (mf_u64)gridDim.x * 256) {\n"
+        << "    const bool v = i < n;  // padding events are written as zeros\n";
+      auto src = [&](int col) {
+        return "(double)__ldg(data + (mf_u64)" + std::to_string(col) + " * stride + i)";
+      };
+      for (size_t m = 0; m < fold.cols.size(); m++) {
+        const auto& terms = fold.cols[m];
+        s << "    {\n      double y = 0.0;\n      if (v) {\n        y = " << src(terms[0].first) << ";\n";
+        for (size_t t = 1; t < terms.size(); t++) {
+          const double c = terms[t].second;
+          if (c == 1.0)
+            s << "        y = __dadd_rn(y, " << src(terms[t].first) << ");\n";
+          else if (c == -1.0)
+            s << "        y = __dsub_rn(y, " << src(terms[t].first) << ");\n";
+          else
+            s << "        y = __fma_rn(" << fmt_const(c, false) << ", " << src(terms[t].first) << ", y);\n";
+        }
+        s << "      }\n";
+        if (pair)
+          s << "      const mf_dw w = mf_dw_split(y);\n      outp[(mf_u64)" << m << " * stride + i] = make_float2(w.h, w.l);\n";
+        else
+          s << "      outp[(mf_u64)" << m << " * stride + i] = (" << PT << ")y;\n";
+        s << "    }\n";
+      }
+      s << "  }\n}\n";
+    }
   } else if (kind == Kind::Store) {
     s << "extern \"C\" __global__ void __launch_bounds__(MF_BLOCK) " << out.entry << "(const " << ST
       << "* __restrict__ data, mf_u64 stride, mf_u64 n, mf_par P, " << ST

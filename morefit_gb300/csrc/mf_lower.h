@@ -17,6 +17,7 @@
 
 #include <cstdint>
 #include <map>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -86,6 +87,13 @@ struct LoweredKernel {
   int tile = 0, stages = 0;
   size_t smem_bytes = 0;  // dynamic shared memory of the main entry
   // REDUCE kernels: host-evaluated argument struct
+  // Prepared input (REDUCE): the kernel reads `prep_cols.size()` columns that
+  // a per-dataset pass (entry + "_prep") derives from the source columns.
+  enum Prep { PrepNone = 0, PrepF64 = 1, PrepF32 = 2, PrepPair = 3 };
+  int prep = PrepNone;
+  std::vector<std::vector<std::pair<int, double>>> prep_cols;
+  std::vector<int> source_inputs;  // source columns the kernel (or its prep pass) reads
+  size_t prep_elem_bytes() const { return prep == PrepF32 ? 4 : 8; }
   bool host_args = false;
   std::vector<Node> nodes;         // the DAG, for host evaluation of the slots
   std::vector<UniformSlot> slots;
@@ -94,6 +102,20 @@ struct LoweredKernel {
   // Fills the argument struct for one parameter vector (params: n_params doubles).
   void fill_args(const double* params, size_t n_params, unsigned char* out) const;
 };
+
+// Rewrite of a REDUCE kernel over prepared columns (mf_fold.cpp). When
+// `rewritten`, prepared column m is the sum over cols[m] of coefficient x
+// source column, and `dag`/`roots` compute the same outputs from the prepared
+// columns; `folded` when linearly dependent source columns were merged
+// (rank < source_columns).
+struct FoldResult {
+  bool rewritten = false, folded = false;
+  std::vector<std::vector<std::pair<int, double>>> cols;
+  std::unique_ptr<Dag> dag;
+  std::vector<int> roots;
+  int rank = 0, source_columns = 0;
+};
+FoldResult fold_columns(const Dag& dag, const std::vector<int>& roots);
 
 enum class Elem { F64, F32 };
 enum class Kind { Reduce, Store, Generate };

@@ -200,10 +200,22 @@ struct mf_context {
   size_t stage_cap = 0;
 };
 
+// A copy of a buffer's columns in the layout a REDUCE kernel reads (folded
+// columns, FP64 values pre-split into float pairs), made by the kernel's
+// prep pass and kept until the buffer is written again.
+struct mf_derived {
+  uint64_t key = 0;  // what was derived (same key: same columns, same layout)
+  uint64_t gen = 0, n = 0, stride = 0;
+  void* ptr = nullptr;
+  uint64_t bytes = 0;  // allocated bytes (counted in the context's budget)
+};
+
 struct mf_buffer {
   mf_context* ctx = nullptr;
   void* ptr = nullptr;
   uint64_t size = 0;
+  uint64_t gen = 1;  // write generation: bumped by every write through the library
+  mutable std::vector<mf_derived> derived;
 };
 
 struct mf_kernel {
@@ -217,6 +229,8 @@ struct mf_kernel {
   cudaLibrary_t lib = nullptr;
   cudaKernel_t fn = nullptr;
   cudaKernel_t fn_seg = nullptr;
+  cudaKernel_t fn_prep = nullptr;  // REDUCE kernels reading prepared columns
+  uint64_t prep_key = 0;
   int blocks_per_sm = 1;
   int max_input = -1;
   bool holds_ref = false;  // counted in ctx->refs
@@ -298,6 +312,88 @@ int check_layout(const mf_kernel* k, const mf_buffer* in, uint64_t stride, uint6
     return fail(MF_ERR_INVALID, "input buffer smaller than columns x stride (" + std::to_string(need) + " > " +
                                     std::to_string(in->size) + " bytes)");
   return MF_OK;
+}
+
+uint64_t fnv1a(const void* p, size_t n, uint64_t h = 0xcbf29ce484222325ULL) {
+  const unsigned char* b = static_cast<const unsigned char*>(p);
+  for (size_t i = 0; i < n; i++) h = (h ^ b[i]) * 0x100000001b3ULL;
+  return h;
+}
+
+uint64_t prep_key(const mf_kernel* k) {
+  const auto& lk = k->lowered;
+  uint64_t h = fnv1a(&lk.prep, sizeof lk.prep);
+  h = fnv1a(&k->elem, sizeof k->elem, h);
+  for (const auto& col : lk.prep_cols) {
+    const uint64_t nt = col.size();
+    h = fnv1a(&nt, sizeof nt, h);
+    for (const auto& [src, c] : col) {
+      h = fnv1a(&src, sizeof src, h);
+      h = fnv1a(&c, sizeof c, h);
+    }
+  }
+  return h;
+}
+
+// The device columns kernel `k` reads for input buffer `in`: the buffer
+// itself, or its prepared copy, (re)made on the context's stream when the
+// buffer was written since (or n / stride changed).
+int prepare_input(const mf_kernel* k, const mf_buffer* in, uint64_t stride, uint64_t n, const void** data) {
+  if (!k->lowered.prep) {
+    *data = in->ptr;
+    return MF_OK;
+  }
+  mf_context* c = k->ctx;
+  mf_derived* d = nullptr;
+  for (auto& x : in->derived)
+    if (x.key == k->prep_key) d = &x;
+  if (d && d->gen == in->gen && d->n == n && d->stride == stride) {
+    *data = d->ptr;
+    return MF_OK;
+  }
+  const uint64_t need = (uint64_t(k->lowered.prep_cols.size()) * stride * k->lowered.prep_elem_bytes() + 255) &
+                        ~uint64_t(255);
+  if (!d || d->bytes < need) {
+    const uint64_t old = d ? d->bytes : 0;
+    if (c->budget && c->allocated.load() - old + need > c->budget)
+      return fail(MF_ERR_BUDGET, "the prepared copy of an input (" + std::to_string(need) +
+                                     " bytes) exceeds the HBM budget");
+    if (d && d->ptr) {
+      MF_CUDA_TRY(cudaStreamSynchronize(c->stream));
+      cudaFree(d->ptr);
+      c->allocated -= d->bytes;
+      d->ptr = nullptr;
+      d->bytes = 0;
+    }
+    if (!d) {
+      in->derived.push_back(mf_derived{});
+      d = &in->derived.back();
+      d->key = k->prep_key;
+    }
+    MF_CUDA_TRY(cudaMalloc(&d->ptr, std::max<uint64_t>(need, 256)));
+    d->bytes = need;
+    c->allocated += need;
+  }
+  const uint64_t blocks = (stride + 255) / 256;
+  const int grid = int(std::max<uint64_t>(1, std::min<uint64_t>(blocks, uint64_t(c->num_sms) * 16)));
+  const void* src = in->ptr;
+  void* dst = d->ptr;
+  void* args[] = {const_cast<void**>(&src), &stride, &n, &dst};
+  MF_CUDA_TRY(cudaLaunchKernel(reinterpret_cast<const void*>(k->fn_prep), dim3(grid), dim3(256), args, 0, c->stream));
+  d->gen = in->gen;
+  d->n = n;
+  d->stride = stride;
+  *data = d->ptr;
+  return MF_OK;
+}
+
+void free_derived(const mf_buffer* b) {
+  for (auto& d : b->derived)
+    if (d.ptr) {
+      cudaFree(d.ptr);
+      b->ctx->allocated -= d.bytes;
+    }
+  b->derived.clear();
 }
 
 }  // namespace
@@ -395,6 +491,7 @@ int mf_buffer_free(mf_buffer* b) {
   mf_context* c = b->ctx;
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
+  free_derived(b);
   cudaFree(b->ptr);
   c->allocated -= (b->size + 255) & ~uint64_t(255);
   delete b;
@@ -406,10 +503,17 @@ uint64_t mf_buffer_size(const mf_buffer* b) { return b ? b->size : 0; }
 
 void* mf_buffer_device_ptr(const mf_buffer* b) { return b ? b->ptr : nullptr; }
 
+int mf_buffer_mark_modified(mf_buffer* b) {
+  if (!b) return fail(MF_ERR_INVALID, "null buffer");
+  b->gen++;
+  return MF_OK;
+}
+
 int mf_buffer_h2d(mf_buffer* b, uint64_t off, const void* src, uint64_t nbytes) {
   if (!b || (!src && nbytes)) return fail(MF_ERR_INVALID, "null argument");
   if (off + nbytes > b->size) return fail(MF_ERR_INVALID, "copy beyond the end of the buffer");
   MF_CUDA_TRY(cudaSetDevice(b->ctx->device));
+  b->gen++;
   MF_CUDA_TRY(cudaMemcpyAsync(static_cast<char*>(b->ptr) + off, src, nbytes, cudaMemcpyHostToDevice, b->ctx->stream));
   MF_CUDA_TRY(cudaStreamSynchronize(b->ctx->stream));
   return MF_OK;
@@ -428,6 +532,7 @@ int mf_buffer_d2h(const mf_buffer* b, uint64_t off, void* dst, uint64_t nbytes) 
 int mf_buffer_memset(mf_buffer* b, int value) {
   if (!b) return fail(MF_ERR_INVALID, "null buffer");
   MF_CUDA_TRY(cudaSetDevice(b->ctx->device));
+  b->gen++;
   MF_CUDA_TRY(cudaMemsetAsync(b->ptr, value, b->size, b->ctx->stream));
   MF_CUDA_TRY(cudaStreamSynchronize(b->ctx->stream));
   return MF_OK;
@@ -448,6 +553,7 @@ static int events_copy(bool up, mf_buffer* b, int elem, void* host, uint32_t nco
   if (ncols == 0) return MF_OK;
   MF_CUDA_TRY(cudaSetDevice(b->ctx->device));
   if (up) {
+    b->gen++;
     if (n)
       MF_CUDA_TRY(cudaMemcpy2DAsync(b->ptr, ds * es, host, hs * es, n * es, ncols, cudaMemcpyHostToDevice,
                                     b->ctx->stream));
@@ -497,7 +603,7 @@ int mf_kernel_build(mf_context* c, const mf_kernel_desc* d, mf_kernel** out) {
   k->n_gen_dims = d->kind == MF_KERNEL_GENERATE ? d->n_gen_dims : 0;
   int lrc = lower_desc(d, k->lowered);
   if (lrc) return lrc;
-  for (int i : k->lowered.used_inputs) k->max_input = std::max(k->max_input, i);
+  for (int i : k->lowered.source_inputs) k->max_input = std::max(k->max_input, i);
   int rc = compile_source(k->lowered.source, k->name, k->image, k->lowered.entry);
   if (rc) return rc;
   MF_CUDA_TRY(cudaSetDevice(c->device));
@@ -505,6 +611,10 @@ int mf_kernel_build(mf_context* c, const mf_kernel_desc* d, mf_kernel** out) {
   MF_CUDA_TRY(cudaLibraryGetKernel(&k->fn, k->lib, k->lowered.entry.c_str()));
   if (d->kind == MF_KERNEL_REDUCE)
     MF_CUDA_TRY(cudaLibraryGetKernel(&k->fn_seg, k->lib, (k->lowered.entry + "_segments").c_str()));
+  if (k->lowered.prep) {
+    MF_CUDA_TRY(cudaLibraryGetKernel(&k->fn_prep, k->lib, (k->lowered.entry + "_prep").c_str()));
+    k->prep_key = prep_key(k.get());
+  }
   if (k->lowered.smem_bytes > 48 * 1024)
     MF_CUDA_TRY(cudaFuncSetAttribute(reinterpret_cast<const void*>(k->fn), cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      int(k->lowered.smem_bytes)));
@@ -684,6 +794,17 @@ int mf_kernel_info(const mf_kernel* k, int* regs, int* spill, int* block, int* v
   return MF_OK;
 }
 
+int mf_kernel_read_layout(const mf_kernel* k, uint32_t* columns, uint32_t* bytes_per_event, uint32_t* source_columns) {
+  if (!k) return fail(MF_ERR_INVALID, "kernel is null");
+  const auto& lk = k->lowered;
+  const uint32_t cols = uint32_t(lk.prep ? lk.prep_cols.size() : lk.used_inputs.size());
+  const uint32_t es = uint32_t(lk.prep ? lk.prep_elem_bytes() : elem_size(k->elem));
+  if (columns) *columns = cols;
+  if (bytes_per_event) *bytes_per_event = cols * es;
+  if (source_columns) *source_columns = uint32_t(lk.source_inputs.size());
+  return MF_OK;
+}
+
 }  // extern "C"
 
 namespace mfi {
@@ -738,7 +859,10 @@ int mf_kernel_reduce(mf_kernel* k, const mf_buffer* in, uint64_t stride, uint64_
   rc = ensure_scratch(c, size_t(grid) * k->n_outputs, k->n_outputs);
   if (rc) return rc;
   *c->status_host = 0u;
-  rc = mfi::launch_reduce(k, in->ptr, stride, n, params, c->partials, c->counter, c->out_dev, c->stream, 0);
+  const void* data = nullptr;
+  rc = prepare_input(k, in, stride, n, &data);
+  if (rc) return rc;
+  rc = mfi::launch_reduce(k, data, stride, n, params, c->partials, c->counter, c->out_dev, c->stream, 0);
   if (rc) return rc;
   MF_CUDA_TRY(cudaStreamSynchronize(c->stream));
   std::memcpy(sums, c->out_host, k->n_outputs * sizeof(double));
@@ -761,7 +885,10 @@ int mf_kernel_reduce_async(mf_kernel* k, const mf_buffer* in, uint64_t stride, u
   rc = ensure_scratch(c, size_t(grid) * k->n_outputs, k->n_outputs);
   if (rc) return rc;
   double* dst = static_cast<double*>(out->ptr) + out_index * k->n_outputs;
-  return mfi::launch_reduce(k, in->ptr, stride, n, params, c->partials, c->counter, dst, c->stream, 0);
+  const void* data = nullptr;
+  rc = prepare_input(k, in, stride, n, &data);
+  if (rc) return rc;
+  return mfi::launch_reduce(k, data, stride, n, params, c->partials, c->counter, dst, c->stream, 0);
 }
 
 int mf_kernel_reduce_many(mf_kernel* k, uint32_t count, const mf_buffer* const* inputs, const uint64_t* strides,
@@ -784,8 +911,11 @@ int mf_kernel_reduce_many(mf_kernel* k, uint32_t count, const mf_buffer* const* 
   if (rc) return rc;
   for (uint32_t i = 0; i < count; i++) {
     double* dst = static_cast<double*>(out->ptr) + uint64_t(i) * k->n_outputs;
-    rc = mfi::launch_reduce(k, inputs[i]->ptr, strides[i], ns[i], params + uint64_t(i) * n_params, c->partials,
-                            c->counter, dst, c->stream, 0);
+    const void* data = nullptr;
+    rc = prepare_input(k, inputs[i], strides[i], ns[i], &data);
+    if (rc) return rc;
+    rc = mfi::launch_reduce(k, data, strides[i], ns[i], params + uint64_t(i) * n_params, c->partials, c->counter, dst,
+                            c->stream, 0);
     if (rc) return rc;
   }
   return MF_OK;
@@ -857,7 +987,9 @@ int mf_kernel_reduce_segments(mf_kernel* k, const mf_buffer* in, uint64_t stride
   const unsigned* d_count = reinterpret_cast<const unsigned*>(base + bytes_begin);
   const void* d_par = base + bytes_begin + bytes_count;
   double* outp = c->out_dev;
-  const void* data = in->ptr;
+  const void* data = nullptr;
+  rc = prepare_input(k, in, stride, end, &data);
+  if (rc) return rc;
   void* args[] = {const_cast<void**>(&data), &stride, &d_begin, &d_count, const_cast<void**>(&d_par), &outp};
   MF_CUDA_TRY(cudaLaunchKernel(reinterpret_cast<const void*>(k->fn_seg), dim3(nseg), dim3(k->lowered.block), args, 0,
                                c->stream));
@@ -885,6 +1017,7 @@ int mf_kernel_store(mf_kernel* k, const mf_buffer* in, uint64_t in_stride, uint6
   if (k->n_params) std::memcpy(pv.data(), params, k->n_params * sizeof(double));
   const void* data = in->ptr;
   void* outp = out->ptr;
+  out->gen++;
   void* args[] = {const_cast<void**>(&data), &in_stride, &n, pv.data(), &outp, &out_stride};
   MF_CUDA_TRY(cudaLaunchKernel(reinterpret_cast<const void*>(k->fn), dim3(grid), dim3(k->lowered.block), args, 0,
                                c->stream));
@@ -914,6 +1047,7 @@ int mf_kernel_generate(mf_kernel* k, const uint32_t* seeds, uint32_t nseeds, uin
   if (k->n_params) std::memcpy(pv.data(), params, k->n_params * sizeof(double));
   const unsigned* sd = static_cast<const unsigned*>(c->stage_dev);
   void* outp = out->ptr;
+  out->gen++;
   unsigned* status = c->status;
   unsigned long long mt = max_tries ? max_tries : 1000000000ULL;
   void* args[] = {&sd, &nseeds, &n, &nper, pv.data(), &outp, &out_stride, &status, &mt};

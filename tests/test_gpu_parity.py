@@ -176,6 +176,65 @@ def test_ragged_segments(backend):
         assert_sums_close(out[s], ref, scale, what=f"segment {s}")
 
 
+def test_prepared_columns_follow_writes(backend, oracle_lib):
+    """REDUCE kernels read a prepared copy of their input (folded columns, FP64
+    as float pairs). A write through the library, or a raw device write
+    declared with mf_buffer_mark_modified, makes the next launch re-derive it."""
+    import torch
+    from morefit_gb300 import _lib as L
+    from morefit_gb300.workloads import Likelihood
+    g = load_golden("pwave_n1000.json")
+    ev = golden_events("pwave", 1000)
+    evb = np.ascontiguousarray(oracle_lib.generate("pwave", 2000, seed=12345)[:, 1000:])  # other events, same n
+    p = g["points"][1]["kernel_params"]["lh_grad_kernel"]
+    like = Likelihood(backend, g, np.float64)
+    like.set_data(ev)
+    a = like.sums("lh_grad_kernel", param_vector=p)
+    like.set_data(evb)  # upload + precompute into the same buffers
+    b = like.sums("lh_grad_kernel", param_vector=p)
+    other = Likelihood(backend, g, np.float64)
+    other.set_data(evb)
+    assert np.array_equal(b, other.sums("lh_grad_kernel", param_vector=p))
+    assert not np.allclose(a, b)
+    # copy dataset A's hoisted columns into the buffer behind the library's back
+    fresh = Likelihood(backend, g, np.float64)
+    fresh.set_data(ev)
+    dst, src = like.input_block("lh_grad_kernel").buf, fresh.input_block("lh_grad_kernel").buf
+    nbytes = int(L.lib.mf_buffer_size(dst))
+    assert nbytes == int(L.lib.mf_buffer_size(src))
+
+    class _Dev:
+        def __init__(self, ptr):
+            self.__cuda_array_interface__ = {"shape": (nbytes,), "typestr": "|u1", "data": (ptr, False),
+                                             "version": 3}
+
+    backend.synchronize()
+    torch.as_tensor(_Dev(L.lib.mf_buffer_device_ptr(dst)), device="cuda").copy_(
+        torch.as_tensor(_Dev(L.lib.mf_buffer_device_ptr(src)), device="cuda"))
+    torch.cuda.synchronize()
+    L.check(L.lib.mf_buffer_mark_modified(dst))
+    assert np.array_equal(like.sums("lh_grad_kernel", param_vector=p), a)
+
+
+def test_budget_covers_prepared_copies():
+    """The prepared copy of an input is allocated against the context's HBM budget."""
+    from morefit_gb300 import _lib as L
+    from morefit_gb300.backend import CUDABackend
+    from morefit_gb300.workloads import Likelihood
+    g = load_golden("pwave_n1000.json")
+    n = 100000
+    ev = np.tile(golden_events("pwave", 1000), (1, n // 1000))
+    # raw (3 columns) + hoisted (14 columns) FP64 fit in the budget; the 9 prepared columns do not
+    need = 17 * 8 * n
+    b = CUDABackend(0, hbm_budget_bytes=need + (1 << 20))
+    like = Likelihood(b, g, np.float64)
+    like.set_data(ev)
+    with pytest.raises(L.MFError, match="BUDGET"):
+        like.sums("lh_grad_kernel", param_vector=g["points"][1]["kernel_params"]["lh_grad_kernel"])
+    del like
+    b.close()
+
+
 def test_budget_is_enforced():
     from morefit_gb300 import _lib as L
     from morefit_gb300.backend import CUDABackend, DeviceColumns

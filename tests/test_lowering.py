@@ -20,11 +20,40 @@ def test_shared_subexpressions_evaluated_once():
     assert body.count("__drcp_rn(") == 2
     dw = _src(g, "lh_grad_kernel", L.MF_F64)
     body = dw[dw.index("void __launch_bounds__(MF_BLOCK) mf_reduce("):dw.index("mf_reduce_segments(")]
-    # pipelined double-float kernel: one event per thread per tile
-    assert body.count("mf_dw_log(") == 1 and body.count("mf_dw_rcp(") == 1
+    # double-float kernel: two events per thread, one log and one reciprocal each
+    assert body.count("mf_dw_log(") == 2 and body.count("mf_dw_rcp(") == 2
     assert " log(" not in body
-    # only the 11 hoisted basis columns are read; ctl, ctk, phi are not
-    assert "data + (mf_u64)0 * stride" not in body and "data + (mf_u64)13 * stride" in body
+    # the event loop reads the 9 folded basis columns as float pairs
+    assert "data + (mf_u64)8 * stride" in body and "data + (mf_u64)9 * stride" not in body
+    assert "const float2 l8 = " in body and "mf_dw_split(" not in body
+
+
+def test_pwave_basis_folds_to_nine_columns():
+    """The 11 hoisted angular columns enter the density and every derivative
+    only as S9*b3 + ... - Fl*b10 + pb0*(b11 + b12) + Fl*b13: b11 + b12 and
+    b10 - b13 are the only combinations the kernels need."""
+    from morefit_gb300 import _lib as L
+    g = load_golden("pwave_n1000.json")
+    for name in ("lh_kernel", "lh_grad_kernel", "lh_hessian_kernel"):
+        for elem, native in ((L.MF_F64, False), (L.MF_F64, True), (L.MF_F32, False)):
+            src = _src(g, name, elem, native_f64=native)
+            assert "// reads 9 prepared columns" in src, (name, elem, native)
+            assert "//   y7 = + 1*morefit_eventbuffer_10 + -1*morefit_eventbuffer_13" in src
+            assert "//   y8 = + 1*morefit_eventbuffer_11 + 1*morefit_eventbuffer_12" in src
+            prep = src[src.index("mf_reduce_prep("):]
+            # the prep pass reads the source columns (3..13), never the raw observables
+            assert "data + (mf_u64)13 * stride" in prep and "data + (mf_u64)0 * stride" not in prep
+
+
+def test_mass_kernels_do_not_fold():
+    """One observable column: nothing to fold. The double-float kernels still
+    read it pre-split; the FP32 kernels read the input buffer directly."""
+    from morefit_gb300 import _lib as L
+    g = load_golden("mass_n1000.json")
+    dw = _src(g, "lh_grad_kernel", L.MF_F64)
+    assert "// reads 1 prepared columns (FP64 as float pairs)" in dw
+    f32 = _src(g, "lh_grad_kernel", L.MF_F32)
+    assert "prepared" not in f32 and "mf_reduce_prep(" not in f32
 
 
 def test_hessian_kernel_shares_the_density():
