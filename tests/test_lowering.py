@@ -25,7 +25,7 @@ def test_shared_subexpressions_evaluated_once():
     assert " log(" not in body
     # the event loop reads the 9 folded basis columns as float pairs
     assert "data + (mf_u64)8 * stride" in body and "data + (mf_u64)9 * stride" not in body
-    assert "const float2 l8 = " in body and "mf_dw_split(" not in body
+    assert "const float4 l8 = " in body and "mf_dw_split(" not in body
 
 
 def test_pwave_basis_folds_to_nine_columns():
