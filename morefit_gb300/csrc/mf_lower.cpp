@@ -467,6 +467,16 @@ __device__ __forceinline__ void mf_neumaier(double& s, double& c, double x) {
   c += (fabs(s) >= fabs(x)) ? ((s - t) + x) : ((x - t) + s);
   s = t;
 }
+// Programmatic dependent launch (PTX griddepcontrol): no-ops unless the grid
+// was launched with programmatic stream serialization.
+__device__ __forceinline__ void mf_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void mf_grid_dependency_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+// Device-scope fetch-and-add with acquire-release semantics.
+__device__ __forceinline__ unsigned mf_atom_add_acq_rel(unsigned* p, unsigned v) {
+  unsigned old;
+  asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+  return old;
+}
 // Kahan step for FP32 per-thread partials (compute_llvm.hh:556-568 semantics).
 __device__ __forceinline__ void mf_kahan_f32(float& s, float& c, float x) {
   const float y = __fsub_rn(x, c);
@@ -1011,6 +1021,7 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
     s << "extern \"C\" __global__ void __launch_bounds__(MF_BLOCK) " << out.entry << "(const " << DT
       << "* __restrict__ data, mf_u64 stride, mf_u64 n, mf_args P, float2* __restrict__ partials,"
       << " unsigned* __restrict__ counter, double* __restrict__ out, unsigned* __restrict__ status) {\n";
+    s << "  mf_launch_dependents();  // the next evaluation may start its event loop on SMs this grid frees\n";
     load_table(s);
     prologue(s, "P.");
     acc_decl(s);
@@ -1108,17 +1119,22 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
     s << R"CUDA(    if (lane == 0) red[j][warp] = make_float2(a.h, a.l);
   }
   __syncthreads();
+  // Launched as a programmatic dependent of the previous evaluation on the
+  // stream (batched evaluations), this grid ran its event loop while that
+  // one finished; the scratch below is shared, so wait for it to complete.
+  mf_grid_dependency_wait();
   for (int j = threadIdx.x; j < MF_NOUT; j += MF_BLOCK) {
     mf_dw b = mf_dw_make(red[j][0].x, red[j][0].y);
     for (int w = 1; w < MF_BLOCK / 32; w++) b = mf_dw_add(b, mf_dw_make(red[j][w].x, red[j][w].y));
     partials[(mf_u64)blockIdx.x * MF_NOUT + j] = make_float2(b.h, b.l);
   }
-  __threadfence();
+  // Completion count with release/acquire semantics: the barrier orders the
+  // block's partial writes before thread 0's release; the last block's
+  // acquire plus the barrier orders its reads of every partial after.
   __syncthreads();
-  if (threadIdx.x == 0) am_last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+  if (threadIdx.x == 0) am_last = (mf_atom_add_acq_rel(counter, 1u) == gridDim.x - 1);
   __syncthreads();
   if (!am_last) return;
-  __threadfence();
   // Fixed-order double-float combine of the block partials by the whole last
   // block: thread t takes blocks t, t + MF_BLOCK, ... for every output (all
   // loads of a round issued before the adds), then a warp tree and a pass

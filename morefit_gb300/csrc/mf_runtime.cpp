@@ -238,7 +238,8 @@ struct mf_kernel {
 
 namespace mfi {
 int launch_reduce(mf_kernel* k, const void* data, uint64_t stride, uint64_t n, const double* params,
-                  double* partials, unsigned* counter, double* out, cudaStream_t stream, int grid_cap);
+                  double* partials, unsigned* counter, double* out, cudaStream_t stream, int grid_cap,
+                  bool dependent = false);
 }
 
 // ---------------------------------------------------------------- helpers --
@@ -817,9 +818,14 @@ int grid_for(const mf_kernel* k, uint64_t n) {
   return int(std::min(need, cap));
 }
 
-// Launches one REDUCE kernel; `out` is a device-visible address for n_outputs doubles.
+// Launches one REDUCE kernel; `out` is a device-visible address for n_outputs
+// doubles. `dependent`: the previous operation on the stream is a REDUCE
+// launch of this library that writes nothing this launch reads; the grid may
+// then start (programmatic dependent launch) while that one finishes, and
+// waits for it before it touches the shared scratch.
 int launch_reduce(mf_kernel* k, const void* data, uint64_t stride, uint64_t n, const double* params,
-                  double* partials, unsigned* counter, double* out, cudaStream_t stream, int grid_cap) {
+                  double* partials, unsigned* counter, double* out, cudaStream_t stream, int grid_cap,
+                  bool dependent) {
   int grid = grid_for(k, n);
   if (grid_cap > 0) grid = std::min(grid, grid_cap);
   // argument struct: parameter-only values evaluated here, pre-rounded for the kernel's arithmetic
@@ -831,8 +837,17 @@ int launch_reduce(mf_kernel* k, const void* data, uint64_t stride, uint64_t n, c
   }
   unsigned* status = k->ctx->status;
   void* args[] = {const_cast<void**>(&data), &stride, &n, pv.data(), &partials, &counter, &out, &status};
-  MF_CUDA_TRY(cudaLaunchKernel(reinterpret_cast<const void*>(k->fn), dim3(grid), dim3(k->lowered.block), args,
-                               k->lowered.smem_bytes, stream));
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(k->lowered.block);
+  cfg.dynamicSmemBytes = k->lowered.smem_bytes;
+  cfg.stream = stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = dependent ? 1 : 0;
+  MF_CUDA_TRY(cudaLaunchKernelExC(&cfg, reinterpret_cast<const void*>(k->fn), args));
   return MF_OK;
 }
 
@@ -909,13 +924,31 @@ int mf_kernel_reduce_many(mf_kernel* k, uint32_t count, const mf_buffer* const* 
   for (uint32_t i = 0; i < count; i++) maxgrid = std::max(maxgrid, mfi::grid_for(k, ns[i]));
   int rc = ensure_scratch(c, size_t(maxgrid) * k->n_outputs, k->n_outputs);
   if (rc) return rc;
-  for (uint32_t i = 0; i < count; i++) {
-    double* dst = static_cast<double*>(out->ptr) + uint64_t(i) * k->n_outputs;
-    const void* data = nullptr;
-    rc = prepare_input(k, inputs[i], strides[i], ns[i], &data);
+  // Prepared inputs first, then the evaluations back to back: each after the
+  // first may overlap its predecessor's tail (it reads only its own input).
+  // A buffer that appears with two different layouts in one batch would have
+  // its prepared copy remade between uses: prepare and launch one by one.
+  bool one_by_one = false;
+  if (k->lowered.prep) {
+    std::map<const mf_buffer*, std::pair<uint64_t, uint64_t>> layout;
+    for (uint32_t i = 0; i < count && !one_by_one; i++) {
+      auto [it, fresh] = layout.emplace(inputs[i], std::make_pair(ns[i], strides[i]));
+      one_by_one = !fresh && it->second != std::make_pair(ns[i], strides[i]);
+    }
+  }
+  std::vector<const void*> data(count, nullptr);
+  for (uint32_t i = 0; i < count && !one_by_one; i++) {
+    rc = prepare_input(k, inputs[i], strides[i], ns[i], &data[i]);
     if (rc) return rc;
-    rc = mfi::launch_reduce(k, data, strides[i], ns[i], params + uint64_t(i) * n_params, c->partials, c->counter, dst,
-                            c->stream, 0);
+  }
+  for (uint32_t i = 0; i < count; i++) {
+    if (one_by_one) {
+      rc = prepare_input(k, inputs[i], strides[i], ns[i], &data[i]);
+      if (rc) return rc;
+    }
+    double* dst = static_cast<double*>(out->ptr) + uint64_t(i) * k->n_outputs;
+    rc = mfi::launch_reduce(k, data[i], strides[i], ns[i], params + uint64_t(i) * n_params, c->partials, c->counter,
+                            dst, c->stream, 0, i > 0 && !one_by_one);
     if (rc) return rc;
   }
   return MF_OK;

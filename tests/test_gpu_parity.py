@@ -216,6 +216,46 @@ def test_prepared_columns_follow_writes(backend, oracle_lib):
     assert np.array_equal(like.sums("lh_grad_kernel", param_vector=p), a)
 
 
+@pytest.mark.parametrize("mixed_n", [False, True])
+def test_batched_evaluations_match_single(backend, oracle_lib, mixed_n):
+    """mf_kernel_reduce_many (evaluations overlapping their predecessors' tails)
+    gives bit-identical sums to one mf_kernel_reduce per evaluation, also when
+    one buffer appears with two event counts in a batch."""
+    import ctypes as C
+    from morefit_gb300 import _lib as L
+    from morefit_gb300.workloads import Likelihood
+    g = load_golden("pwave_n1000.json")
+    n = 20000
+    sets = []
+    for seed in range(3):
+        like = Likelihood(backend, g, np.float64)
+        like.set_data(oracle_lib.generate("pwave", n, seed=1000 + seed))
+        sets.append(like)
+    k = sets[0].blocks["lh_grad_kernel"].kernel
+    order = [0, 1, 2, 0, 2, 1, 1, 0] * 4
+    counts = [n - 5003 * (i % 2) if (mixed_n and o == 0) else n for i, o in enumerate(order)]
+    rows = np.array([g["points"][i % 3]["kernel_params"]["lh_grad_kernel"] for i in range(len(order))])
+    single = np.zeros((len(order), k.nout))
+    for i, o in enumerate(order):
+        blk = sets[o].input_block()
+        L.check(L.lib.mf_kernel_reduce(k.handle, blk.buf, blk.stride, counts[i], L.dptr(rows[i]), rows.shape[1],
+                                       L.dptr(single[i])))
+    ins = (L.c_buf * len(order))(*[sets[o].input_block().buf for o in order])
+    strides = np.array([sets[o].input_block().stride for o in order], np.uint64)
+    ns = np.array(counts, np.uint64)
+    out = L.c_buf()
+    L.check(L.lib.mf_buffer_alloc(backend.handle, single.nbytes, C.byref(out)))
+    u64p = C.POINTER(C.c_uint64)
+    L.check(L.lib.mf_kernel_reduce_many(k.handle, len(order), ins, strides.ctypes.data_as(u64p),
+                                        ns.ctypes.data_as(u64p), L.dptr(np.ascontiguousarray(rows)), rows.shape[1],
+                                        out))
+    got = np.zeros_like(single)
+    L.check(L.lib.mf_buffer_d2h(out, 0, got.ctypes.data, got.nbytes))
+    L.check(L.lib.mf_buffer_free(out))
+    assert np.isfinite(single).all()
+    assert np.array_equal(got, single)
+
+
 def test_budget_covers_prepared_copies():
     """The prepared copy of an input is allocated against the context's HBM budget."""
     from morefit_gb300 import _lib as L
