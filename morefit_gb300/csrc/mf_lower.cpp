@@ -552,6 +552,127 @@ __device__ __forceinline__ mf_dw mf_dw_split(double x) {
   return mf_dw_make(__uint_as_float(hb), __uint_as_float(__float_as_uint(l) | sign));
 }
 __device__ __forceinline__ mf_dw mf_dw_pair(float2 t) { return mf_dw_make(t.x, t.y); }
+// Round-to-nearest split with integer operations only: h = x rounded to 24
+// bits, l = x - h rounded to 24 bits, |x - h - l| <= 2^-48 |x| for |x| from
+// 2^-100 to 2^127 (below 2^-100 l loses bits to the FP32 exponent range).
+// Magnitudes outside [2^-126, 2^127) (and zero, inf, NaN) take the
+// truncating split. No FP64 instruction on any path: a short FP64 fallback
+// would be if-converted and executed for every value.
+__device__ __forceinline__ mf_dw mf_dw_split_rn(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned e = (unsigned)(b >> 52) & 0x7ffu;
+  if (e < 897u || e > 1149u) return mf_dw_split(x);
+  const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+  const unsigned long long M = (b & 0xfffffffffffffull) | 0x10000000000000ull;  // 53-bit significand
+  const unsigned long long H = (M + 0x10000000ull) >> 29;                       // nearest 24-bit value
+  const long long L = (long long)M - (long long)(H << 29);                      // |L| <= 2^28
+  const unsigned carry = (unsigned)(H >> 24);                                   // H = 2^24: next binade
+  const float h = __uint_as_float(sign | ((e - 896u + carry) << 23) | (carry ? 0u : ((unsigned)H & 0x7fffffu)));
+  const unsigned al = (unsigned)(L < 0 ? -L : L);
+  // |L| rounded to its top 24 bits as an exact float (exponent-field trick),
+  // scaled by 2^(e - 1070) (as 2^(e - 1006) * 2^-64 where e - 1070 < -126)
+  const float m = __fsub_rn(__uint_as_float(0x4b000000u | ((al + 16u) >> 5)), 8388608.0f);
+  const bool low = e < 944u;
+  const float lm = __fmul_rn(__fmul_rn(m, __uint_as_float((low ? e - 879u : e - 943u) << 23)),
+                             low ? 0x1p-64f : 1.0f);
+  return mf_dw_make(h, __uint_as_float(__float_as_uint(lm) | (sign ^ (L < 0 ? 0x80000000u : 0u))));
+}
+// h + l as an FP64 value with integer operations only: h's significand
+// extended by l's bits down to the double's last place (l's bits below it
+// are dropped, an error below one unit in the last place). The pair is
+// renormalized first; zero or subnormal h gives a signed zero (an absolute
+// error below 2^-125), inf and NaN carry over.
+__device__ __forceinline__ double mf_dw_to_double_bits(mf_dw a) {
+  a = mf_fast_two_sum(a.h, a.l);
+  const unsigned hb = __float_as_uint(a.h), lb = __float_as_uint(a.l);
+  const int eh = (int)((hb >> 23) & 0xffu), el = (int)((lb >> 23) & 0xffu);
+  const int k = 29 + el - eh;  // scale of l's significand in units of the double's last place (<= 5)
+  if (eh == 0 || eh == 255)
+    return __longlong_as_double((long long)(((unsigned long long)(hb >> 31) << 63) |
+                                            (eh ? (0x7ffull << 52) | ((hb & 0x7fffffu) ? (1ull << 51) : 0ull) : 0ull)));
+  unsigned long long M = (unsigned long long)((hb & 0x7fffffu) | 0x800000u) << 29;
+  int E = eh;
+  if (el != 0) {
+    const unsigned long long ml = (lb & 0x7fffffu) | 0x800000u;
+    const unsigned long long v = k >= 0 ? (ml << k) : (k > -40 ? (ml >> -k) : 0ull);
+    if ((hb ^ lb) >> 31) {
+      M -= v;
+      if (M < (1ull << 52)) { M <<= 1; E -= 1; }
+    } else {
+      M += v;
+      if (M >= (1ull << 53)) { M >>= 1; E += 1; }
+    }
+  }
+  return __longlong_as_double((long long)(((unsigned long long)(hb >> 31) << 63) |
+                                          ((unsigned long long)(E + 896) << 52) | (M & 0xfffffffffffffull)));
+}
+__device__ __forceinline__ mf_dw mf_dw_mulf(mf_dw a, float b) {
+  const float p = __fmul_rn(a.h, b);
+  return mf_fast_two_sum(p, __fmaf_rn(a.l, b, __fmaf_rn(a.h, b, -p)));
+}
+// Square root: the correctly rounded FP32 root s of a.h, corrected by the
+// series sqrt(s^2 + r) = s + d - d^2/(2s) + ..., d = r/(2s). d reaches
+// 2^-23 s, so the residual r = a - s^2 (s^2 exact by FMA) and d are kept as
+// double-float values; the next term, d^3/(2s^2), is below 2^-70 s.
+// sqrt(0) = 0, negative or NaN -> NaN, +inf -> +inf.
+__device__ __forceinline__ mf_dw mf_dw_sqrt(mf_dw a) {
+  if (!(a.h > 0.0f) || a.h == __int_as_float(0x7f800000))
+    return mf_dw_make(a.h == 0.0f ? 0.0f : (a.h > 0.0f ? a.h : __int_as_float(0x7fc00000)), 0.0f);
+  const float s = __fsqrt_rn(a.h);
+  const float p = __fmul_rn(s, s);
+  const float pe = __fmaf_rn(s, s, -p);
+  // a.h - p is exact (Sterbenz); the rest of the residual in double-float
+  const mf_dw r = mf_dw_add(mf_two_sum(__fsub_rn(a.h, p), -pe), mf_dw_make(a.l, 0.0f));
+  const float s2 = __fadd_rn(s, s);
+  const float dh = __fdiv_rn(r.h, s2);
+  const float dl = __fdiv_rn(__fadd_rn(__fmaf_rn(-dh, s2, r.h), r.l), s2);
+  const float q = __fdiv_rn(__fmul_rn(dh, dh), s2);
+  const mf_dw t = mf_fast_two_sum(s, dh);
+  return mf_fast_two_sum(t.h, __fadd_rn(t.l, __fsub_rn(dl, q)));
+}
+// sin and cos of a double-float. a = k*(pi/2) + r, |r| <~ pi/4, by a
+// four-part Cody-Waite reduction: pi/2 = C1 + C2 + C3 + C4 with C1 and C2 of
+// 12 significant bits (k*C1, k*C2 exact for |k| < 2^12) and a remainder below
+// 4e-22. sin r and cos r are their Taylor series, the terms above 2^-26 in
+// double-float (Horner), the rest in FP32; the first omitted term is below
+// 2e-16 relative. Arguments beyond |a| = 6000 (and inf/NaN) use FP64.
+__device__ __forceinline__ void mf_dw_sincos(mf_dw a, mf_dw* sn, mf_dw* cs) {
+  if (!(fabsf(a.h) <= 6000.0f)) {
+    const double x = mf_dw_to_double(a);
+    *sn = mf_dw_from_double(sin(x));
+    *cs = mf_dw_from_double(cos(x));
+    return;
+  }
+  const float k = rintf(__fmul_rn(a.h, 0x1.45f306p-1f));
+  const float t1 = __fmaf_rn(-k, 0x1.92p+0f, a.h);  // exact
+  mf_dw r = mf_two_sum(t1, -__fmul_rn(k, 0x1.fb4p-12f));
+  const float p3 = __fmul_rn(k, 0x1.4442dp-24f);
+  r = mf_dw_sub(r, mf_dw_make(p3, __fmaf_rn(k, 0x1.4442dp-24f, -p3)));
+  r = mf_dw_add(r, mf_dw_make(__fmaf_rn(-k, 0x1.846988p-48f, a.l), 0.0f));
+  const mf_dw r2 = mf_dw_mul(r, r);
+  const float z = r2.h;
+  // sin r = r + r^3 (c3 + r^2 (c5 + r^2 (c7 + r^2 (c9 + r^2 T)))), c_n = (-1)^((n-1)/2) / n!
+  const float T = __fmaf_rn(z, __fmaf_rn(z, -0x1.ae7f3ep-41f, 0x1.612462p-33f), -0x1.ae6456p-26f);
+  mf_dw q = mf_dw_add(mf_dw_make(0x1.71de3ap-19f, 0x1.55b1ccp-45f), mf_dw_mulf(r2, T));
+  q = mf_dw_add(mf_dw_make(-0x1.a01a02p-13f, 0x1.7f97fap-39f), mf_dw_mul(r2, q));
+  q = mf_dw_add(mf_dw_make(0x1.111112p-7f, -0x1.dddddep-32f), mf_dw_mul(r2, q));
+  q = mf_dw_add(mf_dw_make(-0x1.555556p-3f, 0x1.555556p-28f), mf_dw_mul(r2, q));
+  const mf_dw sr = mf_dw_add(r, mf_dw_mul(mf_dw_mul(r, r2), q));
+  // cos r = 1 + r^2 (c2 + r^2 (c4 + r^2 (c6 + r^2 (c8 + r^2 (c10 + r^2 T2))))), c_n = (-1)^(n/2) / n!
+  const float T2 = __fmaf_rn(z, __fmaf_rn(z, 0x1.ae7f3ep-45f, -0x1.93974ap-37f), 0x1.1eed8ep-29f);
+  mf_dw u = mf_dw_add(mf_dw_make(-0x1.27e4fcp-22f, 0x1.10ec14p-47f), mf_dw_mulf(r2, T2));
+  u = mf_dw_add(mf_dw_make(0x1.a01a02p-16f, -0x1.7f97fap-42f), mf_dw_mul(r2, u));
+  u = mf_dw_add(mf_dw_make(-0x1.6c16c2p-10f, 0x1.27d27ep-35f), mf_dw_mul(r2, u));
+  u = mf_dw_add(mf_dw_make(0x1.555556p-5f, -0x1.555556p-30f), mf_dw_mul(r2, u));
+  u = mf_dw_add(mf_dw_make(-0.5f, 0.0f), mf_dw_mul(r2, u));
+  const mf_dw cr = mf_dw_add(mf_dw_make(1.0f, 0.0f), mf_dw_mul(r2, u));
+  const int quad = ((int)k) & 3;
+  const mf_dw s0 = (quad & 1) ? cr : sr, c0 = (quad & 1) ? sr : cr;
+  *sn = (quad & 2) ? mf_dw_neg(s0) : s0;
+  *cs = ((quad + 1) & 2) ? mf_dw_neg(c0) : c0;
+}
+__device__ __forceinline__ mf_dw mf_dw_sin(mf_dw a) { mf_dw s, c; mf_dw_sincos(a, &s, &c); return s; }
+__device__ __forceinline__ mf_dw mf_dw_cos(mf_dw a) { mf_dw s, c; mf_dw_sincos(a, &s, &c); return c; }
 // ln of a positive double-float (see above); zero gives -inf, negative or
 // NaN gives NaN, +inf gives +inf, subnormal h is rescaled by 2^64 first.
 __device__ __forceinline__ mf_dw mf_dw_log(mf_dw a, const float4* __restrict__ tab) {
@@ -575,8 +696,12 @@ __device__ __forceinline__ mf_dw mf_dw_log(mf_dw a, const float4* __restrict__ t
   lt = mf_dw_add(lt, mf_dw_make(__fmul_rn(__fmul_rn(sh, th), P), 0.0f));
   const int Et = E - (sub ? 64 : 0);
   const float Ef = __fsub_rn(__int_as_float(0x4b400000 + Et), 12582912.0f);  // (float)Et without a conversion
-  const float eh = __fmul_rn(Ef, MF_LN2_HI);
-  const mf_dw el = mf_fast_two_sum(eh, __fmaf_rn(Ef, MF_LN2_LO, __fmaf_rn(Ef, MF_LN2_HI, -eh)));
+  // E*ln2 with ln2 = L1 + L2 + L3 (L1 of 12 bits: E*L1 exact; remainder of L3 below 1e-19)
+  const float e1 = __fmul_rn(Ef, 0x1.62ep-1f);
+  const float e2 = __fmul_rn(Ef, 0x1.0bfbe8p-15f);
+  const mf_dw e12 = mf_two_sum(e1, e2);
+  const mf_dw el = mf_fast_two_sum(
+      e12.h, __fadd_rn(e12.l, __fmaf_rn(Ef, 0x1.cf79aap-40f, __fmaf_rn(Ef, 0x1.0bfbe8p-15f, -e2))));
   mf_dw r = mf_dw_add(mf_dw_add(el, mf_dw_make(T.x, T.y)), lt);
   const float inf = __uint_as_float(0x7f800000u);
   if (a.h == 0.0f) r = mf_dw_make(-inf, 0.0f);
@@ -802,14 +927,15 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
     for (int j = 0; j < M; j++) o << indent << "const " << AT << " r" << j << " = " << em.ref(roots[j], "e") << ";\n";
   };
 
-  if (kind == Kind::Reduce) {
+  if (kind == Kind::Reduce || (kind == Kind::Store && !native_f64)) {
     // Arithmetic of the per-event body: FP32 (mixed precision), FP64, or
-    // double-float on FP32 pairs (the default for FP64 storage).
+    // double-float on FP32 pairs (the default for FP64 storage, and for
+    // STORE kernels unless native FP64 is asked for).
     // F32S: FP64 storage, FP32 arithmetic, except that a sum or difference of
     // an input column and a parameter-only value is formed in FP64 before it
     // is rounded (keeps m - mu exact for observables with a large offset).
     enum class Ar { F32, F64, DW, F32S } ar =
-        st32 ? Ar::F32 : (f32_arith ? Ar::F32S : (native_f64 ? Ar::F64 : Ar::DW));
+        kind == Kind::Store ? Ar::DW : st32 ? Ar::F32 : (f32_arith ? Ar::F32S : (native_f64 ? Ar::F64 : Ar::DW));
     auto is_leafish = [&](int k) {
       const Op o = ns[k].op;
       return o == Op::Input || ns[k].uniform;
@@ -827,7 +953,7 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
       if (live[i] && !ns[i].uniform && ns[i].op == Op::Log) has_log = true;
     // The double-float library is always present: every cross-thread sum
     // (warp, block, grid) runs in double-float on the FP32 pipe.
-    s << dw_log_table() << kDwPrelude << kBulkPrelude;
+    s << dw_log_table() << kDwPrelude << (kind == Kind::Reduce ? kBulkPrelude : "");
     // ---- leaves and statements of the per-event body ----
     auto eref = [&](int id) -> std::string {
       const Node& n = ns[id];
@@ -861,6 +987,20 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
       if (n.op == Op::Param) return "p" + std::to_string(n.index);
       return "u" + std::to_string(k);
     };
+    // operands of which both sin and cos are live per-event values: node -> (sin node, cos node)
+    std::map<int, std::pair<int, int>> sincos_pair;
+    if (ar == Ar::DW) {
+      std::map<int, int> sin_of, cos_of;
+      for (size_t i = 0; i < ns.size(); i++) {
+        if (!live[i] || ns[i].uniform) continue;
+        if (ns[i].op == Op::Sin) sin_of[ns[i].a] = int(i);
+        if (ns[i].op == Op::Cos) cos_of[ns[i].a] = int(i);
+      }
+      for (auto& [a, si] : sin_of) {
+        auto c = cos_of.find(a);
+        if (c != cos_of.end()) sincos_pair[a] = {si, c->second};
+      }
+    }
     auto estmt = [&](int id) -> std::string {
       const Node& n = ns[id];
       if (ar == Ar::F32S && dnode[id])
@@ -895,6 +1035,17 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
         case Op::Neg: return lhs + "mf_dw_neg(" + A + ");";
         case Op::Rcp: return lhs + "mf_dw_rcp(" + A + ");";
         case Op::Log: return lhs + "mf_dw_log(" + A + ", mf_logtab);";
+        case Op::Sqrt: return lhs + "mf_dw_sqrt(" + A + ");";
+        case Op::Sin:
+        case Op::Cos: {
+          // sin and cos of the same operand share one reduction and both polynomials
+          auto it = sincos_pair.find(n.a);
+          if (it == sincos_pair.end()) return lhs + (n.op == Op::Sin ? "mf_dw_sin(" : "mf_dw_cos(") + A + ");";
+          const int first = std::min(it->second.first, it->second.second);
+          if (id != first) return "";  // defined with the first of the two
+          const std::string sn = "e" + std::to_string(it->second.first), cn = "e" + std::to_string(it->second.second);
+          return "mf_dw " + sn + ", " + cn + "; mf_dw_sincos(" + A + ", &" + sn + ", &" + cn + ");";
+        }
         case Op::Pow: return lhs + "mf_dw_from_double(pow(" + D(A) + ", " + D(B) + "));";
         case Op::Cmp: return lhs + "(" + D(A) + " " + cmp_str(n.cmp) + " " + D(B) + ");";
         case Op::Select: return lhs + "(" + A + " ? " + B + " : " + Cc + ");";
@@ -903,6 +1054,51 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
       }
       throw std::runtime_error("emit: unexpected node");
     };
+    if (kind == Kind::Store) {
+      // Event-only precompute in double-float: inputs split with rounding
+      // and outputs joined by integer operations (the FP64 pipe, 1/64 of the
+      // FP32 rate on GB300, is not used per event), parameter-only values
+      // evaluated in FP64 once per thread.
+      std::set<int> uni;
+      for (size_t i = 0; i < ns.size(); i++) {
+        if (!live[i] || ns[i].uniform || ns[i].op == Op::Input) continue;
+        for (int c : {ns[i].a, ns[i].b, ns[i].c})
+          if (c >= 0 && ns[c].uniform && ns[c].op != Op::Const) uni.insert(c);
+      }
+      for (int r : roots)
+        if (ns[r].uniform && ns[r].op != Op::Const) uni.insert(r);
+      s << "extern \"C\" __global__ void __launch_bounds__(MF_BLOCK) " << out.entry << "(const " << ST
+        << "* __restrict__ data, mf_u64 stride, mf_u64 n, mf_par P, " << ST
+        << "* __restrict__ outp, mf_u64 out_stride) {\n";
+      if (has_log)
+        s << "  __shared__ float4 mf_logtab[128];\n"
+          << "  for (int q = threadIdx.x; q < 128; q += MF_BLOCK) mf_logtab[q] = mf_dw_logtab_g[q];\n"
+          << "  __syncthreads();\n";
+      emit_params_and_uniform(s, "P.v");
+      for (int k : uni)
+        s << "  const mf_dw " << eref(k) << " = mf_dw_from_double(" << dref(k) << ");\n";
+      s << "  const mf_u64 step = (mf_u64)gridDim.x * MF_BLOCK;\n";
+      s << "  for (mf_u64 i = (mf_u64)blockIdx.x * MF_BLOCK + threadIdx.x; i < n; i += step) {\n";
+      for (int k : out.used_inputs)
+        s << "    const mf_dw x" << k << " = mf_dw_split_rn((double)data[(mf_u64)" << k << " * stride + i]);\n";
+      for (size_t i = 0; i < ns.size(); i++) {
+        if (!live[i] || ns[i].uniform || ns[i].op == Op::Input) continue;
+        s << "    " << estmt(int(i)) << "\n";
+      }
+      for (int j = 0; j < M; j++) {
+        const Node& r = ns[roots[j]];
+        if (r.op == Op::Input)  // a copied column stays bit-exact
+          s << "    outp[(mf_u64)" << j << " * out_stride + i] = data[(mf_u64)" << r.index << " * stride + i];\n";
+        else if (st32)  // h + l rounded once
+          s << "    { const mf_dw o = " << eref(roots[j]) << "; outp[(mf_u64)" << j
+            << " * out_stride + i] = __fadd_rn(o.h, o.l); }\n";
+        else
+          s << "    outp[(mf_u64)" << j << " * out_stride + i] = mf_dw_to_double_bits(" << eref(roots[j]) << ");\n";
+      }
+      s << "  }\n}\n";
+      out.source = s.str();
+      return out;
+    }
     // Uniform (parameter-only) values referenced by the per-event body or by an output.
     std::set<int> uni_used;
     auto note_uniform = [&](int k) {

@@ -555,12 +555,16 @@ static int events_copy(bool up, mf_buffer* b, int elem, void* host, uint32_t nco
   MF_CUDA_TRY(cudaSetDevice(b->ctx->device));
   if (up) {
     b->gen++;
-    if (n)
+    if (n && hs == ds)  // columns contiguous on both sides: one linear copy
+      MF_CUDA_TRY(cudaMemcpyAsync(b->ptr, host, uint64_t(ncols) * ds * es, cudaMemcpyHostToDevice, b->ctx->stream));
+    else if (n)
       MF_CUDA_TRY(cudaMemcpy2DAsync(b->ptr, ds * es, host, hs * es, n * es, ncols, cudaMemcpyHostToDevice,
                                     b->ctx->stream));
     if (ds > n)
       MF_CUDA_TRY(cudaMemset2DAsync(static_cast<char*>(b->ptr) + n * es, ds * es, 0, (ds - n) * es, ncols,
                                     b->ctx->stream));
+  } else if (n && hs == ds) {
+    MF_CUDA_TRY(cudaMemcpyAsync(host, b->ptr, uint64_t(ncols) * ds * es, cudaMemcpyDeviceToHost, b->ctx->stream));
   } else if (n) {
     MF_CUDA_TRY(cudaMemcpy2DAsync(host, hs * es, b->ptr, ds * es, n * es, ncols, cudaMemcpyDeviceToHost,
                                   b->ctx->stream));

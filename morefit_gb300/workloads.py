@@ -56,7 +56,8 @@ class Likelihood:
         # without them reads its raw observables, which keep FP64 storage with
         # FP32 arithmetic (MF_FLAG_F32_ARITH).
         mixed_raw = self.kernelT == np.float32 and not self.has_precompute
-        self.pre = CUDABlock(backend, np.float64 if mixed_raw else kernelT)
+        # The precompute runs in double-float (FP32 pipe) unless native FP64 is asked for.
+        self.pre = CUDABlock(backend, np.float64 if mixed_raw else kernelT, native_f64=native_f64)
         self.blocks = {}
         for name in ("lh_kernel", "lh_grad_kernel", "lh_hessian_kernel"):
             if name not in ks:

@@ -71,15 +71,56 @@ def test_fitter_level_values(backend, workload):
         np.testing.assert_allclose(h.ravel(), pt["hessian"], rtol=1e-8, atol=1e-9 * np.abs(pt["hessian"]).max())
 
 
-def test_precompute_matches_reference_text(backend):
+@pytest.mark.parametrize("native", [True, False])
+def test_precompute_matches_reference_text(backend, native):
+    """Hoisted columns against the reference's precompute text. Native FP64
+    within 1e-14; double-float (48-bit significands, inputs rounded to 48
+    bits) within 3e-14 relative or 5e-15 absolute (the columns are of order
+    0.1). Copied observables are bit-exact in both."""
     from morefit_gb300.workloads import Likelihood
     g = load_golden("pwave_n1000.json")
     ev = golden_events("pwave", 1000)
-    like = Likelihood(backend, g, np.float64)
+    like = Likelihood(backend, g, np.float64, native_f64=native)
     like.set_data(ev)
     got = like.pre.CopyFromOutputBuffer()
     ref = SpecKernel(kernel_spec(g, "precompute_kernel")).store(ev, [])
-    np.testing.assert_allclose(got, ref, rtol=1e-14, atol=1e-15)
+    assert np.array_equal(got[:3], ev)
+    if native:
+        np.testing.assert_allclose(got, ref, rtol=1e-14, atol=1e-15)
+    else:
+        np.testing.assert_allclose(got, ref, rtol=3e-14, atol=5e-15)
+
+
+def test_double_float_functions(backend):
+    """sqrt, sin, cos, log of double-float values (STORE kernel) against numpy
+    FP64. Inputs are rounded to 48 bits first (relative error up to 2^-48), so
+    the bars scale with the input where the function amplifies that: sin/cos
+    within 6e-15 * (1 + |x|) absolute, sqrt within 1e-14 relative, log within
+    2e-14 * (1 + |log y|) absolute (double-float additions round at about
+    2^-47 of the result)."""
+    from morefit_gb300.backend import CUDABlock
+    rng = np.random.default_rng(11)
+    n = 200000
+    x = np.concatenate([rng.uniform(-4, 4, n // 4), rng.uniform(-60, 60, n // 4), rng.uniform(-7000, 7000, n // 4),
+                        rng.normal(0, 1e-3, n // 4 - 6), [0.0, np.pi, -np.pi / 2, 5999.9, 6000.1, -1e-30]])
+    # magnitudes from 1e-25 up: double-float keeps 48 bits down to about 2^-100
+    y = np.concatenate([10.0 ** rng.uniform(-25, 30, n // 2), rng.uniform(0, 2, n // 2 - 3), [0.0, 1.0, 4.0]])
+    blk = CUDABlock(backend, np.float64)
+    blk.MakeComputeKernel("fn", n, ["x", "y"], ["s", "c", "q", "l"], [], ["sin(x)", "cos(x)", "sqrt(y)", "log(y)"],
+                          False)
+    blk.CopyToInputBuffer(np.stack([x, y]))
+    blk.SetNevents(n)
+    blk.SubmitKernel()
+    s, c, q, lg = blk.CopyFromOutputBuffer()
+    ax = 6e-15 * (1.0 + np.abs(x))
+    assert np.all(np.abs(s - np.sin(x)) <= ax)
+    assert np.all(np.abs(c - np.cos(x)) <= ax)
+    np.testing.assert_allclose(q, np.sqrt(y), rtol=1e-14, atol=0)
+    pos = y > 0
+    err = np.abs(lg[pos] - np.log(y[pos])) / (1.0 + np.abs(np.log(y[pos])))
+    w = int(np.argmax(err))
+    assert err[w] <= 2e-14, (y[pos][w], lg[pos][w], np.log(y[pos][w]), err[w])
+    assert lg[~pos][0] == -np.inf
 
 
 @pytest.mark.parametrize("workload,n", [("pwave", 1000000), ("mass", 100000)])
