@@ -120,6 +120,17 @@ int mf_events_download(const mf_buffer* buf, int elem_type, void* host, uint32_t
  * MF_F32 (used to stage FP64 host events into an FP32 device layout). */
 int mf_events_upload_f64_as(mf_buffer* buf, int elem_type, const double* host, uint32_t ncols, uint64_t n,
                             uint64_t host_stride, uint64_t dev_stride);
+/* Stream-ordered forms of mf_events_upload and mf_buffer_d2h: enqueued on the
+ * context's stream, they return at once. The host memory must stay valid and
+ * unchanged (upload) or unread (download) until mf_context_synchronize; page-
+ * locked host memory lets the copy overlap other work. With two contexts on
+ * one device, one context's copies overlap the other's kernels (pipelined
+ * evaluation of independent datasets). Split-phase form of the reference's
+ * CopyToInputBuffer / CopyFromKahanBuffer (include/compute.hh:130-138), whose
+ * OpenCL backend copies blocking (CL_TRUE, include/compute_opencl.hh:359,411). */
+int mf_events_upload_async(mf_buffer* buf, int elem_type, const void* host, uint32_t ncols, uint64_t n,
+                           uint64_t host_stride, uint64_t dev_stride);
+int mf_buffer_d2h_async(const mf_buffer* buf, uint64_t offset, void* dst, uint64_t nbytes);
 
 /* ---- kernels ----
  * Replaces ComputeBlock::MakeComputeKernel / MakeGenerateKernel
@@ -273,6 +284,10 @@ int mf_kernel_reduce_segments(mf_kernel* k, const mf_buffer* input, uint64_t str
  * blocks (include/fitter.hh:345-375,704-712). */
 int mf_kernel_store(mf_kernel* k, const mf_buffer* input, uint64_t in_stride, uint64_t n, const double* params,
                     uint32_t n_params, mf_buffer* output, uint64_t out_stride);
+/* mf_kernel_store enqueued on the context's stream without waiting
+ * (SubmitKernel without Finish). */
+int mf_kernel_store_async(mf_kernel* k, const mf_buffer* input, uint64_t in_stride, uint64_t n, const double* params,
+                          uint32_t n_params, mf_buffer* output, uint64_t out_stride);
 
 /* GENERATE: accept-reject generation with one xoshiro128++ stream per
  * generator thread, as the reference's accelerator generate kernel

@@ -271,6 +271,35 @@ class CUDABlock:
         self.nevents = self.input.n
         return True
 
+    def CopyToInputBufferAsync(self, events: np.ndarray) -> bool:
+        """Stream-ordered upload: `events` (contiguous, page-locked for overlap) must
+        stay valid and unchanged until Finish()."""
+        ev = events if events.ndim == 2 else events[None, :]
+        if not ev.flags.c_contiguous or ev.dtype != (np.float32 if self.elem == L.MF_F32 else np.float64):
+            raise ValueError("asynchronous upload needs a contiguous array of the block's element type")
+        ncols, n = ev.shape
+        self.input.ensure(ncols, n)
+        L.check(L.lib.mf_events_upload_async(self.input.buf, self.elem, ev.ctypes.data, ncols, n, n,
+                                             self.input.stride))
+        self.nevents = n
+        return True
+
+    def SubmitKernelAsync(self, out=None, out_index: int = 0) -> bool:
+        """SubmitKernel without waiting: STORE kernels write the output columns;
+        REDUCE kernels write their sums to row `out_index` of device buffer `out`."""
+        k = self.kernel
+        p = self.params if self.params.size else np.zeros(1)
+        if k.kind == L.MF_KERNEL_STORE:
+            self.output.ensure(k.nout, self.nevents)
+            L.check(L.lib.mf_kernel_store_async(k.handle, self.input.buf, self.input.stride, self.nevents,
+                                                L.dptr(p), k.nparams, self.output.buf, self.output.stride))
+        elif k.kind == L.MF_KERNEL_REDUCE:
+            L.check(L.lib.mf_kernel_reduce_async(k.handle, self.input.buf, self.input.stride, self.nevents,
+                                                 L.dptr(p), k.nparams, out, out_index))
+        else:
+            raise ValueError("generate kernels have no asynchronous form here")
+        return True
+
     def CopyToSeedBuffer(self, seeds: np.ndarray) -> bool:
         self._seeds = np.ascontiguousarray(seeds, dtype=np.uint32)
         return True

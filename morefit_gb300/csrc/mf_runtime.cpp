@@ -545,7 +545,7 @@ uint64_t mf_column_stride(uint64_t n) {
 }
 
 static int events_copy(bool up, mf_buffer* b, int elem, void* host, uint32_t ncols, uint64_t n, uint64_t hs,
-                       uint64_t ds) {
+                       uint64_t ds, bool sync = true) {
   if (!b || (!host && n && ncols)) return fail(MF_ERR_INVALID, "null argument");
   if (elem != MF_F64 && elem != MF_F32) return fail(MF_ERR_INVALID, "element type must be MF_F64 or MF_F32");
   const size_t es = elem_size(elem);
@@ -569,7 +569,7 @@ static int events_copy(bool up, mf_buffer* b, int elem, void* host, uint32_t nco
     MF_CUDA_TRY(cudaMemcpy2DAsync(host, hs * es, b->ptr, ds * es, n * es, ncols, cudaMemcpyDeviceToHost,
                                   b->ctx->stream));
   }
-  MF_CUDA_TRY(cudaStreamSynchronize(b->ctx->stream));
+  if (sync) MF_CUDA_TRY(cudaStreamSynchronize(b->ctx->stream));
   return MF_OK;
 }
 
@@ -580,6 +580,20 @@ int mf_events_upload(mf_buffer* b, int elem, const void* host, uint32_t ncols, u
 int mf_events_download(const mf_buffer* b, int elem, void* host, uint32_t ncols, uint64_t n, uint64_t hs,
                        uint64_t ds) {
   return events_copy(false, const_cast<mf_buffer*>(b), elem, host, ncols, n, hs, ds);
+}
+
+int mf_events_upload_async(mf_buffer* b, int elem, const void* host, uint32_t ncols, uint64_t n, uint64_t hs,
+                           uint64_t ds) {
+  return events_copy(true, b, elem, const_cast<void*>(host), ncols, n, hs, ds, false);
+}
+
+int mf_buffer_d2h_async(const mf_buffer* b, uint64_t off, void* dst, uint64_t nbytes) {
+  if (!b || (!dst && nbytes)) return fail(MF_ERR_INVALID, "null argument");
+  if (off + nbytes > b->size) return fail(MF_ERR_INVALID, "copy beyond the end of the buffer");
+  MF_CUDA_TRY(cudaSetDevice(b->ctx->device));
+  MF_CUDA_TRY(cudaMemcpyAsync(dst, static_cast<const char*>(b->ptr) + off, nbytes, cudaMemcpyDeviceToHost,
+                              b->ctx->stream));
+  return MF_OK;
 }
 
 int mf_events_upload_f64_as(mf_buffer* b, int elem, const double* host, uint32_t ncols, uint64_t n, uint64_t hs,
@@ -1035,8 +1049,8 @@ int mf_kernel_reduce_segments(mf_kernel* k, const mf_buffer* in, uint64_t stride
   return MF_OK;
 }
 
-int mf_kernel_store(mf_kernel* k, const mf_buffer* in, uint64_t in_stride, uint64_t n, const double* params,
-                    uint32_t n_params, mf_buffer* out, uint64_t out_stride) {
+static int kernel_store(mf_kernel* k, const mf_buffer* in, uint64_t in_stride, uint64_t n, const double* params,
+                        uint32_t n_params, mf_buffer* out, uint64_t out_stride, bool sync) {
   if (!k || !out) return fail(MF_ERR_INVALID, "null argument");
   if (k->kind != MF_KERNEL_STORE) return fail(MF_ERR_INVALID, "kernel is not a STORE kernel");
   if (n_params != k->n_params || (n_params && !params)) return fail(MF_ERR_INVALID, "parameter count mismatch");
@@ -1058,8 +1072,18 @@ int mf_kernel_store(mf_kernel* k, const mf_buffer* in, uint64_t in_stride, uint6
   void* args[] = {const_cast<void**>(&data), &in_stride, &n, pv.data(), &outp, &out_stride};
   MF_CUDA_TRY(cudaLaunchKernel(reinterpret_cast<const void*>(k->fn), dim3(grid), dim3(k->lowered.block), args, 0,
                                c->stream));
-  MF_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  if (sync) MF_CUDA_TRY(cudaStreamSynchronize(c->stream));
   return MF_OK;
+}
+
+int mf_kernel_store(mf_kernel* k, const mf_buffer* in, uint64_t in_stride, uint64_t n, const double* params,
+                    uint32_t n_params, mf_buffer* out, uint64_t out_stride) {
+  return kernel_store(k, in, in_stride, n, params, n_params, out, out_stride, true);
+}
+
+int mf_kernel_store_async(mf_kernel* k, const mf_buffer* in, uint64_t in_stride, uint64_t n, const double* params,
+                          uint32_t n_params, mf_buffer* out, uint64_t out_stride) {
+  return kernel_store(k, in, in_stride, n, params, n_params, out, out_stride, false);
 }
 
 int mf_kernel_generate(mf_kernel* k, const uint32_t* seeds, uint32_t nseeds, uint64_t n, uint64_t nper,

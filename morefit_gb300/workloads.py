@@ -90,6 +90,25 @@ class Likelihood:
         for b in self.blocks.values():
             b.SetNevents(self.nevents)
 
+    def set_data_async(self, events: np.ndarray) -> None:
+        """set_data without host waits: upload and precompute are enqueued on the
+        backend's stream; `events` (contiguous FP64, page-locked for overlap) must
+        stay valid until the backend is synchronized."""
+        ev = events if events.ndim == 2 else events[None, :]
+        self.pre.CopyToInputBufferAsync(ev)
+        self.nevents = ev.shape[1]
+        if self.has_precompute:
+            self.pre.SetNevents(self.nevents)
+            self.pre.SubmitKernelAsync()
+        for b in self.blocks.values():
+            b.SetNevents(self.nevents)
+
+    def sums_async(self, kernel: str, theta, out, out_index: int = 0) -> None:
+        """Enqueues one evaluation whose sums land in row `out_index` of device buffer `out`."""
+        b = self.blocks[kernel]
+        b.CopyToParameterBuffer(self.param_vector(kernel, theta))
+        b.SubmitKernelAsync(out, out_index)
+
     def set_device_data(self, cols: DeviceColumns) -> None:
         """Uses an event block already on the device (e.g. from generate_events)."""
         if cols.elem != self.pre.elem:
