@@ -308,6 +308,12 @@ int mf_kernel_generate(mf_kernel* k, const uint32_t* seeds, uint32_t nseeds, uin
  * names a variable not in `names` is an MF_ERR_PARSE error. */
 int mf_eval_expressions(uint32_t n_names, const char* const* names, const double* values, uint32_t n_exprs,
                         const char* const* exprs, double* out);
+/* mf_eval_expressions for n_rows parameter vectors at once (values row-major
+ * [n_rows][n_names], out [n_rows][n_exprs]); the expressions are parsed once.
+ * The per-toy form of the same fitter step for batched toy fits
+ * (include/toystudy.hh:55-82 runs one fitter per toy). */
+int mf_eval_expressions_batch(uint32_t n_names, const char* const* names, uint32_t n_rows, const double* values,
+                              uint32_t n_exprs, const char* const* exprs, double* out);
 
 /* Seed rows for the accelerator generator (include/generator.hh:115-135):
  * an xoshiro128++ state seeded like Xoshiro128pp::setSeed(seed)

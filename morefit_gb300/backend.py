@@ -214,6 +214,16 @@ def eval_expressions(names: Sequence[str], values: Sequence[float], exprs: Seque
     return out[: len(exprs)]
 
 
+def eval_expressions_batch(names: Sequence[str], rows: np.ndarray, exprs: Sequence[str]) -> np.ndarray:
+    """eval_expressions for every row of ``rows`` (shape (n_rows, len(names)))."""
+    v = np.ascontiguousarray(rows, dtype=np.float64).reshape(-1, len(names))
+    out = np.zeros((v.shape[0], max(1, len(exprs))))
+    L.check(L.lib.mf_eval_expressions_batch(len(names), C.cast(L.cstrings(list(names)), L.c_char_pp), v.shape[0],
+                                            L.dptr(v), len(exprs), C.cast(L.cstrings(list(exprs)), L.c_char_pp),
+                                            L.dptr(out)))
+    return out[:, : len(exprs)]
+
+
 class CUDABlock:
     """ComputeBlock<kernelT, evalT> over the CUDA C ABI (compute.hh:110-149).
 

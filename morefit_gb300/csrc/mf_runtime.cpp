@@ -338,8 +338,11 @@ uint64_t prep_key(const mf_kernel* k) {
 
 // The device columns kernel `k` reads for input buffer `in`: the buffer
 // itself, or its prepared copy, (re)made on the context's stream when the
-// buffer was written since (or n / stride changed).
-int prepare_input(const mf_kernel* k, const mf_buffer* in, uint64_t stride, uint64_t n, const void** data) {
+// buffer was written since (or the column stride changed). The copy covers
+// all `stride` rows of the columns, so evaluations of any event count or
+// segment of the buffer share it (event loops never accumulate rows at or
+// beyond their n).
+int prepare_input(const mf_kernel* k, const mf_buffer* in, uint64_t stride, const void** data) {
   if (!k->lowered.prep) {
     *data = in->ptr;
     return MF_OK;
@@ -348,7 +351,7 @@ int prepare_input(const mf_kernel* k, const mf_buffer* in, uint64_t stride, uint
   mf_derived* d = nullptr;
   for (auto& x : in->derived)
     if (x.key == k->prep_key) d = &x;
-  if (d && d->gen == in->gen && d->n == n && d->stride == stride) {
+  if (d && d->gen == in->gen && d->stride == stride) {
     *data = d->ptr;
     return MF_OK;
   }
@@ -379,10 +382,11 @@ int prepare_input(const mf_kernel* k, const mf_buffer* in, uint64_t stride, uint
   const int grid = int(std::max<uint64_t>(1, std::min<uint64_t>(blocks, uint64_t(c->num_sms) * 16)));
   const void* src = in->ptr;
   void* dst = d->ptr;
-  void* args[] = {const_cast<void**>(&src), &stride, &n, &dst};
+  uint64_t rows = stride;
+  void* args[] = {const_cast<void**>(&src), &stride, &rows, &dst};
   MF_CUDA_TRY(cudaLaunchKernel(reinterpret_cast<const void*>(k->fn_prep), dim3(grid), dim3(256), args, 0, c->stream));
   d->gen = in->gen;
-  d->n = n;
+  d->n = stride;
   d->stride = stride;
   *data = d->ptr;
   return MF_OK;
@@ -716,6 +720,27 @@ int mf_eval_expressions(uint32_t n_names, const char* const* names, const double
   return MF_OK;
 }
 
+int mf_eval_expressions_batch(uint32_t n_names, const char* const* names, uint32_t n_rows, const double* values,
+                              uint32_t n_exprs, const char* const* exprs, double* out) {
+  if ((n_names && !names) || (n_rows && n_names && !values) || (n_exprs && (!exprs || (n_rows && !out))))
+    return fail(MF_ERR_INVALID, "null argument");
+  std::vector<std::string> nm;
+  for (uint32_t i = 0; i < n_names; i++) nm.push_back(names[i] ? names[i] : "");
+  try {
+    mf::Dag dag({}, nm);
+    std::vector<int> roots;
+    for (uint32_t i = 0; i < n_exprs; i++) roots.push_back(dag.parse(exprs[i] ? exprs[i] : ""));
+    std::vector<double> row(n_names);
+    for (uint32_t r = 0; r < n_rows; r++) {
+      std::copy(values + size_t(r) * n_names, values + size_t(r + 1) * n_names, row.begin());
+      for (uint32_t i = 0; i < n_exprs; i++) out[size_t(r) * n_exprs + i] = dag.eval(roots[i], {}, row);
+    }
+  } catch (const std::exception& e) {
+    return fail(MF_ERR_PARSE, e.what());
+  }
+  return MF_OK;
+}
+
 int mf_seed_rows(uint64_t seed, uint32_t nrows, uint32_t* out) {
   if (!out && nrows) return fail(MF_ERR_INVALID, "null argument");
   // Splitmix64 seeding of four 32-bit words (upper halves), then xoshiro128++
@@ -893,7 +918,7 @@ int mf_kernel_reduce(mf_kernel* k, const mf_buffer* in, uint64_t stride, uint64_
   if (rc) return rc;
   *c->status_host = 0u;
   const void* data = nullptr;
-  rc = prepare_input(k, in, stride, n, &data);
+  rc = prepare_input(k, in, stride, &data);
   if (rc) return rc;
   rc = mfi::launch_reduce(k, data, stride, n, params, c->partials, c->counter, c->out_dev, c->stream, 0);
   if (rc) return rc;
@@ -919,7 +944,7 @@ int mf_kernel_reduce_async(mf_kernel* k, const mf_buffer* in, uint64_t stride, u
   if (rc) return rc;
   double* dst = static_cast<double*>(out->ptr) + out_index * k->n_outputs;
   const void* data = nullptr;
-  rc = prepare_input(k, in, stride, n, &data);
+  rc = prepare_input(k, in, stride, &data);
   if (rc) return rc;
   return mfi::launch_reduce(k, data, stride, n, params, c->partials, c->counter, dst, c->stream, 0);
 }
@@ -944,24 +969,24 @@ int mf_kernel_reduce_many(mf_kernel* k, uint32_t count, const mf_buffer* const* 
   if (rc) return rc;
   // Prepared inputs first, then the evaluations back to back: each after the
   // first may overlap its predecessor's tail (it reads only its own input).
-  // A buffer that appears with two different layouts in one batch would have
-  // its prepared copy remade between uses: prepare and launch one by one.
+  // A buffer that appears with two column strides in one batch would have its
+  // prepared copy remade between uses: prepare and launch one by one.
   bool one_by_one = false;
   if (k->lowered.prep) {
-    std::map<const mf_buffer*, std::pair<uint64_t, uint64_t>> layout;
+    std::map<const mf_buffer*, uint64_t> layout;
     for (uint32_t i = 0; i < count && !one_by_one; i++) {
-      auto [it, fresh] = layout.emplace(inputs[i], std::make_pair(ns[i], strides[i]));
-      one_by_one = !fresh && it->second != std::make_pair(ns[i], strides[i]);
+      auto [it, fresh] = layout.emplace(inputs[i], strides[i]);
+      one_by_one = !fresh && it->second != strides[i];
     }
   }
   std::vector<const void*> data(count, nullptr);
   for (uint32_t i = 0; i < count && !one_by_one; i++) {
-    rc = prepare_input(k, inputs[i], strides[i], ns[i], &data[i]);
+    rc = prepare_input(k, inputs[i], strides[i], &data[i]);
     if (rc) return rc;
   }
   for (uint32_t i = 0; i < count; i++) {
     if (one_by_one) {
-      rc = prepare_input(k, inputs[i], strides[i], ns[i], &data[i]);
+      rc = prepare_input(k, inputs[i], strides[i], &data[i]);
       if (rc) return rc;
     }
     double* dst = static_cast<double*>(out->ptr) + uint64_t(i) * k->n_outputs;
@@ -1039,7 +1064,7 @@ int mf_kernel_reduce_segments(mf_kernel* k, const mf_buffer* in, uint64_t stride
   const void* d_par = base + bytes_begin + bytes_count;
   double* outp = c->out_dev;
   const void* data = nullptr;
-  rc = prepare_input(k, in, stride, end, &data);
+  rc = prepare_input(k, in, stride, &data);
   if (rc) return rc;
   void* args[] = {const_cast<void**>(&data), &stride, &d_begin, &d_count, const_cast<void**>(&d_par), &outp};
   MF_CUDA_TRY(cudaLaunchKernel(reinterpret_cast<const void*>(k->fn_seg), dim3(nseg), dim3(k->lowered.block), args, 0,
