@@ -294,6 +294,7 @@ def ours(args):
         ms32, res32 = timed_device(sets32, args.steps, args.warmup)
         mixed = {"value": world * args.steps / (ms32 / 1e3), "unit": "evals/s", "dtype": "f32 storage+arith, f64 sums",
                  "speedup_vs_f64": ms64 / ms32,
+                 "speedup_vs_native_f64": (msn / max(50, args.steps // 10)) / (ms32 / args.steps) if native else None,
                  "roofline": {"bound": "hbm", "achieved": bytes32 / (ms32 / 1e3 / args.steps) / 1e9,
                               "peak": hbm_peak, "unit": "GB/s",
                               "frac": bytes32 / (ms32 / 1e3 / args.steps) / 1e9 / hbm_peak},
@@ -430,12 +431,18 @@ def ours(args):
 
 
 VARIANTS = {
-    # name: (kernelT, native_f64, vec, block, bulk-copy pipeline, stages); 0 = library default
+    # name: (kernelT, native_f64, vec, block, bulk-copy pipeline, stages or unroll); 0 = library default
     "f64_native": (np.float64, True, 2, 256, False, 0),
     "f64_dw": (np.float64, False, 0, 0, False, 0),
     "f64_dw_b256": (np.float64, False, 1, 256, False, 0),
     "f64_dw_pipe": (np.float64, False, 1, 256, True, 4),
     "f64_dw_v2": (np.float64, False, 2, 256, False, 0),
+    "f64_dw_u2": (np.float64, False, 2, 256, False, 2),
+    "f64_dw_v1_u2": (np.float64, False, 1, 256, False, 2),
+    "f32_u2": (np.float32, False, 4, 256, False, 2),
+    "f32_v2_u2": (np.float32, False, 2, 256, False, 2),
+    "f32_b512": (np.float32, False, 4, 512, False, 0),
+    "f32_v2_b512_u2": (np.float32, False, 2, 512, False, 2),
     "f64_dw_v2_b512": (np.float64, False, 2, 512, False, 0),
     "f32": (np.float32, False, 0, 0, False, 0),
     "f32_v2": (np.float32, False, 2, 256, False, 0),

@@ -552,6 +552,23 @@ __device__ __forceinline__ mf_dw mf_dw_split(double x) {
   return mf_dw_make(__uint_as_float(hb), __uint_as_float(__float_as_uint(l) | sign));
 }
 __device__ __forceinline__ mf_dw mf_dw_pair(float2 t) { return mf_dw_make(t.x, t.y); }
+// Lazy double-float accumulation (per-thread partials, dot products): TwoSum
+// of the high words, the low words and the rounding error added in FP32;
+// mf_dw_renorm restores a normalized pair (|l| <= ulp(h)/2) at the end.
+__device__ __forceinline__ void mf_dw_acc(mf_dw& a, mf_dw x) {
+  const mf_dw s = mf_two_sum(a.h, x.h);
+  a.h = s.h;
+  a.l = __fadd_rn(a.l, __fadd_rn(s.l, x.l));
+}
+// a += x * y (the product's error terms formed with FMA, as in mf_dw_mul)
+__device__ __forceinline__ void mf_dw_acc_mul(mf_dw& a, mf_dw x, mf_dw y) {
+  const float p = __fmul_rn(x.h, y.h);
+  const float e = __fmaf_rn(x.h, y.l, __fmaf_rn(x.l, y.h, __fmaf_rn(x.h, y.h, -p)));
+  const mf_dw s = mf_two_sum(a.h, p);
+  a.h = s.h;
+  a.l = __fadd_rn(a.l, __fadd_rn(s.l, e));
+}
+__device__ __forceinline__ mf_dw mf_dw_renorm(mf_dw a) { return mf_two_sum(a.h, a.l); }
 // Round-to-nearest split with integer operations only: h = x rounded to 24
 // bits, l = x - h rounded to 24 bits, |x - h - l| <= 2^-48 |x| for |x| from
 // 2^-100 to 2^127 (below 2^-100 l loses bits to the FP32 exponent range).
@@ -863,7 +880,11 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
     }
     if (vec_req == 1 || vec_req == 2 || (vec_req == 4 && st32)) out.vec = vec_req;
     if (block_req >= 64 && block_req <= 1024 && block_req % 32 == 0) out.block = block_req;
-    out.stages = stages_req >= 2 && stages_req <= 8 ? stages_req : (dw_default ? 3 : 4);
+    // bulk-copy pipeline: shared-memory stages; direct loads: loop unroll factor (1 = none)
+    if (out.pipelined)
+      out.stages = stages_req >= 2 && stages_req <= 8 ? stages_req : (dw_default ? 3 : 4);
+    else
+      out.stages = stages_req >= 1 && stages_req <= 4 ? stages_req : 1;
     out.tile = out.block * out.vec;
   }
   const int V = out.vec;
@@ -1001,6 +1022,71 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
         if (c != cos_of.end()) sincos_pair[a] = {si, c->second};
       }
     }
+    // Double-float REDUCE bodies: sums of (value x parameter-only factor)
+    // terms become compensated dot products, and an output that is a product
+    // used nowhere else is multiplied straight into its accumulator.
+    std::vector<int> uses(ns.size(), 0), consumer(ns.size(), -1);
+    std::vector<char> skip(ns.size(), 0);
+    std::map<int, std::vector<std::pair<int, int>>> chains;  // chain root -> its terms (a, b)
+    std::vector<std::pair<int, int>> fused(roots.size(), {-1, -1});
+    if (ar == Ar::DW && kind == Kind::Reduce) {
+      for (size_t i = 0; i < ns.size(); i++) {
+        if (!live[i] || ns[i].uniform || ns[i].op == Op::Input) continue;
+        for (int c : {ns[i].a, ns[i].b, ns[i].c})
+          if (c >= 0) {
+            uses[c]++;
+            consumer[c] = int(i);
+          }
+      }
+      for (int r : roots) {
+        uses[r]++;
+        consumer[r] = -1;
+      }
+      auto is_term = [&](int k) {
+        const Node& n = ns[k];
+        return n.op == Op::Mul && !n.uniform && uses[k] == 1 && (ns[n.a].uniform || ns[n.b].uniform);
+      };
+      std::vector<char> chain(ns.size(), 0);
+      for (size_t i = 0; i < ns.size(); i++) {
+        const Node& n = ns[i];
+        if (!live[i] || n.uniform || n.op != Op::Add) continue;
+        auto part = [&](int c) { return is_term(c) || (chain[c] && uses[c] == 1); };
+        if (part(n.a) && part(n.b)) chain[i] = 1;
+      }
+      std::function<void(int, std::vector<std::pair<int, int>>&)> collect = [&](int k, auto& terms) {
+        if (chain[k]) {
+          collect(ns[k].a, terms);
+          collect(ns[k].b, terms);
+        } else {
+          terms.push_back({ns[k].a, ns[k].b});
+        }
+      };
+      for (size_t i = 0; i < ns.size(); i++) {
+        if (!chain[i]) continue;
+        const bool absorbed = uses[i] == 1 && consumer[i] >= 0 && chain[consumer[i]];
+        if (absorbed) continue;
+        std::vector<std::pair<int, int>> terms;
+        collect(int(i), terms);
+        chains[int(i)] = terms;
+        // every node of the chain below its root is folded into the root's statement
+        std::function<void(int)> mark = [&](int k) {
+          if (k != int(i)) skip[k] = 1;
+          if (chain[k]) {
+            mark(ns[k].a);
+            mark(ns[k].b);
+          }
+        };
+        mark(int(i));
+      }
+      for (size_t j = 0; j < roots.size(); j++) {
+        const int r = roots[j];
+        const Node& n = ns[r];
+        if (n.op == Op::Mul && !n.uniform && uses[r] == 1 && !chains.count(r) && !skip[r]) {
+          fused[j] = {n.a, n.b};
+          skip[r] = 1;
+        }
+      }
+    }
     auto estmt = [&](int id) -> std::string {
       const Node& n = ns[id];
       if (ar == Ar::F32S && dnode[id])
@@ -1027,6 +1113,13 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
         throw std::runtime_error("emit: unexpected node");
       }
       auto D = [](const std::string& v) { return "mf_dw_to_double(" + v + ")"; };
+      if (skip[id]) return "";
+      auto ch = chains.find(id);
+      if (ch != chains.end()) {
+        std::string c = "mf_dw e" + std::to_string(id) + "; { mf_dw t_ = mf_dw_make(0.0f, 0.0f);";
+        for (auto& [ta, tb] : ch->second) c += " mf_dw_acc_mul(t_, " + eref(ta) + ", " + eref(tb) + ");";
+        return c + " e" + std::to_string(id) + " = mf_dw_renorm(t_); }";
+      }
       switch (n.op) {
         case Op::Add: return lhs + "mf_dw_add(" + A + ", " + B + ");";
         case Op::Sub: return lhs + "mf_dw_sub(" + A + ", " + B + ");";
@@ -1083,7 +1176,8 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
         s << "    const mf_dw x" << k << " = mf_dw_split_rn((double)data[(mf_u64)" << k << " * stride + i]);\n";
       for (size_t i = 0; i < ns.size(); i++) {
         if (!live[i] || ns[i].uniform || ns[i].op == Op::Input) continue;
-        s << "    " << estmt(int(i)) << "\n";
+        const std::string st = estmt(int(i));
+        if (!st.empty()) s << "    " << st << "\n";
       }
       for (int j = 0; j < M; j++) {
         const Node& r = ns[roots[j]];
@@ -1165,7 +1259,8 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
     auto body = [&](std::ostringstream& o, const std::string& ind) {
       for (size_t i = 0; i < ns.size(); i++) {
         if (!live[i] || ns[i].uniform || ns[i].op == Op::Input) continue;
-        o << ind << estmt(int(i)) << "\n";
+        const std::string st = estmt(int(i));
+        if (!st.empty()) o << ind << st << "\n";
       }
     };
     // Accumulation of output j from the body's value (per thread).
@@ -1184,8 +1279,11 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
           o << ind << "mf_kahan_f32(acc[" << j << "], cmp[" << j << "], " << r << ");\n";
         else if (ar == Ar::F64)
           o << ind << "acc[" << j << "] += " << r << ";\n";
+        else if (fused[j].first >= 0)
+          o << ind << "mf_dw_acc_mul(acc[" << j << "], " << eref(fused[j].first) << ", " << eref(fused[j].second)
+            << ");\n";
         else
-          o << ind << "acc[" << j << "] = mf_dw_add(acc[" << j << "], " << r << ");\n";
+          o << ind << "mf_dw_acc(acc[" << j << "], " << r << ");\n";
       }
     };
     // Per-thread accumulator of output j as a double-float value, summed over
@@ -1196,7 +1294,7 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
       else if (ar == Ar::F64)
         o << "    mf_dw a = mf_dw_split(acc[j]);\n";
       else
-        o << "    mf_dw a = acc[j];\n";
+        o << "    mf_dw a = mf_dw_renorm(acc[j]);\n";
       o << "#pragma unroll\n    for (int o = 16; o > 0; o >>= 1) a = mf_dw_add(a, mf_dw_shfl_xor(a, o));\n";
     };
     auto load_table = [&](std::ostringstream& o) {
@@ -1301,6 +1399,8 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
         << "  }\n";
     } else {
       s << "  const mf_u64 step = (mf_u64)gridDim.x * MF_BLOCK * " << V << ";\n";
+      // unrolled: the next iteration's loads are issued before this one's arithmetic
+      if (out.stages > 1) s << "#pragma unroll " << out.stages << "\n";
       s << "  for (mf_u64 base = ((mf_u64)blockIdx.x * MF_BLOCK + threadIdx.x) * " << V
         << "; base < n; base += step) {\n";
       emit_events("    ", "base", "base", [&](int k) {
