@@ -165,8 +165,16 @@ typedef struct mf_kernel_desc {
    * per block (64..1024, multiple of 32). */
   uint32_t vec;
   uint32_t block;
-  /* Shared-memory stages of the REDUCE input pipeline (0 = default, 2..8). */
+  /* Shared-memory stages of the REDUCE input pipeline (0 = default, 2..8);
+   * with direct loads, the unroll factor of the event loop (1..4). */
   uint32_t stages;
+  /* Optional (NULL = none): for each of the n_params parameters, NULL or the
+   * parameter-only expression that defines it in terms of the others, e.g.
+   * the fitter's hoisted "morefit_parambuffer_k = (1-FS)*Fl"
+   * (include/fitter.hh:381-396). Used only to find which input columns
+   * always enter together when the lowering folds them; the parameter
+   * vector passed at launch stays authoritative. */
+  const char* const* param_defs;
 } mf_kernel_desc;
 
 /* FP64 REDUCE kernels evaluate the per-event expressions in double-float

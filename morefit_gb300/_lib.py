@@ -73,6 +73,7 @@ class KernelDesc(C.Structure):
         ("vec", C.c_uint32),
         ("block", C.c_uint32),
         ("stages", C.c_uint32),
+        ("param_defs", c_char_pp),
     ]
 
 

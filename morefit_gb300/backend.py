@@ -144,7 +144,7 @@ class Kernel:
 
 def make_desc(name: str, kind: int, elem: int, inputs: Sequence[str], params: Sequence[str],
               exprs: Sequence[str], gen=None, native_f64: bool = False, vec: int = 0, block: int = 0,
-              f32_arith: bool = False, pipeline: bool = False, stages: int = 0):
+              f32_arith: bool = False, pipeline: bool = False, stages: int = 0, param_defs=None):
     keep = {"inputs": L.cstrings(list(inputs)), "params": L.cstrings(list(params)),
             "exprs": L.cstrings(list(exprs)), "name": name.encode()}
     d = L.KernelDesc()
@@ -162,6 +162,9 @@ def make_desc(name: str, kind: int, elem: int, inputs: Sequence[str], params: Se
     d.vec = vec
     d.block = block
     d.stages = stages
+    if param_defs is not None:
+        keep["defs"] = (C.c_char_p * len(params))(*[(x or "").encode() if x else None for x in param_defs])
+        d.param_defs = C.cast(keep["defs"], L.c_char_pp)
     if gen is not None:
         dims, lo, hi, maxprob = gen
         keep["gd"] = L.cstrings(list(dims))
@@ -177,8 +180,9 @@ def make_desc(name: str, kind: int, elem: int, inputs: Sequence[str], params: Se
 
 def build_kernel(backend: CUDABackend, name: str, kind: int, elem: int, inputs, params, exprs, gen=None,
                  native_f64: bool = False, vec: int = 0, block: int = 0, f32_arith: bool = False,
-                 pipeline: bool = False, stages: int = 0) -> Kernel:
-    d, keep = make_desc(name, kind, elem, inputs, params, exprs, gen, native_f64, vec, block, f32_arith, pipeline, stages)
+                 pipeline: bool = False, stages: int = 0, param_defs=None) -> Kernel:
+    d, keep = make_desc(name, kind, elem, inputs, params, exprs, gen, native_f64, vec, block, f32_arith, pipeline, stages,
+                        param_defs)
     h = L.c_ker()
     L.check(L.lib.mf_kernel_build(backend.handle, C.byref(d), C.byref(h)))
     del keep
@@ -186,9 +190,11 @@ def build_kernel(backend: CUDABackend, name: str, kind: int, elem: int, inputs, 
 
 
 def lower_source(name: str, kind: int, elem: int, inputs, params, exprs, gen=None, native_f64: bool = False,
-                 vec: int = 0, block: int = 0, f32_arith: bool = False, pipeline: bool = False, stages: int = 0) -> str:
+                 vec: int = 0, block: int = 0, f32_arith: bool = False, pipeline: bool = False, stages: int = 0,
+                 param_defs=None) -> str:
     """CUDA C the library generates for these expressions (no GPU needed)."""
-    d, keep = make_desc(name, kind, elem, inputs, params, exprs, gen, native_f64, vec, block, f32_arith, pipeline, stages)
+    d, keep = make_desc(name, kind, elem, inputs, params, exprs, gen, native_f64, vec, block, f32_arith, pipeline, stages,
+                        param_defs)
     need = C.c_size_t()
     L.check(L.lib.mf_lower_source(C.byref(d), None, 0, C.byref(need)))
     buf = C.create_string_buffer(need.value)
@@ -197,9 +203,11 @@ def lower_source(name: str, kind: int, elem: int, inputs, params, exprs, gen=Non
 
 
 def compile_check(name: str, kind: int, elem: int, inputs, params, exprs, gen=None, native_f64: bool = False,
-                  vec: int = 0, block: int = 0, f32_arith: bool = False, pipeline: bool = False, stages: int = 0) -> dict:
+                  vec: int = 0, block: int = 0, f32_arith: bool = False, pipeline: bool = False, stages: int = 0,
+                  param_defs=None) -> dict:
     """NVRTC-compiles the lowered kernel for sm_103a without a GPU."""
-    d, keep = make_desc(name, kind, elem, inputs, params, exprs, gen, native_f64, vec, block, f32_arith, pipeline, stages)
+    d, keep = make_desc(name, kind, elem, inputs, params, exprs, gen, native_f64, vec, block, f32_arith, pipeline, stages,
+                        param_defs)
     r, s = C.c_int(), C.c_int()
     L.check(L.lib.mf_compile_check(C.byref(d), C.byref(r), C.byref(s)))
     return {"registers": r.value, "spill_bytes": s.value}
@@ -327,7 +335,9 @@ class CUDABlock:
     # --- kernels (compute.hh:140-148) ---
     def MakeComputeKernel(self, name: str, nevents: int, input_signature: Sequence[str],
                           output_signature: Sequence[str], params: Sequence[str], graphs: Sequence[str],
-                          kahan_summation: bool = False) -> bool:
+                          kahan_summation: bool = False, param_defs=None) -> bool:
+        """``param_defs``: optional, per parameter "" or its defining expression
+        (the fitter's hoisted parameter buffers); helps the lowering fold columns."""
         if len(output_signature) != len(graphs):
             raise ValueError("output_signature and graphs differ in length (compute_opencl.hh:707)")
         self.kahan = bool(kahan_summation)
@@ -336,7 +346,7 @@ class CUDABlock:
         self.kernel = build_kernel(self.backend, name, kind, self.elem, input_signature, params, graphs,
                                    native_f64=self.native_f64, vec=self.shape[0], block=self.shape[1],
                                    f32_arith=self.f32_arith and kind == L.MF_KERNEL_REDUCE, pipeline=self.pipeline,
-                                   stages=self.shape[2])
+                                   stages=self.shape[2], param_defs=param_defs)
         self._sums = np.zeros(self.nout)
         self.nevents = int(nevents)
         return True

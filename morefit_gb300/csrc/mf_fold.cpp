@@ -106,8 +106,8 @@ double snap(double v) {
 // dependents, and M[d][m] with coef_d = sum_m M[d][m] coef_{pivot m}.
 // False when there are none or anything is doubtful.
 bool find_relations(const Dag& d2, const std::vector<Affine>& aff, const std::vector<int>& lroots,
-                    const std::map<int, int>& colpos, size_t np, std::vector<int>& pivots,
-                    std::vector<int>& dependents, std::vector<std::vector<double>>& M) {
+                    const std::map<int, int>& colpos, size_t np, const std::vector<std::string>& param_defs,
+                    std::vector<int>& pivots, std::vector<int>& dependents, std::vector<std::vector<double>>& M) {
   const int J = int(colpos.size());
   {
     const auto& n2 = d2.nodes();
@@ -116,10 +116,23 @@ bool find_relations(const Dag& d2, const std::vector<Affine>& aff, const std::ve
       for (auto& [col, c] : aff[r].coef)
         if (has_conditional(n2, c, seen)) return false;
   }
+  // Parameters defined by expressions of the others take their defined value
+  // in every sample (definitions in parameter order; a definition may use
+  // parameters defined before it).
+  Dag defs({}, d2.param_names());
+  std::vector<std::pair<int, int>> def_roots;  // (parameter index, root)
+  for (size_t i = 0; i < param_defs.size() && i < np; i++)
+    if (!param_defs[i].empty()) def_roots.push_back({int(i), defs.parse(param_defs[i])});
+  auto sample_set = [&](size_t count, uint64_t seed) {
+    auto S = samples(count, np, seed);
+    for (auto& pv : S)
+      for (auto& [i, r] : def_roots) pv[i] = defs.eval(r, {}, pv);
+    return S;
+  };
   // Sample matrix: one row per (sample, linear root), one column per source column.
   auto matrix = [&](uint64_t seed, size_t count, std::vector<std::vector<double>>& Z) {
     Z.assign(J, {});
-    for (const auto& pv : samples(count, np, seed))
+    for (const auto& pv : sample_set(count, seed))
       for (int r : lroots) {
         std::vector<double> row(J, 0.0);
         for (auto& [col, c] : aff[r].coef) {
@@ -202,7 +215,7 @@ bool find_relations(const Dag& d2, const std::vector<Affine>& aff, const std::ve
 
 }  // namespace
 
-FoldResult fold_columns(const Dag& dag, const std::vector<int>& roots) {
+FoldResult fold_columns(const Dag& dag, const std::vector<int>& roots, const std::vector<std::string>& param_defs) {
   FoldResult res;
   const auto& ns = dag.nodes();
   const size_t N = ns.size();
@@ -318,7 +331,8 @@ FoldResult fold_columns(const Dag& dag, const std::vector<int>& roots) {
   for (auto& [col, pos] : colpos) src_of[pos] = col;
   std::vector<int> pivots, dependents;
   std::vector<std::vector<double>> M(J);  // M[d][m]: dependent column d on pivot m
-  if (J >= 2 && find_relations(d2, aff, lroots, colpos, dag.param_names().size(), pivots, dependents, M)) {
+  if (J >= 2 &&
+      find_relations(d2, aff, lroots, colpos, dag.param_names().size(), param_defs, pivots, dependents, M)) {
     res.folded = true;
   } else {
     pivots.clear();

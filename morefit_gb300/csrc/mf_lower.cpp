@@ -817,7 +817,7 @@ OpCount count_ops(const std::vector<std::string>& inputs, const std::vector<std:
 LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::vector<std::string>& inputs,
                     const std::vector<std::string>& params, const std::vector<std::string>& exprs,
                     const GenerateSpec* gen, bool native_f64, int vec_req, int block_req, bool f32_arith,
-                    bool direct_loads, int stages_req) {
+                    bool direct_loads, int stages_req, const std::vector<std::string>& param_defs) {
   std::vector<std::string> in_names = inputs;
   if (kind == Kind::Generate) {
     if (!gen) throw std::runtime_error("generate kernel without generate spec");
@@ -843,7 +843,7 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
   FoldResult fold;
   int prep = LoweredKernel::PrepNone;
   if (kind == Kind::Reduce && !f32_arith) {
-    fold = fold_columns(dag, roots0);
+    fold = fold_columns(dag, roots0, param_defs);
     const bool dw = !st32 && !native_f64;
     if (fold.rewritten && (dw || fold.folded))
       prep = dw ? LoweredKernel::PrepPair : st32 ? LoweredKernel::PrepF32 : LoweredKernel::PrepF64;

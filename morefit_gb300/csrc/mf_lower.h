@@ -115,7 +115,10 @@ struct FoldResult {
   std::vector<int> roots;
   int rank = 0, source_columns = 0;
 };
-FoldResult fold_columns(const Dag& dag, const std::vector<int>& roots);
+// param_defs: per parameter, "" or a parameter-only expression defining it
+// from the others (sampled values of defined parameters follow their definition).
+FoldResult fold_columns(const Dag& dag, const std::vector<int>& roots,
+                        const std::vector<std::string>& param_defs = {});
 
 enum class Elem { F64, F32 };
 enum class Kind { Reduce, Store, Generate };
@@ -130,7 +133,8 @@ struct GenerateSpec {
 LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::vector<std::string>& inputs,
                     const std::vector<std::string>& params, const std::vector<std::string>& exprs,
                     const GenerateSpec* gen = nullptr, bool native_f64 = false, int vec = 0, int block = 0,
-                    bool f32_arith = false, bool direct_loads = false, int stages = 0);
+                    bool f32_arith = false, bool direct_loads = false, int stages = 0,
+                    const std::vector<std::string>& param_defs = {});
 
 // Counts per-event operations of a lowered expression set (diagnostics).
 struct OpCount {

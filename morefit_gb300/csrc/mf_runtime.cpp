@@ -676,6 +676,9 @@ static int lower_desc(const mf_kernel_desc* d, mf::LoweredKernel& lk) {
     gs.hi.assign(d->gen_hi, d->gen_hi + d->n_gen_dims);
     gs.maxprob = d->maxprob;
   }
+  std::vector<std::string> defs;
+  if (d->param_defs)
+    for (uint32_t i = 0; i < d->n_params; i++) defs.push_back(d->param_defs[i] ? d->param_defs[i] : "");
   try {
     lk = mf::lower(d->name ? d->name : "kernel",
                    d->kind == MF_KERNEL_REDUCE  ? mf::Kind::Reduce
@@ -685,7 +688,7 @@ static int lower_desc(const mf_kernel_desc* d, mf::LoweredKernel& lk) {
                    names(d->n_params, d->param_names), names(d->n_outputs, d->exprs),
                    d->kind == MF_KERNEL_GENERATE ? &gs : nullptr, (d->flags & MF_FLAG_NATIVE_F64) != 0, int(d->vec),
                    int(d->block), d->elem_type == MF_F64 && (d->flags & MF_FLAG_F32_ARITH) != 0,
-                   (d->flags & MF_FLAG_BULK_PIPELINE) == 0, int(d->stages));
+                   (d->flags & MF_FLAG_BULK_PIPELINE) == 0, int(d->stages), defs);
   } catch (const std::exception& e) {
     return fail(MF_ERR_PARSE, e.what());
   }

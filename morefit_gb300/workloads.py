@@ -69,8 +69,9 @@ class Likelihood:
             else:
                 b.SetupInputBuffer(self.pre, True)
             k = ks[name]
+            defs = dict(self.buffers[name])
             b.MakeComputeKernel(name, 0, k["inputs"], [f"r{i}" for i in range(len(k["exprs"]))], k["params"],
-                                k["exprs"], True)
+                                k["exprs"], True, param_defs=[defs.get(p, "") for p in k["params"]])
             self.blocks[name] = b
         if self.has_precompute:
             k = ks["precompute_kernel"]

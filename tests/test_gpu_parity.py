@@ -38,11 +38,14 @@ def _cols(g, ev):
     return ev
 
 
-@pytest.mark.parametrize("workload", ["pwave", "mass"])
-def test_fp64_matches_reference_golden(backend, workload):
+GOLDEN_SMALL = [("pwave", 1000), ("mass", 1000), ("spwave", 2000)]
+
+
+@pytest.mark.parametrize("workload,n", GOLDEN_SMALL)
+def test_fp64_matches_reference_golden(backend, workload, n):
     from morefit_gb300.workloads import Likelihood
-    g = load_golden(f"{workload}_n1000.json")
-    ev = golden_events(workload, 1000)
+    g = load_golden(f"{workload}_n{n}.json")
+    ev = golden_events(workload, n)
     like = Likelihood(backend, g, np.float64)
     like.set_data(ev)
     cols = _cols(g, ev)
@@ -54,13 +57,13 @@ def test_fp64_matches_reference_golden(backend, workload):
             assert_sums_close(got, ref, _abs_scale(g, name, cols, p), what=f"{workload} {name}")
 
 
-@pytest.mark.parametrize("workload", ["pwave", "mass"])
-def test_fitter_level_values(backend, workload):
+@pytest.mark.parametrize("workload,n", GOLDEN_SMALL)
+def test_fitter_level_values(backend, workload, n):
     """likelihood / likelihood_and_gradient / hessian as the fitter returns them."""
     from morefit_gb300.workloads import Likelihood
-    g = load_golden(f"{workload}_n1000.json")
+    g = load_golden(f"{workload}_n{n}.json")
     like = Likelihood(backend, g, np.float64)
-    like.set_data(golden_events(workload, 1000))
+    like.set_data(golden_events(workload, n))
     for pt in g["points"]:
         nll = like.likelihood(pt["params"])
         assert abs(nll - pt["nll"]) <= 1e-10 * abs(pt["nll"])
@@ -166,7 +169,8 @@ def test_deterministic(backend):
     assert np.array_equal(a, b)
 
 
-@pytest.mark.parametrize("workload,n", [("pwave", 1000), ("mass", 1000), ("pwave", 1000000), ("mass", 100000)])
+@pytest.mark.parametrize("workload,n", [("pwave", 1000), ("mass", 1000), ("pwave", 1000000), ("mass", 100000),
+                                        ("spwave", 20000)])
 def test_mixed_precision_parameter_shift(backend, oracle_lib, workload, n):
     """FP32 columns/arithmetic with FP64 sums move the estimate by at most 1e-3 sigma.
 
@@ -176,7 +180,10 @@ def test_mixed_precision_parameter_shift(backend, oracle_lib, workload, n):
     agree to 1e-6 relative."""
     from morefit_gb300.workloads import Likelihood
     g = load_golden(f"{workload}_n{n}.json")
-    ev = golden_events(workload, n) if n == 1000 else oracle_lib.generate(workload, n)
+    if workload == "spwave":  # no C restatement: the GPU generator on the reference's one-stream partition
+        ev = _reference_stream_events(backend, g, n)
+    else:
+        ev = golden_events(workload, n) if n == 1000 else oracle_lib.generate(workload, n)
     l64 = Likelihood(backend, g, np.float64)
     l64.set_data(ev)
     l32 = Likelihood(backend, g, np.float32)
@@ -191,6 +198,28 @@ def test_mixed_precision_parameter_shift(backend, oracle_lib, workload, n):
         shift = -hinv @ (g32 - g64) / sigma
         assert np.abs(shift).max() <= 1e-3, f"{workload} n={n}: shift/sigma {shift}"
         assert abs(f32 - f64) <= 1e-6 * abs(f64)
+
+
+def _reference_stream_events(backend, g, n):
+    """Events of the reference's generator run on one CPU thread: the GPU
+    generator with a single xoshiro128++ stream (seed row 0) draws the same
+    proposals in the same order; checked against the golden event hash."""
+    from oracle import mforacle
+    from morefit_gb300.workloads import generate_events
+    ev = generate_events(backend, g, n, max_workitems=1).download()
+    assert mforacle.fnv1a(ev) == g["events_fnv1a"], "GPU single-stream events differ from the reference's"
+    return ev
+
+
+@pytest.mark.parametrize("n", [2000, 20000])
+def test_gpu_generator_reproduces_reference_stream_spwave(backend, n):
+    """The S+P-wave-with-acceptance density (no C restatement) through the
+    GPU generator on the reference's one-stream partition gives the
+    reference generator's events bit for bit."""
+    g = load_golden(f"spwave_n{n}.json")
+    ev = _reference_stream_events(backend, g, n)
+    if n == 2000:
+        assert np.array_equal(ev, golden_events("spwave", n))
 
 
 def test_ragged_segments(backend):

@@ -105,3 +105,19 @@ def test_parse_error_is_reported():
         lower_source("bad", 0, 0, ["x"], [], ["log(x"])
     with pytest.raises(L.MFError, match="PARSE"):
         lower_source("bad", 0, 0, ["x"], [], ["foo(x)"])
+
+
+def test_spwave_folds_with_parameter_definitions():
+    """S+P wave with acceptance: 17 hoisted columns; the density's coefficients
+    (1-FS)(1-Fl) (two columns) and +-(1-FS)Fl (two columns) are hoisted parameter
+    buffers, so the relations show only when their definitions are given."""
+    from morefit_gb300 import _lib as L
+    from morefit_gb300.backend import lower_source
+    g = load_golden("spwave_n2000.json")
+    k = kernel_spec(g, "lh_grad_kernel")
+    defs = dict(g["grad_buffers"])
+    with_defs = lower_source("g", L.MF_KERNEL_REDUCE, L.MF_F64, k["inputs"], k["params"], k["exprs"],
+                             param_defs=[defs.get(p, "") for p in k["params"]])
+    assert "// reads 15 prepared columns (FP64 as float pairs) derived from 17 source columns" in with_defs
+    without = lower_source("g", L.MF_KERNEL_REDUCE, L.MF_F64, k["inputs"], k["params"], k["exprs"])
+    assert "// reads 16 prepared columns" in without
