@@ -922,6 +922,8 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
   s << "#define MF_BLOCK " << out.block << "\n#define MF_NOUT " << M << "\n#define MF_NPAR " << NP << "\n";
   // partial blocks each last-block thread loads per round (bounded register use)
   s << "#define MF_Q " << std::max(1, 32 / std::max(1, M)) << "\n";
+  // outputs per block-reduction chunk (one warp each)
+  s << "#define MF_RC " << std::max(1, std::min(8, out.block / 32)) << "\n";
   s << "struct mf_par { double v[MF_NPAR]; };\n";
 
   // Parameter-only prologue (u*), emitted once per thread.
@@ -1286,16 +1288,32 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
           o << ind << "mf_dw_acc(acc[" << j << "], " << r << ");\n";
       }
     };
-    // Per-thread accumulator of output j as a double-float value, summed over
-    // the warp (lane 0 holds the result).
-    auto warp_sum = [&](std::ostringstream& o) {
-      if (ar == Ar::F32 || ar == Ar::F32S)
-        o << "    mf_dw a = mf_two_sum(acc[j], -cmp[j]);\n";
-      else if (ar == Ar::F64)
-        o << "    mf_dw a = mf_dw_split(acc[j]);\n";
-      else
-        o << "    mf_dw a = mf_dw_renorm(acc[j]);\n";
-      o << "#pragma unroll\n    for (int o = 16; o > 0; o >>= 1) a = mf_dw_add(a, mf_dw_shfl_xor(a, o));\n";
+    // A thread's partial of output J as a double-float value (expression).
+    auto thread_dw = [&](const std::string& J) -> std::string {
+      if (ar == Ar::F32 || ar == Ar::F32S) return "mf_two_sum(acc[" + J + "], -cmp[" + J + "])";
+      if (ar == Ar::F64) return "mf_dw_split(acc[" + J + "])";
+      return "mf_dw_renorm(acc[" + J + "])";
+    };
+    // Block reduction of every output into mf_blk[] (shared): outputs go in
+    // chunks of MF_RC through a [MF_RC][MF_BLOCK] staging array; warp w sums
+    // output j0 + w (each lane a fixed stride of threads, then a shuffle
+    // tree), so every output costs one warp's work instead of every warp's.
+    // The order is fixed, so the result is reproducible.
+    auto block_reduce = [&](std::ostringstream& o) {
+      o << "  __shared__ float2 mf_stage_red[MF_RC][MF_BLOCK];\n  __shared__ float2 mf_blk[MF_NOUT];\n"
+        << "  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;\n"
+        << "#pragma unroll\n  for (int j0 = 0; j0 < MF_NOUT; j0 += MF_RC) {\n"
+        << "#pragma unroll\n    for (int c = 0; c < MF_RC; c++)\n"
+        << "      if (j0 + c < MF_NOUT) {\n        const mf_dw t = " << thread_dw("j0 + c") << ";\n"
+        << "        mf_stage_red[c][threadIdx.x] = make_float2(t.h, t.l);\n      }\n"
+        << "    __syncthreads();\n"
+        << "    if (warp < MF_RC && j0 + warp < MF_NOUT) {\n"
+        << "      mf_dw a = mf_dw_make(mf_stage_red[warp][lane].x, mf_stage_red[warp][lane].y);\n"
+        << "#pragma unroll\n      for (int k = 1; k < MF_BLOCK / 32; k++)\n"
+        << "        a = mf_dw_add(a, mf_dw_make(mf_stage_red[warp][lane + 32 * k].x, mf_stage_red[warp][lane + 32 * k].y));\n"
+        << "#pragma unroll\n      for (int o = 16; o > 0; o >>= 1) a = mf_dw_add(a, mf_dw_shfl_xor(a, o));\n"
+        << "      if (lane == 0) mf_blk[j0 + warp] = make_float2(a.h, a.l);\n    }\n"
+        << "    __syncthreads();\n  }\n";
     };
     auto load_table = [&](std::ostringstream& o) {
       if (ar != Ar::DW || !has_log) return;
@@ -1408,22 +1426,13 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
       });
       s << "  }\n";
     }
-    s << "  __shared__ float2 red[MF_NOUT][MF_BLOCK / 32];\n  __shared__ bool am_last;\n"
-      << "  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;\n#pragma unroll\n"
-      << "  for (int j = 0; j < MF_NOUT; j++) {\n";
-    warp_sum(s);
-    s << R"CUDA(    if (lane == 0) red[j][warp] = make_float2(a.h, a.l);
-  }
-  __syncthreads();
-  // Launched as a programmatic dependent of the previous evaluation on the
+    s << "  __shared__ float2 red[MF_NOUT][MF_BLOCK / 32];\n  __shared__ bool am_last;\n";
+    block_reduce(s);
+    s << R"CUDA(  // Launched as a programmatic dependent of the previous evaluation on the
   // stream (batched evaluations), this grid ran its event loop while that
   // one finished; the scratch below is shared, so wait for it to complete.
   mf_grid_dependency_wait();
-  for (int j = threadIdx.x; j < MF_NOUT; j += MF_BLOCK) {
-    mf_dw b = mf_dw_make(red[j][0].x, red[j][0].y);
-    for (int w = 1; w < MF_BLOCK / 32; w++) b = mf_dw_add(b, mf_dw_make(red[j][w].x, red[j][w].y));
-    partials[(mf_u64)blockIdx.x * MF_NOUT + j] = make_float2(b.h, b.l);
-  }
+  for (int j = threadIdx.x; j < MF_NOUT; j += MF_BLOCK) partials[(mf_u64)blockIdx.x * MF_NOUT + j] = mf_blk[j];
   // Completion count with release/acquire semantics: the barrier orders the
   // block's partial writes before thread 0's release; the last block's
   // acquire plus the barrier orders its reads of every partial after.
@@ -1489,18 +1498,9 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
     body(s, "    ");
     acc_add(s, "    ");
     s << "  }\n";
-    s << "  __shared__ float2 red[MF_NOUT][MF_BLOCK / 32];\n"
-      << "  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;\n#pragma unroll\n"
-      << "  for (int j = 0; j < MF_NOUT; j++) {\n";
-    warp_sum(s);
-    s << R"CUDA(    if (lane == 0) red[j][warp] = make_float2(a.h, a.l);
-  }
-  __syncthreads();
-  for (int j = threadIdx.x; j < MF_NOUT; j += MF_BLOCK) {
-    mf_dw b = mf_dw_make(red[j][0].x, red[j][0].y);
-    for (int w = 1; w < MF_BLOCK / 32; w++) b = mf_dw_add(b, mf_dw_make(red[j][w].x, red[j][w].y));
-    out[(mf_u64)seg * MF_NOUT + j] = mf_dw_to_double(b);
-  }
+    block_reduce(s);
+    s << R"CUDA(  for (int j = threadIdx.x; j < MF_NOUT; j += MF_BLOCK)
+    out[(mf_u64)seg * MF_NOUT + j] = mf_dw_to_double(mf_dw_make(mf_blk[j].x, mf_blk[j].y));
 }
 )CUDA";
     // ---- per-dataset preparation of the columns the entries above read ----
