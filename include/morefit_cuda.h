@@ -309,6 +309,20 @@ int mf_kernel_generate(mf_kernel* k, const uint32_t* seeds, uint32_t nseeds, uin
                        const double* params, uint32_t n_params, mf_buffer* out, uint64_t out_stride,
                        uint64_t max_tries);
 
+/* GENERATE for many datasets at once (toy studies with a different truth per
+ * toy): segment s owns output events [seg_begin[s], seg_begin[s] +
+ * seg_count[s]) and is generated by threads_per_seg xoshiro128++ streams
+ * (seeds: SoA [4][nthreads], nthreads = nseg x threads_per_seg; stream r of
+ * segment s fills the r-th block of ceil(count / threads_per_seg) events)
+ * with parameter row s (seg_params[s * n_params ...]) and accept-reject bound
+ * seg_maxprob[s]. The reference generates one toy per generator call
+ * (include/toystudy.hh:62-75, include/generator.hh:71-175); this is the
+ * batched form of the same accept-reject loop. */
+int mf_kernel_generate_segments(mf_kernel* k, const uint32_t* seeds, uint32_t nthreads, uint32_t threads_per_seg,
+                                uint32_t nseg, const uint64_t* seg_begin, const uint32_t* seg_count,
+                                const double* seg_params, uint32_t n_params, const double* seg_maxprob,
+                                mf_buffer* out, uint64_t out_stride, uint64_t max_tries);
+
 /* Host evaluation of parameter-only expressions (the hoisted parameter
  * buffers "morefit_parambuffer_k" that the fitter evaluates before every
  * launch). Replaces ComputeGraphNode::eval (include/graph.hh:193) as used by

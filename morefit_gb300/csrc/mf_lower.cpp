@@ -1576,20 +1576,43 @@ __device__ __forceinline__ unsigned mf_xoshiro(unsigned* s) {
     };
     const char* mul = ar32 ? "__fmul_rn" : "__dmul_rn";
     const char* add = ar32 ? "__fadd_rn" : "__dadd_rn";
+    auto accept_reject = [&]() {
+      s << "  unsigned long long tries = 0;\n";
+      s << "  for (mf_u64 i = from; i < to; i++) {\n    for (;;) {\n";
+      s << "      if (++tries > max_tries) { atomicOr(status, 1u); return; }\n";
+      for (int d = 0; d < D; d++) {
+        s << "      const " << AT << " x" << d << " = " << add << "(" << fmt_const(printed15(gen->lo[d]), ar32) << ", "
+          << mul << "(" << fmt_const(printed15(gen->hi[d] - gen->lo[d]), ar32) << ", (" << AT
+          << ")(mf_xoshiro(st) * 2.3283064365386963e-10)));\n";
+      }
+      emit_body(s, "      ");
+      s << "      if (" << mul << "(maxprob, (" << AT << ")(mf_xoshiro(st) * 2.3283064365386963e-10)) < r0) {\n";
+      for (int d = 0; d < D; d++)
+        s << "        outp[(mf_u64)" << d << " * out_stride + i] = (" << ST << ")x" << d << ";\n";
+      s << "        break;\n      }\n    }\n  }\n}\n";
+    };
     s << "  const " << AT << " maxprob = " << fmt_const(printed15(gen->maxprob), ar32) << ";\n";
     s << "  const mf_u64 from = (mf_u64)t * nper;\n  mf_u64 to = from + nper; if (to > n) to = n;\n";
-    s << "  unsigned long long tries = 0;\n";
-    s << "  for (mf_u64 i = from; i < to; i++) {\n    for (;;) {\n";
-    s << "      if (++tries > max_tries) { atomicOr(status, 1u); return; }\n";
-    for (int d = 0; d < D; d++) {
-      s << "      const " << AT << " x" << d << " = " << add << "(" << fmt_const(printed15(gen->lo[d]), ar32) << ", "
-        << mul << "(" << fmt_const(printed15(gen->hi[d] - gen->lo[d]), ar32) << ", (" << AT
-        << ")(mf_xoshiro(st) * 2.3283064365386963e-10)));\n";
-    }
-    emit_body(s, "      ");
-    s << "      if (" << mul << "(maxprob, (" << AT << ")(mf_xoshiro(st) * 2.3283064365386963e-10)) < r0) {\n";
-    for (int d = 0; d < D; d++) s << "        outp[(mf_u64)" << d << " * out_stride + i] = (" << ST << ")x" << d << ";\n";
-    s << "        break;\n      }\n    }\n  }\n}\n";
+    accept_reject();
+    // Segments (toy studies): `threads_per_seg` streams per segment; segment
+    // s owns events [seg_begin[s], seg_begin[s] + seg_count[s]) and generates
+    // them with its own parameter row and bound (thread r of the segment
+    // takes the r-th block of ceil(count / threads_per_seg) events).
+    s << "extern \"C\" __global__ void __launch_bounds__(MF_BLOCK) " << out.entry
+      << "_segments(const unsigned* __restrict__ seeds, unsigned nthreads, unsigned threads_per_seg,"
+      << " const mf_u64* __restrict__ seg_begin, const unsigned* __restrict__ seg_count,"
+      << " const mf_par* __restrict__ seg_params, const double* __restrict__ seg_maxprob, " << ST
+      << "* __restrict__ outp, mf_u64 out_stride, unsigned* __restrict__ status, unsigned long long max_tries) {\n";
+    s << "  const unsigned t = blockIdx.x * MF_BLOCK + threadIdx.x;\n  if (t >= nthreads) return;\n";
+    s << "  const unsigned seg = t / threads_per_seg, r = t - seg * threads_per_seg;\n";
+    s << "  unsigned st[4];\n#pragma unroll\n  for (int k = 0; k < 4; k++) st[k] = seeds[(mf_u64)k * nthreads + t];\n";
+    s << "  const mf_par& P = seg_params[seg];\n";
+    emit_params_and_uniform(s, "P.v");
+    s << "  const " << AT << " maxprob = (" << AT << ")seg_maxprob[seg];\n";
+    s << "  const mf_u64 cnt = seg_count[seg], per = (cnt + threads_per_seg - 1) / threads_per_seg;\n";
+    s << "  const mf_u64 from = seg_begin[seg] + (mf_u64)r * per;\n";
+    s << "  mf_u64 to = from + per; if (to > seg_begin[seg] + cnt) to = seg_begin[seg] + cnt;\n";
+    accept_reject();
   }
   out.source = s.str();
   return out;

@@ -632,7 +632,7 @@ int mf_kernel_build(mf_context* c, const mf_kernel_desc* d, mf_kernel** out) {
   MF_CUDA_TRY(cudaSetDevice(c->device));
   MF_CUDA_TRY(cudaLibraryLoadData(&k->lib, k->image->cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0));
   MF_CUDA_TRY(cudaLibraryGetKernel(&k->fn, k->lib, k->lowered.entry.c_str()));
-  if (d->kind == MF_KERNEL_REDUCE)
+  if (d->kind == MF_KERNEL_REDUCE || d->kind == MF_KERNEL_GENERATE)
     MF_CUDA_TRY(cudaLibraryGetKernel(&k->fn_seg, k->lib, (k->lowered.entry + "_segments").c_str()));
   if (k->lowered.prep) {
     MF_CUDA_TRY(cudaLibraryGetKernel(&k->fn_prep, k->lib, (k->lowered.entry + "_prep").c_str()));
@@ -1142,6 +1142,61 @@ int mf_kernel_generate(mf_kernel* k, const uint32_t* seeds, uint32_t nseeds, uin
   void* args[] = {&sd, &nseeds, &n, &nper, pv.data(), &outp, &out_stride, &status, &mt};
   const unsigned grid = (nseeds + k->lowered.block - 1) / k->lowered.block;
   MF_CUDA_TRY(cudaLaunchKernel(reinterpret_cast<const void*>(k->fn), dim3(grid), dim3(k->lowered.block), args, 0,
+                               c->stream));
+  MF_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  const unsigned st = *c->status_host;
+  *c->status_host = 0u;
+  if (st) return fail(MF_ERR_TIMEOUT, "generation gave up after max_tries proposals in at least one thread");
+  return MF_OK;
+}
+
+int mf_kernel_generate_segments(mf_kernel* k, const uint32_t* seeds, uint32_t nthreads, uint32_t threads_per_seg,
+                                uint32_t nseg, const uint64_t* seg_begin, const uint32_t* seg_count,
+                                const double* seg_params, uint32_t n_params, const double* seg_maxprob,
+                                mf_buffer* out, uint64_t out_stride, uint64_t max_tries) {
+  if (!k || !seeds || !seg_begin || !seg_count || !seg_maxprob || !out || (n_params && !seg_params))
+    return fail(MF_ERR_INVALID, "null argument");
+  if (k->kind != MF_KERNEL_GENERATE) return fail(MF_ERR_INVALID, "kernel is not a GENERATE kernel");
+  if (n_params != k->n_params) return fail(MF_ERR_INVALID, "parameter count mismatch");
+  if (threads_per_seg == 0 || uint64_t(nseg) * threads_per_seg != nthreads)
+    return fail(MF_ERR_INVALID, "nthreads must equal nseg x threads_per_seg");
+  if (nseg == 0) return MF_OK;
+  for (uint32_t s = 0; s < nseg; s++)
+    if (seg_begin[s] + seg_count[s] > out_stride)
+      return fail(MF_ERR_INVALID, "segment " + std::to_string(s) + " reaches beyond the output stride");
+  if (uint64_t(k->n_gen_dims) * out_stride * elem_size(k->elem) > out->size)
+    return fail(MF_ERR_INVALID, "output buffer smaller than dimensions x stride");
+  mf_context* c = k->ctx;
+  MF_CUDA_TRY(cudaSetDevice(c->device));
+  const size_t np = std::max<uint32_t>(1, n_params);  // mf_par holds at least one value
+  const size_t b_seeds = (size_t(nthreads) * 16 + 15) / 16 * 16, b_begin = size_t(nseg) * 8,
+               b_count = (size_t(nseg) * 4 + 15) / 16 * 16, b_par = size_t(nseg) * np * 8, b_max = size_t(nseg) * 8;
+  std::vector<unsigned char> host(b_seeds + b_begin + b_count + b_par + b_max, 0);
+  std::memcpy(host.data(), seeds, size_t(nthreads) * 16);
+  std::memcpy(host.data() + b_seeds, seg_begin, b_begin);
+  std::memcpy(host.data() + b_seeds + b_begin, seg_count, size_t(nseg) * 4);
+  double* par = reinterpret_cast<double*>(host.data() + b_seeds + b_begin + b_count);
+  for (uint32_t s = 0; s < nseg; s++)
+    for (uint32_t q = 0; q < n_params; q++) par[size_t(s) * np + q] = seg_params[size_t(s) * n_params + q];
+  std::memcpy(host.data() + b_seeds + b_begin + b_count + b_par, seg_maxprob, b_max);
+  int rc = ensure_stage(c, host.size());
+  if (rc) return rc;
+  MF_CUDA_TRY(cudaMemcpyAsync(c->stage_dev, host.data(), host.size(), cudaMemcpyHostToDevice, c->stream));
+  char* base = static_cast<char*>(c->stage_dev);
+  const unsigned* d_seeds = reinterpret_cast<const unsigned*>(base);
+  const uint64_t* d_begin = reinterpret_cast<const uint64_t*>(base + b_seeds);
+  const unsigned* d_count = reinterpret_cast<const unsigned*>(base + b_seeds + b_begin);
+  const void* d_par = base + b_seeds + b_begin + b_count;
+  const double* d_max = reinterpret_cast<const double*>(base + b_seeds + b_begin + b_count + b_par);
+  *c->status_host = 0u;
+  out->gen++;
+  void* outp = out->ptr;
+  unsigned* status = c->status;
+  unsigned long long mt = max_tries ? max_tries : 1000000000ULL;
+  void* args[] = {&d_seeds, &nthreads, &threads_per_seg, &d_begin, &d_count, const_cast<void**>(&d_par), &d_max,
+                  &outp, &out_stride, &status, &mt};
+  const unsigned grid = (nthreads + k->lowered.block - 1) / k->lowered.block;
+  MF_CUDA_TRY(cudaLaunchKernel(reinterpret_cast<const void*>(k->fn_seg), dim3(grid), dim3(k->lowered.block), args, 0,
                                c->stream));
   MF_CUDA_TRY(cudaStreamSynchronize(c->stream));
   const unsigned st = *c->status_host;

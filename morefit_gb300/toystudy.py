@@ -26,8 +26,13 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from .backend import CUDABackend, eval_expressions_batch
-from .workloads import DEFAULT_SEED, Likelihood, generate_events
+import ctypes as C
+import math
+import re
+
+from . import _lib as L
+from .backend import CUDABackend, CUDABlock, DeviceColumns, eval_expressions_batch
+from .workloads import DEFAULT_SEED, Likelihood, generate_events, seed_rows
 
 # Parameter limits of the K*mumu P-wave fit (Fl in [0, 1], the rest in [-1, 1]),
 # as the reference's benchmark drivers declare them.
@@ -147,11 +152,61 @@ def fit_segments(sl: SegmentLikelihood, theta0: np.ndarray, limits, tol: float =
     return FitResult(theta, errors, fmin, edm, iters, conv, sl.evaluations)
 
 
+def density_expression(spec: dict):
+    """The model's density as one expression of the raw observables with the
+    fitter's parameters: exp of the log-density kernel text (the lh kernel,
+    fitter.hh:380-396) with every hoisted event buffer replaced by its own
+    expression. Returns (expression, parameter names, parameter-buffer list)."""
+    k = next(k for k in spec["kernels"] if k["name"] == "lh_kernel")
+    expr = k["exprs"][0]
+    for name, e in sorted(spec["event_buffers"], key=lambda x: -len(x[0])):
+        if name != e:
+            expr = re.sub(r"\b" + re.escape(name) + r"\b", "(" + e + ")", expr)
+    return "exp(" + expr + ")", list(k["params"]), spec["lh_buffers"]
+
+
+def pwave_maxprob(theta: np.ndarray) -> np.ndarray:
+    """KstarmumuAngularPDF::get_max (physicspdfs.hh:209-213) for each row of theta
+    (Fl, S3, S4, S5, Afb, S7, S8, S9)."""
+    t = np.abs(np.asarray(theta, dtype=np.float64))
+    return 9.0 / 32.0 / math.pi * (4.0 + t[:, 1] + t[:, 2] + t[:, 3] + 4.0 / 3.0 * t[:, 4] + t[:, 5] + t[:, 6]
+                                   + t[:, 7])
+
+
+def generate_segments(backend: CUDABackend, spec: dict, theta: np.ndarray, counts, maxprob: np.ndarray,
+                      seed: int = DEFAULT_SEED, threads_per_seg: int = 16) -> DeviceColumns:
+    """Events of many datasets, dataset s at parameters theta[s] (one launch):
+    dataset s owns events [begin[s], begin[s] + counts[s]) of the returned block."""
+    expr, params, bufs = density_expression(spec)
+    gk = next(k for k in spec["kernels"] if k.get("generate"))
+    blk = CUDABlock(backend, np.float64)
+    blk.MakeGenerateKernel("gen_segments", 0, [], gk["outputs"], params, [expr], 1.0,
+                           ranges=list(zip(gk["lo"], gk["hi"])))
+    theta = np.ascontiguousarray(theta, dtype=np.float64)
+    nfloat = theta.shape[1]
+    rows = theta if len(params) == nfloat else np.concatenate(
+        [theta, eval_expressions_batch(params[:nfloat], theta, [e for _, e in bufs])], axis=1)
+    counts = np.ascontiguousarray(counts, dtype=np.uint32)
+    begins = np.concatenate([[0], np.cumsum(counts, dtype=np.uint64)[:-1]]).astype(np.uint64)
+    nseg = len(counts)
+    nthreads = nseg * threads_per_seg
+    seeds = np.ascontiguousarray(seed_rows(nthreads, seed), dtype=np.uint32)
+    out = DeviceColumns(backend, L.MF_F64)
+    out.ensure(len(gk["outputs"]), int(counts.sum()))
+    mp = np.ascontiguousarray(maxprob, dtype=np.float64)
+    per = int(-(-int(counts.max()) // threads_per_seg))
+    L.check(L.lib.mf_kernel_generate_segments(
+        blk.kernel.handle, seeds.ctypes.data_as(C.POINTER(C.c_uint32)), nthreads, threads_per_seg, nseg,
+        begins.ctypes.data_as(C.POINTER(C.c_uint64)), counts.ctypes.data_as(C.POINTER(C.c_uint32)),
+        L.dptr(np.ascontiguousarray(rows)), rows.shape[1], L.dptr(mp), out.buf, out.stride, 10000 * per))
+    return out
+
+
 @dataclass
 class ToyResult:
     counts: np.ndarray
     fit: FitResult
-    truth: np.ndarray
+    truth: np.ndarray       # (ntoys, npar)
     pulls: np.ndarray       # (ntoys, npar)
     timing: dict
 
@@ -174,7 +229,24 @@ class ToyStudy:
         self.seed = seed
         self.generator_threads = generator_threads
 
-    def toy(self, nruns: int, nevents: int, poisson: bool = False, clip=(1, None)) -> ToyResult:
+    def serial_fits_per_s(self, result: "ToyResult", ntoys: int = 32) -> float:
+        """The per-fit serial baseline: the first ``ntoys`` toys of ``result``'s
+        event block fitted one at a time (one segment per launch, each fit
+        waiting for the previous), same fitter and tolerances."""
+        import time
+        sl_all = self._last_segments
+        t0 = time.perf_counter()
+        for t in range(min(ntoys, len(result.counts))):
+            sl = SegmentLikelihood(sl_all.like, sl_all.begins[t:t + 1], sl_all.counts[t:t + 1])
+            fit_segments(sl, result.truth[t:t + 1], self.limits)
+        return min(ntoys, len(result.counts)) / (time.perf_counter() - t0)
+
+    def toy(self, nruns: int, nevents: int, poisson: bool = False, clip=(1, None), jitter: float = 0.0,
+            maxprob=pwave_maxprob) -> ToyResult:
+        """``jitter``: each toy's truth is the model truth times (1 + u), u
+        uniform in [-jitter, jitter] (zero truths stay zero); such toys are
+        generated one dataset per segment, each at its own truth, with the
+        bound ``maxprob(theta)`` per toy (the P-wave's get_max by default)."""
         import time
         t0 = time.perf_counter()
         rng = np.random.default_rng(self.seed)
@@ -185,15 +257,21 @@ class ToyStudy:
         counts = np.clip(counts, clip[0], clip[1] if clip[1] is not None else np.iinfo(np.int64).max)
         begins = np.concatenate([[0], np.cumsum(counts)[:-1]]).astype(np.uint64)
         total = int(counts.sum())
-        cols = generate_events(self.backend, self.spec, total, seed=self.seed, max_workitems=self.generator_threads,
-                               kernelT=np.float64)
+        base = np.array(self.spec["truth"], dtype=np.float64)
+        if jitter > 0.0:
+            truth = base * (1.0 + rng.uniform(-jitter, jitter, (nruns, base.size)))
+            cols = generate_segments(self.backend, self.spec, truth, counts, maxprob(truth), seed=self.seed)
+        else:
+            truth = np.tile(base, (nruns, 1))
+            cols = generate_events(self.backend, self.spec, total, seed=self.seed,
+                                   max_workitems=self.generator_threads, kernelT=np.float64)
         like = Likelihood(self.backend, self.spec, self.kernelT)
         like.set_device_data(cols)
         self.backend.synchronize()
         t1 = time.perf_counter()
-        truth = np.array(self.spec["truth"], dtype=np.float64)
         sl = SegmentLikelihood(like, begins, counts)
-        fit = fit_segments(sl, np.tile(truth, (nruns, 1)), self.limits)
+        self._last_segments = sl
+        fit = fit_segments(sl, truth, self.limits)
         t2 = time.perf_counter()
         pulls = (fit.values - truth) / fit.errors
         return ToyResult(counts, fit, truth, pulls,

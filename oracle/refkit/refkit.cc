@@ -20,6 +20,7 @@
 // Usage:
 //   refkit golden <mass|pwave|spwave> <nevents> <out.json> [events.bin]
 //   refkit bench  <mass|pwave|spwave> <nevents> <nthreads> <nevals>
+//   refkit toys   <pwave> <ntoys> <mean events> <jitter> <out.json>
 #define MOREFIT_H 1  // keep graph.hh from pulling in the OpenCL/LLVM backends
 #include <cassert>
 #include <chrono>
@@ -588,6 +589,74 @@ static int cmd_bench(const std::string& which, unsigned n, unsigned nthreads, un
   return 0;
 }
 
+// Toy study with the reference's own generator and fitter, one toy at a
+// time as toystudy::toy does (toystudy.hh:55-82), except that every toy's
+// truth is the workload's truth times (1 + u), u uniform in [-jitter, jitter]
+// (SplitMix64 stream), and the event count is the reference's
+// RandomGenerator::poisson(mean) (random.hh:42-80) clipped to [200, 50000].
+// Each toy is generated at its truth (the generate kernel is rebuilt per toy
+// because the generator substitutes the parameter values into it,
+// generator.hh:145) and fitted from it (MIGRAD + HESSE). Writes the pulls.
+static int cmd_toys(const std::string& which, unsigned ntoys, double mean, double jitter, const std::string& out) {
+  compute_options copts;
+  copts.llvm_nthreads = 1;
+  copts.print_kernel = false;
+  backendT backend(&copts);
+  Workload w = make_workload(which);
+  Xoshiro128pp rnd;
+  rnd.setSeed(int64_t(229387429));
+  generator_options gen_opts;
+  gen_opts.rndtype = generator_options::randomization_type::on_accelerator;
+  gen_opts.print_level = 0;
+  generator<kT, eT, backendT, blockT> gen(&gen_opts, &backend, &rnd);
+  fitter_options fopts = make_fit_opts(w);
+  fitter<kT, eT, backendT, blockT> fit(&fopts, &backend);
+  std::vector<double> base;
+  for (auto* p : w.params) base.push_back(p->get_value());
+  uint64_t sm = 0x746f79737475ULL;
+  auto uni = [&sm]() {
+    sm += 0x9e3779b97f4a7c15ULL;
+    uint64_t z = sm;
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+    return double((z ^ (z >> 31)) >> 11) * 0x1.0p-53;
+  };
+  std::string pulls = "[", truths = "[", counts = "[";
+  unsigned nconv = 0;
+  std::ostringstream sink;
+  auto* old = std::cout.rdbuf(sink.rdbuf());
+  for (unsigned t = 0; t < ntoys; t++) {
+    std::vector<double> truth(base.size());
+    for (size_t i = 0; i < base.size(); i++) truth[i] = base[i] * (1.0 + jitter * (2.0 * uni() - 1.0));
+    for (size_t i = 0; i < base.size(); i++) {
+      w.params[i]->set_value(truth[i]);
+      w.params[i]->set_start_value(truth[i]);
+    }
+    unsigned n = rnd.poisson(mean);
+    n = std::min(50000u, std::max(200u, n));
+    EventVector<kT, eT> data(w.dims, n);
+    gen.generate(n, w.pdf, w.params, data, false);
+    for (size_t i = 0; i < base.size(); i++) w.params[i]->set_value(truth[i]);
+    const bool ok = fit.fit(w.pdf, w.params, &data, t > 0);
+    nconv += ok ? 1 : 0;
+    std::vector<double> pl;
+    for (size_t i = 0; i < base.size(); i++)
+      pl.push_back((w.params[i]->get_value() - truth[i]) / w.params[i]->get_error());
+    pulls += std::string(t ? "," : "") + jvec(pl);
+    truths += std::string(t ? "," : "") + jvec(truth);
+    counts += std::string(t ? "," : "") + std::to_string(n);
+  }
+  std::cout.rdbuf(old);
+  std::string js = "{\"workload\":" + jstr(which) + ",\"ntoys\":" + std::to_string(ntoys) + ",\"mean\":" + jnum(mean) +
+                   ",\"jitter\":" + jnum(jitter) + ",\"converged\":" + std::to_string(nconv) + ",\"counts\":" +
+                   counts + "],\"truths\":" + truths + "],\"pulls\":" + pulls + "]}\n";
+  FILE* f = std::fopen(out.c_str(), "w");
+  std::fputs(js.c_str(), f);
+  std::fclose(f);
+  std::fprintf(stderr, "toys %s: %u of %u fits converged\n", which.c_str(), nconv, ntoys);
+  return 0;
+}
+
 int main(int argc, char** argv) {
   install_capture();
   if (argc >= 5 && std::string(argv[1]) == "golden")
@@ -595,7 +664,10 @@ int main(int argc, char** argv) {
   if (argc >= 6 && std::string(argv[1]) == "bench")
     return cmd_bench(argv[2], unsigned(std::stoul(argv[3])), unsigned(std::stoul(argv[4])),
                      unsigned(std::stoul(argv[5])));
-  std::fprintf(stderr, "usage: refkit golden <mass|pwave> <n> <out.json> [events.bin]\n"
-                       "       refkit bench <mass|pwave> <n> <nthreads> <nevals>\n");
+  if (argc >= 7 && std::string(argv[1]) == "toys")
+    return cmd_toys(argv[2], unsigned(std::stoul(argv[3])), std::stod(argv[4]), std::stod(argv[5]), argv[6]);
+  std::fprintf(stderr, "usage: refkit golden <mass|pwave|spwave> <n> <out.json> [events.bin]\n"
+                       "       refkit bench <mass|pwave|spwave> <n> <nthreads> <nevals>\n"
+                       "       refkit toys <pwave> <ntoys> <mean events> <jitter> <out.json>\n");
   return 2;
 }

@@ -14,4 +14,5 @@ K="$ROOT/oracle/_ref/refkit"
 "$K" golden pwave 1000000 "$HERE/pwave_n1000000.json"
 "$K" golden spwave 2000 "$HERE/spwave_n2000.json" "$HERE/spwave_n2000_events.f64"
 "$K" golden spwave 20000 "$HERE/spwave_n20000.json"
+"$K" toys pwave 1000 2000 0.1 "$HERE/toys_pwave_ref.json"
 python3 "$HERE/extract_specs.py"

@@ -65,23 +65,66 @@ def test_batched_fits_equal_single_fits(backend):
     begins = np.concatenate([[0], np.cumsum(res.counts)[:-1]])
     for t in (5, 17):
         sl = SegmentLikelihood(like, [begins[t]], [res.counts[t]])
-        one = fit_segments(sl, np.array([res.truth]), PWAVE_LIMITS)
+        one = fit_segments(sl, res.truth[t:t + 1], PWAVE_LIMITS)
         assert np.array_equal(one.values[0], res.fit.values[t])
         assert np.array_equal(one.errors[0], res.fit.errors[t])
 
 
-def test_toy_study_pulls(backend):
-    """256 toys of Poisson(2000) events: every fit converges and the pulls of
-    every parameter have mean within 0.35 of 0 and width within 0.15 of 1
-    (seeded, so the outcome is fixed). The mean bar leaves room for the
-    maximum-likelihood estimator's finite-sample bias: S4's pull mean is
-    -0.20 +- 0.02 over 4096 such toys."""
+def test_toy_study_pulls_match_reference_toys(backend):
+    """Config of the batched toy study: Poisson(2000) events clipped to
+    [200, 50000], every toy's truth jittered by +-10%, each toy generated at
+    and fitted from its own truth. The pull distributions of 2048 GPU toys
+    match those of 1000 toys run through the reference's own generator and
+    fitter (MIGRAD + HESSE, tests/golden/toys_pwave_ref.json): per parameter,
+    means within 3 combined standard errors and widths within 3 combined
+    standard errors of each other."""
     from morefit_gb300.toystudy import ToyStudy
     from morefit_gb300.workloads import load_spec
-    res = ToyStudy(backend, load_spec("pwave"), seed=99).toy(256, 2000, poisson=True, clip=(200, 50000))
+    ref = load_golden("toys_pwave_ref.json")
+    rp = np.array(ref["pulls"])
+    assert ref["converged"] == ref["ntoys"]
+    res = ToyStudy(backend, load_spec("pwave"), seed=99).toy(2048, 2000, poisson=True, clip=(200, 50000),
+                                                             jitter=0.1)
     assert res.fit.converged.all()
     assert res.counts.min() >= 200
-    mean = res.pulls.mean(axis=0)
-    std = res.pulls.std(axis=0)
-    assert np.all(np.abs(mean) < 0.35), mean
-    assert np.all(np.abs(std - 1.0) < 0.15), std
+    gp = res.pulls
+    n_r, n_g = len(rp), len(gp)
+    se_mean = 3.0 * np.sqrt(1.0 / n_r + 1.0 / n_g)
+    se_std = 3.0 * np.sqrt(1.0 / (2 * n_r) + 1.0 / (2 * n_g))
+    assert np.all(np.abs(gp.mean(0) - rp.mean(0)) < se_mean), (gp.mean(0), rp.mean(0))
+    assert np.all(np.abs(gp.std(0) - rp.std(0)) < se_std), (gp.std(0), rp.std(0))
+
+
+def test_segment_generation_is_independent_per_segment(backend):
+    """Segment s's events depend only on its own streams, truth and bound:
+    generating it alone gives the same events as within the batch."""
+    from morefit_gb300.toystudy import generate_segments, pwave_maxprob
+    from morefit_gb300.workloads import load_spec, seed_rows
+    spec = load_spec("pwave")
+    rng = np.random.default_rng(5)
+    truth = np.array(spec["truth"]) * (1.0 + rng.uniform(-0.1, 0.1, (5, 8)))
+    counts = np.array([300, 1200, 17, 800, 2000])
+    allv = generate_segments(backend, spec, truth, counts, pwave_maxprob(truth), seed=77, threads_per_seg=8).download()
+    begins = np.concatenate([[0], np.cumsum(counts)[:-1]])
+    assert np.all(np.abs(allv[:2]) <= 1.0) and np.all(np.abs(allv[2]) <= np.pi)
+    # segment 3 alone, with its own seed rows (rows 24..31 of the batch's table)
+    from morefit_gb300 import _lib as L
+    import ctypes as C
+    from morefit_gb300.backend import CUDABlock, DeviceColumns
+    from morefit_gb300.toystudy import density_expression
+    expr, params, bufs = density_expression(spec)
+    gk = next(k for k in spec["kernels"] if k.get("generate"))
+    blk = CUDABlock(backend, np.float64)
+    blk.MakeGenerateKernel("g", 0, [], gk["outputs"], params, [expr], 1.0, ranges=list(zip(gk["lo"], gk["hi"])))
+    from morefit_gb300.backend import eval_expressions_batch
+    row = np.concatenate([truth[3:4], eval_expressions_batch(params[:8], truth[3:4], [e for _, e in bufs])], axis=1)
+    seeds = np.ascontiguousarray(seed_rows(40, 77)[:, 24:32], dtype=np.uint32)
+    out = DeviceColumns(backend, L.MF_F64)
+    out.ensure(3, int(counts[3]))
+    L.check(L.lib.mf_kernel_generate_segments(
+        blk.kernel.handle, seeds.ctypes.data_as(C.POINTER(C.c_uint32)), 8, 8, 1,
+        np.array([0], np.uint64).ctypes.data_as(C.POINTER(C.c_uint64)),
+        np.array([counts[3]], np.uint32).ctypes.data_as(C.POINTER(C.c_uint32)), L.dptr(np.ascontiguousarray(row)),
+        row.shape[1], L.dptr(pwave_maxprob(truth[3:4])), out.buf, out.stride, 10000000))
+    alone = out.download()
+    assert np.array_equal(alone, allv[:, begins[3]:begins[3] + counts[3]])
