@@ -336,6 +336,14 @@ int mf_eval_expressions(uint32_t n_names, const char* const* names, const double
  * (include/toystudy.hh:55-82 runs one fitter per toy). */
 int mf_eval_expressions_batch(uint32_t n_names, const char* const* names, uint32_t n_rows, const double* values,
                               uint32_t n_exprs, const char* const* exprs, double* out);
+/* The same with the expressions parsed once into a handle, for callers that
+ * evaluate them at every step (a fitter's per-evaluation parameter buffers,
+ * a server's many concurrent fits): out [n_rows][n_exprs]. */
+typedef struct mf_expr_set mf_expr_set;
+int mf_expr_set_create(uint32_t n_names, const char* const* names, uint32_t n_exprs, const char* const* exprs,
+                       mf_expr_set** out);
+int mf_expr_set_eval(const mf_expr_set* set, uint32_t n_rows, const double* values, double* out);
+int mf_expr_set_free(mf_expr_set* set);
 
 /* Seed rows for the accelerator generator (include/generator.hh:115-135):
  * an xoshiro128++ state seeded like Xoshiro128pp::setSeed(seed)

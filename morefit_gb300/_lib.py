@@ -123,6 +123,9 @@ _proto("mf_columns_sum_noalloc", C.c_int, C.c_void_p, C.c_int, C.c_uint32, C.c_u
        C.c_void_p)
 _proto("mf_context_stream", C.c_int, c_ctx, C.POINTER(C.c_void_p))
 _proto("mf_buffer_mark_modified", C.c_int, c_buf)
+_proto("mf_expr_set_create", C.c_int, C.c_uint32, c_char_pp, C.c_uint32, c_char_pp, C.POINTER(C.c_void_p))
+_proto("mf_expr_set_eval", C.c_int, C.c_void_p, C.c_uint32, c_dbl_p, c_dbl_p)
+_proto("mf_expr_set_free", C.c_int, C.c_void_p)
 _proto("mf_kernel_generate_segments", C.c_int, c_ker, C.POINTER(C.c_uint32), C.c_uint32, C.c_uint32, C.c_uint32,
        C.POINTER(C.c_uint64), C.POINTER(C.c_uint32), c_dbl_p, C.c_uint32, c_dbl_p, c_buf, C.c_uint64, C.c_uint64)
 _proto("mf_eval_expressions_batch", C.c_int, C.c_uint32, c_char_pp, C.c_uint32, c_dbl_p, C.c_uint32, c_char_pp,
@@ -171,4 +174,5 @@ def exported_symbols() -> list[str]:
         "mf_kernel_generate", "mf_eval_expressions", "mf_seed_rows", "mf_generate_partition", "mf_lower_source",
         "mf_compile_check", "mf_buffer_mark_modified", "mf_kernel_read_layout", "mf_events_upload_async",
         "mf_buffer_d2h_async", "mf_kernel_store_async", "mf_eval_expressions_batch", "mf_kernel_generate_segments",
+        "mf_expr_set_create", "mf_expr_set_eval", "mf_expr_set_free",
     ]

@@ -232,6 +232,29 @@ def eval_expressions_batch(names: Sequence[str], rows: np.ndarray, exprs: Sequen
     return out[:, : len(exprs)]
 
 
+class ExpressionSet:
+    """Parameter-only expressions parsed once (mf_expr_set); ``eval(rows)``
+    evaluates them for every row of parameter values."""
+
+    def __init__(self, names: Sequence[str], exprs: Sequence[str]):
+        self.n_names, self.n_exprs = len(names), len(exprs)
+        self.handle = C.c_void_p()
+        L.check(L.lib.mf_expr_set_create(len(names), C.cast(L.cstrings(list(names)), L.c_char_pp), len(exprs),
+                                         C.cast(L.cstrings(list(exprs)), L.c_char_pp), C.byref(self.handle)))
+
+    def eval(self, rows) -> np.ndarray:
+        v = np.ascontiguousarray(rows, dtype=np.float64).reshape(-1, self.n_names)
+        out = np.zeros((v.shape[0], self.n_exprs))
+        if self.n_exprs:
+            L.check(L.lib.mf_expr_set_eval(self.handle, v.shape[0], L.dptr(v), L.dptr(out)))
+        return out
+
+    def __del__(self):
+        if getattr(self, "handle", None):
+            L.lib.mf_expr_set_free(self.handle)
+            self.handle = None
+
+
 class CUDABlock:
     """ComputeBlock<kernelT, evalT> over the CUDA C ABI (compute.hh:110-149).
 

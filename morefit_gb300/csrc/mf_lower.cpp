@@ -340,6 +340,24 @@ int Dag::parse(const std::string& expr) {
   return p.run();
 }
 
+void Dag::eval_all(const double* pa, size_t np, std::vector<double>& v) const {
+  v.resize(nodes_.size());
+  for (size_t i = 0; i < nodes_.size(); i++) {
+    const Node& n = nodes_[i];
+    switch (n.op) {
+      case Op::Const: v[i] = n.value; break;
+      case Op::Input: v[i] = 0.0; break;
+      case Op::Param: v[i] = size_t(n.index) < np ? pa[n.index] : 0.0; break;
+      case Op::Add: case Op::Sub: case Op::Mul: case Op::Div: case Op::Pow:
+        v[i] = apply_binary(n.op, v[n.a], v[n.b]);
+        break;
+      case Op::Cmp: v[i] = apply_cmp(n.cmp, v[n.a], v[n.b]) ? 1.0 : 0.0; break;
+      case Op::Select: v[i] = v[n.a] != 0.0 ? v[n.b] : v[n.c]; break;
+      default: v[i] = apply_unary(n.op, v[n.a]); break;
+    }
+  }
+}
+
 double Dag::eval(int id, const std::vector<double>& in, const std::vector<double>& pa) const {
   const Node& n = nodes_[id];
   switch (n.op) {

@@ -55,6 +55,9 @@ class Dag {
   int select(int cond, int a, int b);
   // Host evaluation (parameter-only expressions, tests).
   double eval(int id, const std::vector<double>& inputs, const std::vector<double>& params) const;
+  // Every node in order (children before parents) for one parameter vector;
+  // inputs evaluate to 0. `vals` is resized to the node count.
+  void eval_all(const double* params, size_t np, std::vector<double>& vals) const;
 
  private:
   int intern(const Node& n);

@@ -198,6 +198,11 @@ struct mf_context {
   // device staging for segment tables and parameter rows
   void* stage_dev = nullptr;
   size_t stage_cap = 0;
+  // freed buffer memory kept for reuse (size -> pointer), up to cache_limit
+  // bytes: a server admitting and retiring datasets does not pay a
+  // cudaMalloc / cudaFree (which synchronises the device) for each
+  std::multimap<uint64_t, void*> free_cache;
+  uint64_t cached = 0, cache_limit = 0;
 };
 
 // A copy of a buffer's columns in the layout a REDUCE kernel reads (folded
@@ -255,12 +260,46 @@ void release_context(mf_context* c) {
   if (c->out_host) cudaFreeHost(c->out_host);
   if (c->status_host) cudaFreeHost(c->status_host);
   if (c->stage_dev) cudaFree(c->stage_dev);
+  for (auto& [sz, q] : c->free_cache) cudaFree(q);
   cudaStreamDestroy(c->stream);
   delete c;
 }
 
 
 size_t elem_size(int e) { return e == MF_F32 ? 4 : 8; }
+
+// Device memory for buffers and prepared copies: a cached block of the same
+// rounded size (within 1/8) when one is free, else cudaMalloc; when that
+// fails, the cache is released and the allocation tried once more.
+cudaError_t ctx_malloc(mf_context* c, uint64_t bytes, void** p) {
+  auto it = c->free_cache.lower_bound(bytes);
+  if (it != c->free_cache.end() && it->first <= bytes + bytes / 8) {
+    *p = it->second;
+    c->cached -= it->first;
+    c->free_cache.erase(it);
+    return cudaSuccess;
+  }
+  cudaError_t e = cudaMalloc(p, std::max<uint64_t>(bytes, 256));
+  if (e == cudaErrorMemoryAllocation && !c->free_cache.empty()) {
+    cudaGetLastError();
+    for (auto& [sz, q] : c->free_cache) cudaFree(q);
+    c->free_cache.clear();
+    c->cached = 0;
+    e = cudaMalloc(p, std::max<uint64_t>(bytes, 256));
+  }
+  return e;
+}
+// Returns memory of `bytes` (the size it was allocated with) for reuse; the
+// caller has synchronised the context's stream.
+void ctx_free(mf_context* c, void* p, uint64_t bytes) {
+  if (!p) return;
+  if (c->cached + bytes <= c->cache_limit) {
+    c->free_cache.emplace(bytes, p);
+    c->cached += bytes;
+  } else {
+    cudaFree(p);
+  }
+}
 
 // Reads (and clears) the kernels' error word after the stream has drained.
 int check_status(mf_context* c) {
@@ -364,7 +403,7 @@ int prepare_input(const mf_kernel* k, const mf_buffer* in, uint64_t stride, cons
                                      " bytes) exceeds the HBM budget");
     if (d && d->ptr) {
       MF_CUDA_TRY(cudaStreamSynchronize(c->stream));
-      cudaFree(d->ptr);
+      ctx_free(c, d->ptr, d->bytes);
       c->allocated -= d->bytes;
       d->ptr = nullptr;
       d->bytes = 0;
@@ -374,7 +413,7 @@ int prepare_input(const mf_kernel* k, const mf_buffer* in, uint64_t stride, cons
       d = &in->derived.back();
       d->key = k->prep_key;
     }
-    MF_CUDA_TRY(cudaMalloc(&d->ptr, std::max<uint64_t>(need, 256)));
+    MF_CUDA_TRY(ctx_malloc(c, need, &d->ptr));
     d->bytes = need;
     c->allocated += need;
   }
@@ -395,7 +434,7 @@ int prepare_input(const mf_kernel* k, const mf_buffer* in, uint64_t stride, cons
 void free_derived(const mf_buffer* b) {
   for (auto& d : b->derived)
     if (d.ptr) {
-      cudaFree(d.ptr);
+      ctx_free(b->ctx, d.ptr, d.bytes);
       b->ctx->allocated -= d.bytes;
     }
   b->derived.clear();
@@ -440,6 +479,7 @@ int mf_context_create(int device, uint64_t hbm_budget_bytes, mf_context** out) {
   c->device = device;
   c->num_sms = prop.multiProcessorCount;
   c->budget = hbm_budget_bytes;
+  c->cache_limit = hbm_budget_bytes ? hbm_budget_bytes / 4 : (uint64_t(8) << 30);
   MF_CUDA_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
   MF_CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&c->counter), sizeof(unsigned)));
   MF_CUDA_TRY(cudaMemset(c->counter, 0, sizeof(unsigned)));
@@ -484,7 +524,7 @@ int mf_buffer_alloc(mf_context* c, uint64_t nbytes, mf_buffer** out) {
   auto b = std::make_unique<mf_buffer>();
   b->ctx = c;
   b->size = nbytes;
-  MF_CUDA_TRY(cudaMalloc(&b->ptr, std::max<uint64_t>(rounded, 256)));
+  MF_CUDA_TRY(ctx_malloc(c, std::max<uint64_t>(rounded, 256), &b->ptr));
   c->allocated += rounded;
   c->refs++;
   *out = b.release();
@@ -497,7 +537,7 @@ int mf_buffer_free(mf_buffer* b) {
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
   free_derived(b);
-  cudaFree(b->ptr);
+  ctx_free(c, b->ptr, std::max<uint64_t>((b->size + 255) & ~uint64_t(255), 256));
   c->allocated -= (b->size + 255) & ~uint64_t(255);
   delete b;
   release_context(c);
@@ -741,6 +781,49 @@ int mf_eval_expressions_batch(uint32_t n_names, const char* const* names, uint32
   } catch (const std::exception& e) {
     return fail(MF_ERR_PARSE, e.what());
   }
+  return MF_OK;
+}
+
+}  // extern "C"
+
+struct mf_expr_set {
+  mf::Dag dag;
+  std::vector<int> roots;
+  uint32_t n_names = 0;
+  mf_expr_set(const std::vector<std::string>& names) : dag({}, names), n_names(uint32_t(names.size())) {}
+};
+
+extern "C" {
+
+int mf_expr_set_create(uint32_t n_names, const char* const* names, uint32_t n_exprs, const char* const* exprs,
+                       mf_expr_set** out) {
+  if (!out || (n_names && !names) || (n_exprs && !exprs)) return fail(MF_ERR_INVALID, "null argument");
+  *out = nullptr;
+  std::vector<std::string> nm;
+  for (uint32_t i = 0; i < n_names; i++) nm.push_back(names[i] ? names[i] : "");
+  try {
+    auto set = std::make_unique<mf_expr_set>(nm);
+    for (uint32_t i = 0; i < n_exprs; i++) set->roots.push_back(set->dag.parse(exprs[i] ? exprs[i] : ""));
+    *out = set.release();
+  } catch (const std::exception& e) {
+    return fail(MF_ERR_PARSE, e.what());
+  }
+  return MF_OK;
+}
+
+int mf_expr_set_eval(const mf_expr_set* set, uint32_t n_rows, const double* values, double* out) {
+  if (!set || (n_rows && (!out || (set->n_names && !values)))) return fail(MF_ERR_INVALID, "null argument");
+  std::vector<double> v;
+  const size_t ne = set->roots.size();
+  for (uint32_t r = 0; r < n_rows; r++) {
+    set->dag.eval_all(values + size_t(r) * set->n_names, set->n_names, v);
+    for (size_t i = 0; i < ne; i++) out[size_t(r) * ne + i] = v[set->roots[i]];
+  }
+  return MF_OK;
+}
+
+int mf_expr_set_free(mf_expr_set* set) {
+  delete set;
   return MF_OK;
 }
 

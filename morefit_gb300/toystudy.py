@@ -62,11 +62,7 @@ class SegmentLikelihood:
         self.evaluations = 0
 
     def _rows(self, kernel: str, theta: np.ndarray) -> np.ndarray:
-        bufs = self.like.buffers[kernel]
-        if not bufs:
-            return theta
-        extra = eval_expressions_batch(self.params, theta, [e for _, e in bufs])
-        return np.concatenate([theta, extra], axis=1)
+        return self.like.param_rows(kernel, theta)
 
     def _submit(self, kernel: str, idx: np.ndarray, theta: np.ndarray) -> np.ndarray:
         self.evaluations += 1

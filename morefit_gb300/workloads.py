@@ -25,7 +25,7 @@ import numpy as np
 import ctypes as C
 
 from . import _lib as L
-from .backend import CUDABackend, CUDABlock, DeviceColumns, eval_expressions
+from .backend import CUDABackend, CUDABlock, DeviceColumns, ExpressionSet
 
 DEFAULT_SEED = 229387429
 MAX_GENERATOR_WORKITEMS = 8192  # compute_options::opencl_max_generator_workitems (compute.hh:59)
@@ -129,12 +129,22 @@ class Likelihood:
     def input_block(self, kernel: str = "lh_grad_kernel") -> DeviceColumns:
         return self.blocks[kernel].input
 
+    def _exprs(self, kernel: str) -> ExpressionSet:
+        cache = self.__dict__.setdefault("_expr_sets", {})
+        if kernel not in cache:
+            cache[kernel] = ExpressionSet(self.params, [e for _, e in self.buffers[kernel]])
+        return cache[kernel]
+
     def param_vector(self, kernel: str, theta) -> np.ndarray:
         """[floating values..., parameter buffers...] as the fitter builds it (fitter.hh:1059-1072)."""
-        theta = np.asarray(theta, dtype=np.float64)
-        bufs = self.buffers[kernel]
-        extra = eval_expressions(self.params, theta, [e for _, e in bufs]) if bufs else np.zeros(0)
-        return np.concatenate([theta, extra])
+        return self.param_rows(kernel, np.asarray(theta, dtype=np.float64)[None, :])[0]
+
+    def param_rows(self, kernel: str, thetas) -> np.ndarray:
+        """param_vector for every row of ``thetas`` (n, n_floating)."""
+        th = np.atleast_2d(np.asarray(thetas, dtype=np.float64))
+        if not self.buffers[kernel]:
+            return th.copy()
+        return np.concatenate([th, self._exprs(kernel).eval(th)], axis=1)
 
     def sums(self, kernel: str, theta=None, param_vector=None) -> np.ndarray:
         b = self.blocks[kernel]

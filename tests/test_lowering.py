@@ -121,3 +121,17 @@ def test_spwave_folds_with_parameter_definitions():
     assert "// reads 15 prepared columns (FP64 as float pairs) derived from 17 source columns" in with_defs
     without = lower_source("g", L.MF_KERNEL_REDUCE, L.MF_F64, k["inputs"], k["params"], k["exprs"])
     assert "// reads 16 prepared columns" in without
+
+
+def test_expression_set_matches_single_evaluation():
+    """mf_expr_set (parsed once, evaluated per row) gives the values of
+    mf_eval_expressions row by row (host only)."""
+    import numpy as np
+    from morefit_gb300.backend import ExpressionSet, eval_expressions
+    g = load_golden("spwave_n2000.json")
+    names = g["parameters"]
+    exprs = [e for _, e in g["hessian_buffers"]]
+    rows = np.array(g["truth"]) * (1.0 + np.random.default_rng(3).uniform(-0.2, 0.2, (7, len(names))))
+    got = ExpressionSet(names, exprs).eval(rows)
+    for r in range(len(rows)):
+        assert np.array_equal(got[r], eval_expressions(names, rows[r], exprs))
