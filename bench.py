@@ -55,7 +55,7 @@ def _peaks():
 # dram__bytes_read.sum + dram__bytes_write.sum of one lh_grad launch (FP64
 # storage, double-float arithmetic, 9 prepared columns, 1M events) from the
 # full ncu capture summarised in profiles/mf_reduce_lh_grad_pwave_1M.md.
-NCU_TRAFFIC_F64 = 72.052224e6 + 0.556544e6
+NCU_TRAFFIC_F64 = 72.046336e6 + 0.542976e6
 NCU_TRAFFIC_SOURCE = "ncu --set full, one launch, profiles/mf_reduce_lh_grad_pwave_1M.md"
 
 
