@@ -10,16 +10,23 @@ def _src(g, name, elem, kind=0, native_f64=False):
     return lower_source(name, kind, elem, k["inputs"], k["params"], k["exprs"], native_f64=native_f64)
 
 
+def _entry(src, head):
+    """Text of one entry point: from its name to the next entry."""
+    i = src.index(head)
+    j = src.find('extern "C"', i)
+    return src[i:] if j < 0 else src[i:j]
+
+
 def test_shared_subexpressions_evaluated_once():
     from morefit_gb300 import _lib as L
     g = load_golden("pwave_n1000.json")
     src = _src(g, "lh_grad_kernel", L.MF_F64, native_f64=True)
-    body = src[src.index("mf_reduce("):src.index("mf_reduce_segments(")]
+    body = _entry(src, "mf_reduce(")
     # one density, one log and one reciprocal per event (vector width 2)
     assert body.count("= log(") == 2
     assert body.count("__drcp_rn(") == 2
     dw = _src(g, "lh_grad_kernel", L.MF_F64)
-    body = dw[dw.index("void __launch_bounds__(MF_BLOCK) mf_reduce("):dw.index("mf_reduce_segments(")]
+    body = _entry(dw, "void __launch_bounds__(MF_BLOCK) mf_reduce(")
     # double-float kernel: two events per thread, one log and one reciprocal each
     assert body.count("mf_dw_log(") == 2 and body.count("mf_dw_rcp(") == 2
     assert " log(" not in body
@@ -60,7 +67,7 @@ def test_hessian_kernel_shares_the_density():
     from morefit_gb300 import _lib as L
     g = load_golden("pwave_n1000.json")
     src = _src(g, "lh_hessian_kernel", L.MF_F64, native_f64=True)
-    body = src[src.index("mf_reduce("):src.index("mf_reduce_segments(")]
+    body = _entry(src, "mf_reduce(")
     assert body.count("__drcp_rn(") <= 4  # 1/p and 1/p^2, twice for the two vector lanes
 
 
@@ -68,7 +75,7 @@ def test_float_kernels_use_float_literals_and_functions():
     from morefit_gb300 import _lib as L
     g = load_golden("mass_n1000.json")
     src = _src(g, "lh_grad_kernel", L.MF_F32)
-    body = src[src.index("mf_reduce("):src.index("mf_reduce_segments(")]
+    body = _entry(src, "mf_reduce(")
     assert "expf(" in body and "logf(" in body
     assert " exp(" not in body and " log(" not in body
     assert "double2" not in body and "float4" in body
