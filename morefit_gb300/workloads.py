@@ -14,6 +14,12 @@ parameter-buffer expressions evaluated on the host before every launch.
 d2logp/dtheta_i dtheta_j (fitter.hh:1221-1326). The event block is uploaded
 once (fitter.hh:704-757) and every evaluation moves only the parameter
 vector in and the sums out.
+
+Weighted data (a spec with a ``weight`` column): the reference multiplies
+log p by the weight column (fitter.hh:337-338), builds the Fisher kernel
+d(w log p)/dtheta_i * d(w log p)/dtheta_j (fitter.hh:471-523), and corrects
+the covariance to -2 H^-1 F H^-1 (fitter.hh:894-943). ``fisher()`` and
+``corrected_covariance()`` restate those two steps.
 """
 from __future__ import annotations
 
@@ -37,6 +43,14 @@ def load_spec(name: str) -> dict:
     return json.loads((SPEC_DIR / f"{name}.json").read_text())
 
 
+def weighted_covariance(hessian: np.ndarray, fisher: np.ndarray) -> np.ndarray:
+    """-2 H^-1 F H^-1 from H = -2 sum d2(w log p) and F = -2 sum d(w log p) d(w log p)
+    (fitter.hh:931-933): the sandwich (sum w d2 log p)^-1 (sum w^2 d log p d log p)
+    (sum w d2 log p)^-1 in the fitter's -2 ln L convention."""
+    hinv = np.linalg.inv(np.asarray(hessian, dtype=np.float64))
+    return -2.0 * hinv @ np.asarray(fisher, dtype=np.float64) @ hinv
+
+
 class Likelihood:
     """NLL, gradient and Hessian of one dataset, device resident."""
 
@@ -50,7 +64,9 @@ class Likelihood:
         self.kspec = ks
         self.has_precompute = "precompute_kernel" in ks
         self.buffers = {"lh_kernel": spec["lh_buffers"], "lh_grad_kernel": spec["grad_buffers"],
-                        "lh_hessian_kernel": spec["hessian_buffers"]}
+                        "lh_hessian_kernel": spec["hessian_buffers"],
+                        "lh_fisher_kernel": spec.get("fisher_buffers", [])}
+        self.weight = spec.get("weight")
         # Blocks as the fitter wires them (fitter.hh:525-657, 704-757). In
         # mixed precision the hoisted basis columns are stored in FP32; a model
         # without them reads its raw observables, which keep FP64 storage with
@@ -59,7 +75,7 @@ class Likelihood:
         # The precompute runs in double-float (FP32 pipe) unless native FP64 is asked for.
         self.pre = CUDABlock(backend, np.float64 if mixed_raw else kernelT, native_f64=native_f64)
         self.blocks = {}
-        for name in ("lh_kernel", "lh_grad_kernel", "lh_hessian_kernel"):
+        for name in ("lh_kernel", "lh_grad_kernel", "lh_hessian_kernel", "lh_fisher_kernel"):
             if name not in ks:
                 continue
             b = CUDABlock(backend, kernelT, native_f64=native_f64, vec=vec, block=block, f32_arith=mixed_raw,
@@ -160,8 +176,8 @@ class Likelihood:
         s = self.sums("lh_grad_kernel", theta)
         return -2.0 * float(s[0]), -2.0 * s[1:]
 
-    def hessian(self, theta) -> np.ndarray:
-        s = self.sums("lh_hessian_kernel", theta)
+    def _symmetric(self, s: np.ndarray) -> np.ndarray:
+        """-2 * the lower-triangle sums (row i, columns j <= i) as a full matrix."""
         npar = len(self.params)
         h = np.zeros((npar, npar))
         idx = 0
@@ -170,6 +186,58 @@ class Likelihood:
                 h[i, j] = h[j, i] = -2.0 * s[idx]
                 idx += 1
         return h
+
+    def hessian(self, theta) -> np.ndarray:
+        return self._symmetric(self.sums("lh_hessian_kernel", theta))
+
+    def fisher(self, theta) -> np.ndarray:
+        """-2 sum d(w log p)/dtheta_i d(w log p)/dtheta_j (fitter.hh:1328-1370)."""
+        if "lh_fisher_kernel" not in self.blocks:
+            raise ValueError("the model has no Fisher kernel (unweighted data)")
+        return self._symmetric(self.sums("lh_fisher_kernel", theta))
+
+    def corrected_covariance(self, theta) -> np.ndarray:
+        """Covariance of a weighted fit at theta (fitter.hh:894-943)."""
+        return weighted_covariance(self.hessian(theta), self.fisher(theta))
+
+    def fit(self, theta0=None, limits=None, tol: float = 1e-9):
+        """Minimises -2 ln L of the whole dataset from theta0 (default: the
+        spec's truth) within limits (default: none) by damped Newton steps
+        on the analytic gradient and Hessian, the derivative information the
+        reference's MIGRAD + HESSE run uses (fitter.hh:659-1000). Errors come
+        from 2 H^-1 (errordef 1), or for weighted data from the corrected
+        covariance, as the reference reports them (fitter.hh:894-994).
+        Returns a FitResult with one row."""
+        from .toystudy import fit_segments
+        th0 = np.asarray(self.spec["truth"] if theta0 is None else theta0, dtype=np.float64)[None, :]
+        lim = limits if limits is not None else [(-np.inf, np.inf)] * len(self.params)
+        r = fit_segments(_WholeDataset(self), th0, lim, tol=tol)
+        if self.weight is not None:
+            r.errors[0] = np.sqrt(np.abs(np.diag(self.corrected_covariance(r.values[0]))))
+        return r
+
+
+class _WholeDataset:
+    """The batched-fit interface (value, value_and_gradient, hessian of rows
+    of parameters) over one whole dataset through the full-grid kernels."""
+
+    def __init__(self, like: Likelihood):
+        self.like = like
+        self.params = like.params
+        self.evaluations = 0
+
+    def value(self, idx, theta):
+        self.evaluations += len(theta)
+        return np.array([self.like.likelihood(t) for t in theta])
+
+    def value_and_gradient(self, idx, theta):
+        self.evaluations += len(theta)
+        fg = [self.like.likelihood_and_gradient(t) for t in theta]
+        return np.array([f for f, _ in fg]), np.array([g for _, g in fg])
+
+    def hessian(self, idx, theta):
+        self.evaluations += len(theta)
+        return np.array([self.like.hessian(t) for t in theta])
 
 
 def seed_rows(nrows: int, seed: int = DEFAULT_SEED) -> np.ndarray:

@@ -58,8 +58,18 @@ def lib():
     return _lib
 
 
+def mass_weights(n: int) -> np.ndarray:
+    """Event weights of the weighted mass workload, w_i = 0.5 + frac(i * 0.6180339887498949)
+    (the column oracle/refkit appends after generation)."""
+    f = np.arange(n, dtype=np.float64) * 0.6180339887498949
+    return 0.5 + (f - np.floor(f))
+
+
 def generate(workload: str, n: int, truth=None, seed: int = SEED, nthreads: int = 1) -> np.ndarray:
-    """Seeded accept-reject events, shape (ndims, n), as the reference generates them."""
+    """Seeded accept-reject events, shape (ndims, n), as the reference generates them
+    (the weighted mass workload: the mass events plus the weight column)."""
+    if workload == "mass_w":
+        return np.vstack([generate("mass", n, truth, seed, nthreads), mass_weights(n)[None, :]])
     w = 0 if workload == "mass" else 1
     th = np.asarray(truth if truth is not None else (MASS_TRUTH if w == 0 else PWAVE_TRUTH), dtype=np.float64)
     lo, hi = (MASS_RANGE if w == 0 else PWAVE_RANGE)

@@ -343,12 +343,13 @@ struct Workload {
   std::vector<parameter<eT>*> params;
   PDF<kT, eT>* pdf;
   bool optimize_dimensions;
+  dimension<eT>* weight = nullptr;  // event weight column appended after generation
 };
 
 static Workload make_workload(const std::string& which) {
   Workload w;
   w.name = which;
-  if (which == "mass") {
+  if (which == "mass" || which == "mass_w") {
     auto* m = new dimension<eT>("m", "m", 5000.0, 5600.0, false);
     auto* mb = new parameter<eT>("mb", "mb", 5280.0, 5200.0, 5400.0, 1.0, false);
     auto* sigma = new parameter<eT>("sigma", "sigma", 20.0, 5.0, 50.0, 0.5, false);
@@ -360,6 +361,7 @@ static Workload make_workload(const std::string& which) {
     w.dims = {m};
     w.params = {mb, sigma, fsig, alpha};
     w.optimize_dimensions = false;
+    if (which == "mass_w") w.weight = new dimension<eT>("w", "w", 0.0, 2.0, false);
   } else if (which == "pwave") {
     auto* ctl = new dimension<eT>("ctl", "ctl", -1.0, 1.0, false);
     auto* ctk = new dimension<eT>("ctk", "ctk", -1.0, 1.0, false);
@@ -408,6 +410,10 @@ static fitter_options make_fit_opts(const Workload& w) {
   o.kahan_on_accelerator = true;
   o.print_level = 0;
   o.minuit_printlevel = 0;
+  // Weighted data: the analytic Fisher kernel and the covariance correction
+  // -2 H^-1 F H^-1 (fitter.hh:894-943; correct_weighted_fit defaults to true).
+  o.analytic_fisher = w.weight != nullptr;
+  o.correct_weighted_fit = true;
   return o;
 }
 
@@ -417,6 +423,18 @@ static void generate(Workload& w, backendT* backend, Xoshiro128pp* rnd, unsigned
   gen_opts.print_level = 0;
   generator<kT, eT, backendT, blockT> gen(&gen_opts, backend, rnd);
   gen.generate(n, w.pdf, w.params, out);
+  if (w.weight) {
+    // Weights w_i = 0.5 + frac(i * 0.6180339887498949) in [0.5, 1.5), a
+    // deterministic sequence uncorrelated with the generated events.
+    out.add_dimensions({w.weight});
+    const unsigned d = out.ndimensions() - 1;
+    for (unsigned i = 0; i < n; i++) {
+      double f = double(i) * 0.6180339887498949;
+      f -= std::floor(f);
+      out(i, d) = 0.5 + f;
+    }
+    out.set_event_weight(w.weight->get_name());
+  }
 }
 
 // Parses "<prefix><name> = <expr>" lines printed by fitter::make_kernels at print_level 2.
@@ -499,11 +517,16 @@ static int cmd_golden(const std::string& which, unsigned n, const std::string& o
     double nll2 = fit.likelihood_and_gradient(npar, grad.data());
     std::vector<double> h(npar * npar);
     fit.hessian(npar, h.data());
+    std::vector<double> fm;
+    if (w.weight) {
+      fm.resize(size_t(npar) * npar);
+      fit.fisher(w.pdf, w.params, &data, npar, fm.data());
+    }
     std::cout.rdbuf(old);
     g_capture = nullptr;
     pts += std::string(k ? "," : "") + "{\"params\":" + jvec(points[k]) + ",\"nll\":" + jnum(nll) +
            ",\"nll_from_grad_kernel\":" + jnum(nll2) + ",\"grad\":" + jvec(grad) + ",\"hessian\":" + jvec(h) +
-           ",\"kernel_params\":{";
+           (w.weight ? ",\"fisher\":" + jvec(fm) : std::string()) + ",\"kernel_params\":{";
     bool first = true;
     for (auto& kv : cap.params) {
       pts += std::string(first ? "" : ",") + jstr(kv.first) + ":" + jvec(kv.second);
@@ -534,6 +557,7 @@ static int cmd_golden(const std::string& which, unsigned n, const std::string& o
   kern += "]";
   std::vector<std::string> dnames, pnames;
   for (auto* d : w.dims) dnames.push_back(d->get_name());
+  if (w.weight) dnames.push_back(w.weight->get_name());
   for (auto* p : w.params) pnames.push_back(p->get_name());
   char hash[32];
   std::snprintf(hash, sizeof hash, "%016llx", (unsigned long long)ev_hash);
@@ -544,7 +568,11 @@ static int cmd_golden(const std::string& which, unsigned n, const std::string& o
                    ",\"event_buffers\":" + jpairs(grab(log, "EVENTBUFFER ")) +
                    ",\"lh_buffers\":" + jpairs(grab(log, "BUFFER ")) +
                    ",\"grad_buffers\":" + jpairs(grab(log, "GRADBUFFER: ")) +
-                   ",\"hessian_buffers\":" + jpairs(grab(log, "HESSIANBUFFER: ")) + ",\"fit\":{\"values\":" +
+                   ",\"hessian_buffers\":" + jpairs(grab(log, "HESSIANBUFFER: ")) +
+                   (w.weight ? ",\"weight\":" + jstr(w.weight->get_name()) +
+                                   ",\"fisher_buffers\":" + jpairs(grab(log, "FISHERBUFFER: "))
+                             : std::string()) +
+                   ",\"fit\":{\"values\":" +
                    jvec(values) + ",\"errors\":" + jvec(errors) + ",\"wall_ms\":" +
                    jnum(std::chrono::duration<double, std::milli>(t1 - t0).count()) + "},\"points\":" + pts + "}\n";
   FILE* f = std::fopen(out_json.c_str(), "w");
@@ -666,7 +694,7 @@ int main(int argc, char** argv) {
                      unsigned(std::stoul(argv[5])));
   if (argc >= 7 && std::string(argv[1]) == "toys")
     return cmd_toys(argv[2], unsigned(std::stoul(argv[3])), std::stod(argv[4]), std::stod(argv[5]), argv[6]);
-  std::fprintf(stderr, "usage: refkit golden <mass|pwave|spwave> <n> <out.json> [events.bin]\n"
+  std::fprintf(stderr, "usage: refkit golden <mass|mass_w|pwave|spwave> <n> <out.json> [events.bin]\n"
                        "       refkit bench <mass|pwave|spwave> <n> <nthreads> <nevals>\n"
                        "       refkit toys <pwave> <ntoys> <mean events> <jitter> <out.json>\n");
   return 2;

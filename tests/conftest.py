@@ -23,7 +23,7 @@ def load_golden(name: str) -> dict:
 
 def golden_events(workload: str, n: int) -> np.ndarray:
     raw = np.fromfile(GOLDEN / f"{workload}_n{n}_events.f64", dtype=np.float64)
-    ndim = 1 if workload == "mass" else 3
+    ndim = {"mass": 1, "mass_w": 2}.get(workload, 3)
     return raw.reshape(ndim, n)
 
 

@@ -10,7 +10,7 @@ from conftest import assert_sums_close, golden_events, kernel_spec, load_golden
 from oracle.spec_kernel import SpecKernel
 
 
-@pytest.mark.parametrize("workload,n", [("pwave", 1000), ("mass", 1000)])
+@pytest.mark.parametrize("workload,n", [("pwave", 1000), ("mass", 1000), ("mass_w", 1000)])
 def test_generator_reproduces_reference_events(oracle_lib, workload, n):
     ev = oracle_lib.generate(workload, n)
     ref = golden_events(workload, n)
@@ -18,7 +18,7 @@ def test_generator_reproduces_reference_events(oracle_lib, workload, n):
     assert oracle_lib.fnv1a(ev) == load_golden(f"{workload}_n{n}.json")["events_fnv1a"]
 
 
-@pytest.mark.parametrize("workload,n", [("mass", 100000), ("pwave", 1000000)])
+@pytest.mark.parametrize("workload,n", [("mass", 100000), ("mass_w", 100000), ("pwave", 1000000)])
 def test_generator_hash_at_full_size(oracle_lib, workload, n):
     ev = oracle_lib.generate(workload, n)
     assert oracle_lib.fnv1a(ev) == load_golden(f"{workload}_n{n}.json")["events_fnv1a"]
@@ -40,11 +40,13 @@ def _inputs_for(g, events, spec_name):
     return events
 
 
-@pytest.mark.parametrize("workload", ["pwave", "mass"])
+@pytest.mark.parametrize("workload", ["pwave", "mass", "mass_w"])
 def test_spec_kernel_reproduces_reference_sums(oracle_lib, workload):
     g = load_golden(f"{workload}_n1000.json")
     ev = golden_events(workload, 1000)
-    for name in ("lh_kernel", "lh_grad_kernel", "lh_hessian_kernel"):
+    names = [k["name"] for k in g["kernels"] if k["name"].startswith("lh_")]
+    assert ("lh_fisher_kernel" in names) == (workload == "mass_w")
+    for name in names:
         sk = SpecKernel(kernel_spec(g, name))
         cols = _inputs_for(g, ev, name)
         for pt in g["points"]:
@@ -91,3 +93,19 @@ def test_closed_form_pwave_full_size(oracle_lib):
     got = oracle_lib.pwave_nll_grad(basis, pt["params"], nthreads=4)
     ref = np.array(pt["kernel_sums"]["lh_grad_kernel"])
     assert_sums_close(got, ref, np.full(9, 1e6), rtol=1e-11, stol=1e-13, what="pwave 1M closed form")
+
+
+@pytest.mark.parametrize("n", [1000, 100000])
+def test_weighted_covariance_reproduces_reference_errors(n):
+    """The reference's weighted fit reports sqrt(diag(-2 H^-1 F H^-1)) at its
+    minimum (fitter.hh:894-994); H and F at that point are in the golden file."""
+    from morefit_gb300.workloads import weighted_covariance
+    g = load_golden(f"mass_w_n{n}.json")
+    pt = g["points"][1]
+    assert pt["params"] == g["fit"]["values"]
+    npar = len(g["parameters"])
+    cov = weighted_covariance(np.reshape(pt["hessian"], (npar, npar)), np.reshape(pt["fisher"], (npar, npar)))
+    np.testing.assert_allclose(np.sqrt(np.diag(cov)), g["fit"]["errors"], rtol=1e-9)
+    # the correction is not the unweighted 2 H^-1
+    plain = np.sqrt(np.diag(2.0 * np.linalg.inv(np.reshape(pt["hessian"], (npar, npar)))))
+    assert np.abs(plain / np.array(g["fit"]["errors"]) - 1.0).max() > 0.01
