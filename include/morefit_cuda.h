@@ -180,7 +180,15 @@ typedef struct mf_kernel_desc {
 /* FP64 REDUCE kernels evaluate the per-event expressions in double-float
  * arithmetic (pairs of FP32 values, ~48-bit significand, with FP64 sums) by
  * default, because GB300 issues FP32 at 64x its FP64 rate; this flag selects
- * native FP64 arithmetic instead. */
+ * native FP64 arithmetic instead. A double-float value has FP32's exponent
+ * range (|x| up to 3.4e38): when mf_kernel_reduce or
+ * mf_kernel_reduce_segments gets a non-finite sum from a double-float
+ * kernel (an intermediate such as pow(x, n)^4 overflowed), it evaluates the
+ * same launch (or the affected segments) again with a native-FP64 build of
+ * the kernel, made on first need, and returns those sums
+ * (mf_kernel_fallback_count counts such calls). The asynchronous and batched
+ * entry points (mf_kernel_reduce_async, mf_kernel_reduce_many) return the
+ * double-float sums as they are. */
 #define MF_FLAG_NATIVE_F64 1u
 /* FP64 columns, FP32 per-event arithmetic with FP64 sums (the mixed-precision
  * form for raw observables that need their FP64 storage, e.g. a mass with a
@@ -286,6 +294,11 @@ int mf_context_stream(mf_context* ctx, void** stream);
 int mf_kernel_reduce_segments(mf_kernel* k, const mf_buffer* input, uint64_t stride, uint32_t nseg,
                               const uint64_t* seg_begin, const uint32_t* seg_count, const double* params,
                               uint32_t n_params, double* sums);
+
+/* How many mf_kernel_reduce / mf_kernel_reduce_segments calls on `k` were
+ * evaluated again in native FP64 because a double-float sum was not finite
+ * (see MF_FLAG_NATIVE_F64). */
+int mf_kernel_fallback_count(const mf_kernel* k, uint64_t* count);
 
 /* STORE: output column j of `output` (stride out_stride) receives output j
  * for events [0, n). Replaces SubmitKernel for non-Kahan and precompute

@@ -141,6 +141,12 @@ class Kernel:
         L.check(L.lib.mf_kernel_read_layout(self.handle, C.byref(c), C.byref(b), C.byref(sc)))
         return {"columns": c.value, "bytes_per_event": b.value, "source_columns": sc.value}
 
+    def fallback_count(self) -> int:
+        """Reductions evaluated again in native FP64 after a non-finite double-float sum."""
+        v = C.c_uint64()
+        L.check(L.lib.mf_kernel_fallback_count(self.handle, C.byref(v)))
+        return v.value
+
 
 def make_desc(name: str, kind: int, elem: int, inputs: Sequence[str], params: Sequence[str],
               exprs: Sequence[str], gen=None, native_f64: bool = False, vec: int = 0, block: int = 0,

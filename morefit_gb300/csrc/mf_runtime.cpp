@@ -13,6 +13,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cctype>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -223,6 +224,35 @@ struct mf_buffer {
   mutable std::vector<mf_derived> derived;
 };
 
+// Owned copy of a kernel description (its strings and arrays), kept by
+// double-float REDUCE kernels to build their native-FP64 twin on demand.
+struct DescCopy {
+  std::string name;
+  std::vector<std::string> inputs, params, exprs, defs;
+  std::vector<const char*> p_inputs, p_params, p_exprs, p_defs;
+  mf_kernel_desc d{};
+  explicit DescCopy(const mf_kernel_desc* s) : d(*s) {
+    name = s->name ? s->name : "kernel";
+    for (uint32_t i = 0; i < s->n_inputs; i++) inputs.emplace_back(s->input_names[i]);
+    for (uint32_t i = 0; i < s->n_params; i++) params.emplace_back(s->param_names[i]);
+    for (uint32_t i = 0; i < s->n_outputs; i++) exprs.emplace_back(s->exprs[i]);
+    if (s->param_defs)
+      for (uint32_t i = 0; i < s->n_params; i++) defs.emplace_back(s->param_defs[i] ? s->param_defs[i] : "");
+    for (auto& x : inputs) p_inputs.push_back(x.c_str());
+    for (auto& x : params) p_params.push_back(x.c_str());
+    for (auto& x : exprs) p_exprs.push_back(x.c_str());
+    for (auto& x : defs) p_defs.push_back(x.c_str());
+    d.name = name.c_str();
+    d.input_names = p_inputs.data();
+    d.param_names = p_params.data();
+    d.exprs = p_exprs.data();
+    d.param_defs = s->param_defs ? p_defs.data() : nullptr;
+    d.n_gen_dims = 0;
+    d.gen_dim_names = nullptr;
+    d.gen_lo = d.gen_hi = nullptr;
+  }
+};
+
 struct mf_kernel {
   mf_context* ctx = nullptr;
   std::string name;
@@ -239,6 +269,11 @@ struct mf_kernel {
   int blocks_per_sm = 1;
   int max_input = -1;
   bool holds_ref = false;  // counted in ctx->refs
+  // Double-float REDUCE kernels: the description, and the native-FP64 build
+  // of it that re-evaluates launches whose sums came out non-finite.
+  std::unique_ptr<DescCopy> desc;
+  mf_kernel* f64 = nullptr;
+  uint64_t fallbacks = 0;
 };
 
 namespace mfi {
@@ -688,6 +723,8 @@ int mf_kernel_build(mf_context* c, const mf_kernel_desc* d, mf_kernel** out) {
     return fail(MF_ERR_UNSUPPORTED, "kernel '" + k->name + "' does not fit on an SM (" +
                                         std::to_string(k->lowered.smem_bytes) + " B shared memory)");
   k->blocks_per_sm = std::max(1, nb);
+  if (d->kind == MF_KERNEL_REDUCE && d->elem_type == MF_F64 && !(d->flags & (MF_FLAG_NATIVE_F64 | MF_FLAG_F32_ARITH)))
+    k->desc = std::make_unique<DescCopy>(d);
   c->refs++;
   k->holds_ref = true;
   *out = k.release();
@@ -891,6 +928,7 @@ int mf_compile_check(const mf_kernel_desc* d, int* regs, int* spill) {
 
 int mf_kernel_free(mf_kernel* k) {
   if (!k) return MF_OK;
+  if (k->f64) mf_kernel_free(k->f64);
   mf_context* c = k->ctx;
   if (k->lib) {
     cudaSetDevice(c->device);
@@ -982,6 +1020,24 @@ int launch_reduce(mf_kernel* k, const void* data, uint64_t stride, uint64_t n, c
 
 }  // namespace mfi
 
+namespace {
+bool all_finite(const double* v, size_t n) {
+  for (size_t i = 0; i < n; i++)
+    if (!std::isfinite(v[i])) return false;
+  return true;
+}
+}  // namespace
+
+extern "C" int mf_kernel_build(mf_context* c, const mf_kernel_desc* d, mf_kernel** out);
+
+// The native-FP64 build of a double-float REDUCE kernel, made on first use.
+static int f64_twin(mf_kernel* k) {
+  if (k->f64) return MF_OK;
+  mf_kernel_desc d = k->desc->d;
+  d.flags |= MF_FLAG_NATIVE_F64;
+  return mf_kernel_build(k->ctx, &d, &k->f64);
+}
+
 extern "C" {
 
 int mf_kernel_reduce(mf_kernel* k, const mf_buffer* in, uint64_t stride, uint64_t n, const double* params,
@@ -1010,7 +1066,14 @@ int mf_kernel_reduce(mf_kernel* k, const mf_buffer* in, uint64_t stride, uint64_
   if (rc) return rc;
   MF_CUDA_TRY(cudaStreamSynchronize(c->stream));
   std::memcpy(sums, c->out_host, k->n_outputs * sizeof(double));
-  return check_status(c);
+  rc = check_status(c);
+  if (rc || !k->desc || all_finite(sums, k->n_outputs)) return rc;
+  // A double-float intermediate left the FP32 exponent range (|x| > 3.4e38
+  // or a quotient of underflowed values): the same launch in native FP64.
+  rc = f64_twin(k);
+  if (rc) return rc;
+  k->fallbacks++;
+  return mf_kernel_reduce(k->f64, in, stride, n, params, n_params, sums);
 }
 
 int mf_kernel_reduce_async(mf_kernel* k, const mf_buffer* in, uint64_t stride, uint64_t n, const double* params,
@@ -1157,6 +1220,35 @@ int mf_kernel_reduce_segments(mf_kernel* k, const mf_buffer* in, uint64_t stride
                                c->stream));
   MF_CUDA_TRY(cudaStreamSynchronize(c->stream));
   std::memcpy(sums, c->out_host, size_t(nseg) * k->n_outputs * sizeof(double));
+  if (!k->desc) return MF_OK;
+  // Segments whose double-float sums are non-finite: again in native FP64.
+  std::vector<uint32_t> bad;
+  for (uint32_t s = 0; s < nseg; s++)
+    if (!all_finite(sums + size_t(s) * k->n_outputs, k->n_outputs)) bad.push_back(s);
+  if (bad.empty()) return MF_OK;
+  rc = f64_twin(k);
+  if (rc) return rc;
+  k->fallbacks++;
+  std::vector<uint64_t> b2(bad.size());
+  std::vector<uint32_t> c2(bad.size());
+  std::vector<double> p2(bad.size() * n_params), s2(bad.size() * k->n_outputs);
+  for (size_t i = 0; i < bad.size(); i++) {
+    b2[i] = seg_begin[bad[i]];
+    c2[i] = seg_count[bad[i]];
+    std::copy(params + size_t(bad[i]) * n_params, params + size_t(bad[i] + 1) * n_params, p2.begin() + i * n_params);
+  }
+  rc = mf_kernel_reduce_segments(k->f64, in, stride, uint32_t(bad.size()), b2.data(), c2.data(), p2.data(), n_params,
+                                 s2.data());
+  if (rc) return rc;
+  for (size_t i = 0; i < bad.size(); i++)
+    std::copy(s2.begin() + i * k->n_outputs, s2.begin() + (i + 1) * k->n_outputs,
+              sums + size_t(bad[i]) * k->n_outputs);
+  return MF_OK;
+}
+
+int mf_kernel_fallback_count(const mf_kernel* k, uint64_t* count) {
+  if (!k || !count) return fail(MF_ERR_INVALID, "null argument");
+  *count = k->fallbacks;
   return MF_OK;
 }
 

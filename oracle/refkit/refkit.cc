@@ -362,6 +362,26 @@ static Workload make_workload(const std::string& which) {
     w.params = {mb, sigma, fsig, alpha};
     w.optimize_dimensions = false;
     if (which == "mass_w") w.weight = new dimension<eT>("w", "w", 0.0, 2.0, false);
+  } else if (which == "cbpoly") {
+    // Crystal Ball peak over a quadratic background on a normalised mass
+    // x in [-1, 1]: conditionals, pow with a parameter exponent and the
+    // polynomial's Horner form. The background 1 - 0.3 x + 0.1 x^2 falls
+    // monotonically on the range, so PolynomialPDF::get_max's bound (range
+    // limits only) holds.
+    auto* x = new dimension<eT>("x", "x", -1.0, 1.0, false);
+    auto* mu = new parameter<eT>("mu", "mu", 0.1, -0.2, 0.4, 0.001, false);
+    auto* sigma = new parameter<eT>("sigma", "sigma", 0.05, 0.01, 0.2, 0.001, false);
+    auto* alpha = new parameter<eT>("alpha", "alpha", 1.5, 0.5, 5.0, 0.01, false);
+    auto* nn = new parameter<eT>("n", "n", 3.0, 1.5, 10.0, 0.05, false);
+    auto* c1 = new parameter<eT>("c1", "c1", -0.3, -1.0, 1.0, 0.01, false);
+    auto* c2 = new parameter<eT>("c2", "c2", 0.1, -1.0, 1.0, 0.01, false);
+    auto* fsig = new parameter<eT>("fsig", "fsig", 0.3, 0.0, 1.0, 0.01, false);
+    auto* cb = new CrystalballPDF<kT, eT>(x, mu, sigma, alpha, nn);
+    auto* poly = new PolynomialPDF<kT, eT>(x, {c1, c2});
+    w.pdf = new SumPDF<kT, eT>(cb, poly, fsig);
+    w.dims = {x};
+    w.params = {mu, sigma, alpha, nn, c1, c2, fsig};
+    w.optimize_dimensions = false;
   } else if (which == "pwave") {
     auto* ctl = new dimension<eT>("ctl", "ctl", -1.0, 1.0, false);
     auto* ctk = new dimension<eT>("ctk", "ctk", -1.0, 1.0, false);
@@ -503,7 +523,11 @@ static int cmd_golden(const std::string& which, unsigned n, const std::string& o
   std::vector<std::vector<double>> points = {truth, values};
   {
     std::vector<double> d = truth;
-    for (int i = 0; i < npar; i++) d[i] = truth[i] + 0.5 * errors[i] * ((i % 2) ? -1.0 : 1.0);
+    // half an error from the truth, alternating in sign, kept within each
+    // parameter's limits (a poorly constrained parameter would leave them)
+    for (int i = 0; i < npar; i++)
+      d[i] = std::min(std::max(truth[i] + 0.5 * errors[i] * ((i % 2) ? -1.0 : 1.0), w.params[i]->get_min()),
+                      w.params[i]->get_max());
     points.push_back(d);
   }
   std::string pts = "[";
@@ -694,7 +718,7 @@ int main(int argc, char** argv) {
                      unsigned(std::stoul(argv[5])));
   if (argc >= 7 && std::string(argv[1]) == "toys")
     return cmd_toys(argv[2], unsigned(std::stoul(argv[3])), std::stod(argv[4]), std::stod(argv[5]), argv[6]);
-  std::fprintf(stderr, "usage: refkit golden <mass|mass_w|pwave|spwave> <n> <out.json> [events.bin]\n"
+  std::fprintf(stderr, "usage: refkit golden <mass|mass_w|cbpoly|pwave|spwave> <n> <out.json> [events.bin]\n"
                        "       refkit bench <mass|pwave|spwave> <n> <nthreads> <nevals>\n"
                        "       refkit toys <pwave> <ntoys> <mean events> <jitter> <out.json>\n");
   return 2;

@@ -23,7 +23,7 @@ def load_golden(name: str) -> dict:
 
 def golden_events(workload: str, n: int) -> np.ndarray:
     raw = np.fromfile(GOLDEN / f"{workload}_n{n}_events.f64", dtype=np.float64)
-    ndim = {"mass": 1, "mass_w": 2}.get(workload, 3)
+    ndim = len(load_golden(f"{workload}_n{n}.json")["dimensions"])
     return raw.reshape(ndim, n)
 
 
@@ -39,7 +39,7 @@ def assert_sums_close(got, ref, abs_scale, rtol=1e-10, stol=1e-12, what=""):
     got = np.asarray(got, dtype=np.float64)
     ref = np.asarray(ref, dtype=np.float64)
     tol = rtol * np.abs(ref) + stol * np.asarray(abs_scale, dtype=np.float64)
-    bad = np.abs(got - ref) > tol
+    bad = ~(np.abs(got - ref) <= tol)  # NaN counts as a mismatch
     assert not bad.any(), (f"{what}: outputs {np.nonzero(bad)[0].tolist()} differ: got {got[bad]}, "
                            f"ref {ref[bad]}, |diff| {np.abs(got - ref)[bad]}, tol {tol[bad]}")
 

@@ -15,14 +15,14 @@ HERE = Path(__file__).resolve().parent
 OUT = HERE.parent.parent / "morefit_gb300" / "specs"
 
 ANGLES = {"ctl": [-1.0, 1.0], "ctk": [-1.0, 1.0], "phi": [-3.141592653589793, 3.141592653589793]}
-RANGES = {"mass": {"m": [5000.0, 5600.0]}, "mass_w": {"m": [5000.0, 5600.0], "w": [0.0, 2.0]}, "pwave": ANGLES,
-          "spwave": ANGLES}
+RANGES = {"mass": {"m": [5000.0, 5600.0]}, "mass_w": {"m": [5000.0, 5600.0], "w": [0.0, 2.0]},
+          "cbpoly": {"x": [-1.0, 1.0]}, "pwave": ANGLES, "spwave": ANGLES}
 
 
 def main():
     OUT.mkdir(parents=True, exist_ok=True)
-    for wl, src in (("mass", "mass_n1000.json"), ("mass_w", "mass_w_n1000.json"), ("pwave", "pwave_n1000.json"),
-                    ("spwave", "spwave_n2000.json")):
+    for wl, src in (("mass", "mass_n1000.json"), ("mass_w", "mass_w_n1000.json"), ("cbpoly", "cbpoly_n1000.json"),
+                    ("pwave", "pwave_n1000.json"), ("spwave", "spwave_n2000.json")):
         g = json.loads((HERE / src).read_text())
         spec = {k: g[k] for k in ("workload", "dimensions", "parameters", "truth", "kernels", "event_buffers",
                                   "lh_buffers", "grad_buffers", "hessian_buffers")}

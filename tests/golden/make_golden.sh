@@ -13,6 +13,8 @@ K="$ROOT/oracle/_ref/refkit"
 "$K" golden mass 100000 "$HERE/mass_n100000.json"
 "$K" golden mass_w 1000 "$HERE/mass_w_n1000.json" "$HERE/mass_w_n1000_events.f64"
 "$K" golden mass_w 100000 "$HERE/mass_w_n100000.json"
+"$K" golden cbpoly 1000 "$HERE/cbpoly_n1000.json" "$HERE/cbpoly_n1000_events.f64"
+"$K" golden cbpoly 100000 "$HERE/cbpoly_n100000.json"
 "$K" golden pwave 1000000 "$HERE/pwave_n1000000.json"
 "$K" golden spwave 2000 "$HERE/spwave_n2000.json" "$HERE/spwave_n2000_events.f64"
 "$K" golden spwave 20000 "$HERE/spwave_n20000.json"

@@ -81,7 +81,7 @@ def test_float_kernels_use_float_literals_and_functions():
     assert "double2" not in body and "float4" in body
 
 
-@pytest.mark.parametrize("workload", ["pwave", "mass", "mass_w"])
+@pytest.mark.parametrize("workload", ["pwave", "mass", "mass_w", "cbpoly"])
 @pytest.mark.parametrize("elem", [0, 1])
 def test_all_kernels_compile_without_spills(workload, elem):
     from morefit_gb300 import _lib as L

@@ -40,7 +40,7 @@ def _inputs_for(g, events, spec_name):
     return events
 
 
-@pytest.mark.parametrize("workload", ["pwave", "mass", "mass_w"])
+@pytest.mark.parametrize("workload", ["pwave", "mass", "mass_w", "cbpoly"])
 def test_spec_kernel_reproduces_reference_sums(oracle_lib, workload):
     g = load_golden(f"{workload}_n1000.json")
     ev = golden_events(workload, 1000)
