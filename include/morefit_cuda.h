@@ -284,6 +284,21 @@ int mf_columns_sum(const mf_buffer* buf, int elem_type, uint32_t ncols, uint64_t
 int mf_columns_sum_noalloc(const void* data, int elem_type, uint32_t ncols, uint64_t n, uint64_t stride,
                            double* sums, void* stream);
 
+/* Histogram of one event column for plotting (the data histogram of
+ * plotter::plot, include/plotter.hh:296-319): event i goes to bin
+ * floor((x_i - lo) / (hi - lo) * nbins), computed in FP64 as the reference
+ * does. y[b] receives the number of events in bin b (weights == NULL) or the
+ * sum of their weights, y2[b] the sum of squared weights (= y[b] without
+ * weights). `data` and `weights` (NULL or the weight column) are device
+ * pointers to n values of elem_type (MF_F64/MF_F32); y and y2 device pointers
+ * to nbins doubles, `outside` a device pointer to one uint64 that receives
+ * the number of events whose bin index is not in [0, nbins) (x >= hi, x < lo,
+ * NaN) -- the reference throws for those. Unweighted counts are exact;
+ * weighted sums are FP64 sums in an unspecified order. Enqueued on `stream`
+ * (a cudaStream_t, NULL for the default stream); allocates nothing. */
+int mf_histogram(const void* data, const void* weights, int elem_type, uint64_t n, double lo, double hi,
+                 uint32_t nbins, double* y, double* y2, uint64_t* outside, void* stream);
+
 /* The context's cudaStream_t, as an opaque pointer (interop: events, graphs). */
 int mf_context_stream(mf_context* ctx, void** stream);
 

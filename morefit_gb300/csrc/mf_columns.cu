@@ -211,3 +211,136 @@ extern "C" int mf_columns_sum_noalloc(const void* data, int elem_type, uint32_t 
   if (e != cudaSuccess) return set_error(MF_ERR_CUDA, std::string("cudaMemsetAsync: ") + cudaGetErrorString(e));
   return mfi::columns_sum_launch(data, elem_type, stride, n, ncols, s->partials, s->counter, sums, st, s->num_sms);
 }
+
+// ---- histogram of one column (plotting) ----
+//
+// Bin index as the reference's plotter computes it (plotter.hh:301-319):
+// floor((x - lo) / (hi - lo) * nbins) in FP64, so every event lands in the
+// same bin. Per-block shared-memory histograms (atomics) flushed to global
+// memory; unweighted counts are integers (exact), accumulated in place in
+// the output array's 8-byte words and converted to FP64 at the end.
+namespace {
+
+constexpr uint32_t kHistSharedCount = 8192;  // u32 counters in shared memory
+constexpr uint32_t kHistSharedWeight = 2048;  // (sum w, sum w^2) pairs in shared memory
+
+template <typename T, bool Weighted, bool Shared>
+__global__ void __launch_bounds__(kThreads) histogram_kernel(const T* __restrict__ x, const T* __restrict__ w,
+                                                              uint64_t n, double lo, double width, uint32_t nbins,
+                                                              double* __restrict__ y, double* __restrict__ y2,
+                                                              unsigned long long* __restrict__ outside) {
+  extern __shared__ __align__(16) unsigned char hist_smem[];
+  unsigned* scount = reinterpret_cast<unsigned*>(hist_smem);
+  double* sw = reinterpret_cast<double*>(hist_smem);
+  unsigned long long* gcount = reinterpret_cast<unsigned long long*>(y);
+  if (Shared) {
+    for (uint32_t b = threadIdx.x; b < nbins; b += blockDim.x) {
+      if (Weighted) {
+        sw[2 * b] = 0.0;
+        sw[2 * b + 1] = 0.0;
+      } else {
+        scount[b] = 0u;
+      }
+    }
+    __syncthreads();
+  }
+  const double nb = double(nbins);
+  unsigned long long out = 0;
+  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x) {
+    const double f = floor((double(x[i]) - lo) / width * nb);
+    if (!(f >= 0.0 && f < nb)) {
+      out++;
+      continue;
+    }
+    const uint32_t b = uint32_t(f);
+    if (Weighted) {
+      const double wi = double(w[i]);
+      if (Shared) {
+        atomicAdd(&sw[2 * b], wi);
+        atomicAdd(&sw[2 * b + 1], wi * wi);
+      } else {
+        atomicAdd(&y[b], wi);
+        atomicAdd(&y2[b], wi * wi);
+      }
+    } else {
+      if (Shared)
+        atomicAdd(&scount[b], 1u);
+      else
+        atomicAdd(&gcount[b], 1ull);
+    }
+  }
+  if (out) atomicAdd(outside, out);
+  if (Shared) {
+    __syncthreads();
+    for (uint32_t b = threadIdx.x; b < nbins; b += blockDim.x) {
+      if (Weighted) {
+        if (sw[2 * b] != 0.0 || sw[2 * b + 1] != 0.0) {
+          atomicAdd(&y[b], sw[2 * b]);
+          atomicAdd(&y2[b], sw[2 * b + 1]);
+        }
+      } else if (scount[b]) {
+        atomicAdd(&gcount[b], (unsigned long long)scount[b]);
+      }
+    }
+  }
+}
+
+// Unweighted: integer counts (in y's words) to FP64 counts in y and y2.
+__global__ void histogram_counts_to_f64(double* __restrict__ y, double* __restrict__ y2, uint32_t nbins) {
+  const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nbins) return;
+  const double c = double(reinterpret_cast<const unsigned long long*>(y)[b]);
+  y[b] = c;
+  y2[b] = c;
+}
+
+template <typename T>
+int histogram_launch(const void* data, const void* weights, uint64_t n, double lo, double width, uint32_t nbins,
+                     double* y, double* y2, unsigned long long* outside, cudaStream_t st, int grid) {
+  const T* x = static_cast<const T*>(data);
+  const T* w = static_cast<const T*>(weights);
+  if (w) {
+    if (nbins <= kHistSharedWeight)
+      histogram_kernel<T, true, true><<<grid, kThreads, size_t(nbins) * 16, st>>>(x, w, n, lo, width, nbins, y, y2,
+                                                                                   outside);
+    else
+      histogram_kernel<T, true, false><<<grid, kThreads, 0, st>>>(x, w, n, lo, width, nbins, y, y2, outside);
+  } else {
+    if (nbins <= kHistSharedCount)
+      histogram_kernel<T, false, true><<<grid, kThreads, size_t(nbins) * 4, st>>>(x, w, n, lo, width, nbins, y, y2,
+                                                                                   outside);
+    else
+      histogram_kernel<T, false, false><<<grid, kThreads, 0, st>>>(x, w, n, lo, width, nbins, y, y2, outside);
+    histogram_counts_to_f64<<<(nbins + kThreads - 1) / kThreads, kThreads, 0, st>>>(y, y2, nbins);
+  }
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return set_error(MF_ERR_CUDA, std::string("histogram launch: ") + cudaGetErrorString(e));
+  return MF_OK;
+}
+
+}  // namespace
+
+extern "C" int mf_histogram(const void* data, const void* weights, int elem_type, uint64_t n, double lo, double hi,
+                            uint32_t nbins, double* y, double* y2, uint64_t* outside, void* stream) {
+  if (!data || !y || !y2 || !outside) return set_error(MF_ERR_INVALID, "null argument");
+  if (elem_type != MF_F64 && elem_type != MF_F32)
+    return set_error(MF_ERR_INVALID, "element type must be MF_F64 or MF_F32");
+  if (nbins == 0) return set_error(MF_ERR_INVALID, "nbins must be positive");
+  if (!(hi > lo)) return set_error(MF_ERR_INVALID, "histogram range must have hi > lo");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaMemsetAsync(y, 0, size_t(nbins) * sizeof(double), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(y2, 0, size_t(nbins) * sizeof(double), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(outside, 0, sizeof(uint64_t), st);
+  if (e != cudaSuccess) return set_error(MF_ERR_CUDA, std::string("cudaMemsetAsync: ") + cudaGetErrorString(e));
+  int dev = 0, sms = 0;
+  e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return set_error(MF_ERR_CUDA, std::string("device query: ") + cudaGetErrorString(e));
+  const uint64_t need = (n + uint64_t(kThreads) * 8 - 1) / (uint64_t(kThreads) * 8);
+  const int grid = int(std::max<uint64_t>(1, std::min<uint64_t>(need, uint64_t(sms) * 4)));
+  auto* outp = reinterpret_cast<unsigned long long*>(outside);
+  const double width = hi - lo;
+  return elem_type == MF_F64
+             ? histogram_launch<double>(data, weights, n, lo, width, nbins, y, y2, outp, st, grid)
+             : histogram_launch<float>(data, weights, n, lo, width, nbins, y, y2, outp, st, grid);
+}

@@ -69,8 +69,9 @@ inline std::vector<RecordedKernel>& recorded_kernels() {
   return r;
 }
 
-// Observer of every parameter vector handed to a block ("params") and every
-// Kahan result read back ("sums"), keyed by kernel name (golden capture).
+// Observer of every parameter vector handed to a block ("params"), every
+// Kahan result ("sums") and every output buffer ("outputs") read back, keyed
+// by kernel name (golden capture).
 using BlockObserver = std::function<void(const std::string&, const char*, const std::vector<double>&)>;
 inline BlockObserver& block_observer() {
   static BlockObserver f;
@@ -183,6 +184,11 @@ class LLVMBlock : public ComputeBlock<kernelT, evalT, seedT> {
   }
   bool CopyFromOutputBuffer(EventVector<kernelT, evalT>& data) override {
     std::memcpy(data.get_data(), output_, data.buffer_size());
+    if (block_observer()) {
+      const kernelT* o = reinterpret_cast<const kernelT*>(output_);
+      block_observer()(name_, "outputs",
+                       std::vector<double>(o, o + data.buffer_size() / sizeof(kernelT)));
+    }
     return true;
   }
   bool CopyFromKahanBuffer(std::vector<evalT>& sums) override {

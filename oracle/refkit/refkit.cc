@@ -13,18 +13,24 @@
 //           benchmarking/morefit_kstarmumu.cc:74-92.
 //   spwave: the P-wave density plus S-wave and S-P interference terms times
 //           a Legendre acceptance (SPwaveAccPDF below), 14 floating parameters.
+//   mass_w: the mass model with an event weight column (weighted fit with
+//           the Fisher kernel and the covariance correction).
+//   cbpoly: Crystal Ball + quadratic polynomial on x in [-1,1] (pdf.hh:199-419,
+//           :717-892), 7 floating parameters.
 // Events come from generator::generate on the accelerator path with one
 // xoshiro128++ stream seeded by Xoshiro128pp::setSeed(229387429)
 // (random.hh:355-362, generator.hh:102-113), as in the reference drivers.
 //
 // Usage:
-//   refkit golden <mass|pwave|spwave> <nevents> <out.json> [events.bin]
+//   refkit golden <workload> <nevents> <out.json> [events.bin]
 //   refkit bench  <mass|pwave|spwave> <nevents> <nthreads> <nevals>
 //   refkit toys   <pwave> <ntoys> <mean events> <jitter> <out.json>
+//   refkit plot   <workload> <nevents> <variable> <nbins> <out.py> <out.json>
 #define MOREFIT_H 1  // keep graph.hh from pulling in the OpenCL/LLVM backends
 #include <cassert>
 #include <chrono>
 #include <cmath>
+#include <fstream>
 #include <functional>
 #include <cstdint>
 #include <cstdio>
@@ -43,6 +49,7 @@
 #include "gcc_block.hh"
 #include "fitter.hh"
 #include "generator.hh"
+#include "plotter.hh"
 #include "random.hh"
 
 using namespace morefit;
@@ -53,24 +60,37 @@ typedef LLVMBlock<kT, eT> blockT;
 
 // ---- capture hooks: every parameter vector and Kahan result, per kernel ----
 struct Capture {
-  std::map<std::string, std::vector<double>> params, sums;
+  std::map<std::string, std::vector<double>> params, sums, outputs;
 };
 static Capture* g_capture = nullptr;
 static void install_capture() {
   block_observer() = [](const std::string& kernel, const char* what, const std::vector<double>& v) {
     if (!g_capture) return;
-    if (std::string(what) == "params")
+    const std::string w = what;
+    if (w == "params")
       g_capture->params[kernel] = v;
-    else
+    else if (w == "sums")
       g_capture->sums[kernel] = v;
+    else
+      g_capture->outputs[kernel] = v;
   };
 }
 
 static std::string jstr(const std::string& s) {
   std::string o = "\"";
   for (char c : s) {
-    if (c == '"' || c == '\\') o += '\\';
-    o += c;
+    if (c == '"' || c == '\\') {
+      o += '\\';
+      o += c;
+    } else if (c == '\n') {
+      o += "\\n";
+    } else if (static_cast<unsigned char>(c) < 0x20) {
+      char b[8];
+      std::snprintf(b, sizeof b, "\\u%04x", unsigned(c));
+      o += b;
+    } else {
+      o += c;
+    }
   }
   return o + "\"";
 }
@@ -709,6 +729,108 @@ static int cmd_toys(const std::string& which, unsigned ntoys, double mean, doubl
   return 0;
 }
 
+// Runs the reference's plotter (matplotlib output, pulls on) on generated
+// events at the truth and records: the integral kernel it builds (parameter
+// values substituted, plotter.hh:138-216) with its per-bin integrals, the
+// written .py text, and the same definite integral with the parameters kept
+// as names (parameter-only terms hoisted into buffers as the fitter does),
+// for a backend that takes parameter values at launch.
+static int cmd_plot(const std::string& which, unsigned n, const std::string& var, unsigned nbins,
+                    const std::string& out_py, const std::string& out_json) {
+  compute_options copts;
+  copts.llvm_nthreads = 1;
+  copts.print_kernel = false;
+  backendT backend(&copts);
+  Workload w = make_workload(which);
+  Xoshiro128pp rnd;
+  rnd.setSeed(int64_t(229387429));
+  EventVector<kT, eT> data(w.dims);
+  generate(w, &backend, &rnd, n, data);
+  const uint64_t ev_hash = fnv1a(data.get_data(), data.buffer_size());
+
+  plotter_options popts;
+  popts.plotter = plotter_options::plotter_type::MatPlotLib;
+  popts.plot_pulls = true;
+  popts.print_level = 0;
+  plotter<kT, eT, backendT, blockT> pl(&popts, &backend);
+  recorded_kernels().clear();
+  Capture cap;
+  g_capture = &cap;
+  std::ostringstream captured;
+  auto* old = std::cout.rdbuf(captured.rdbuf());
+  pl.plot(w.pdf, w.params, &data, var, out_py, "", nbins);
+  // the same plot as a ROOT macro (same stem, kernels reused)
+  const std::string out_c = out_py.substr(0, out_py.size() - 3) + ".C";
+  popts.plotter = plotter_options::plotter_type::Root;
+  pl.plot(w.pdf, w.params, &data, var, out_c, "", nbins, 0.0, 0.0, true);
+  std::cout.rdbuf(old);
+  g_capture = nullptr;
+  RecordedKernel rk;
+  for (auto& r : recorded_kernels())
+    if (r.name == "integral_kernel") rk = r;
+  std::vector<double> pdf_y = cap.outputs["integral_kernel"];
+  pdf_y.resize(size_t(nbins) * popts.pdf_bin_multiplier);
+
+  // the integral with symbolic parameters (plotter::make_kernels without the
+  // parameter substitution)
+  std::vector<std::string> dn, floating;
+  std::vector<eT> dv;
+  std::string vfrom, vto;
+  double lo = 0.0, hi = 0.0;
+  for (auto* d : w.pdf->dimensions())
+    if (d->get_name() != var) {
+      dn.push_back(d->get_from_name());
+      dv.push_back(d->get_min());
+      dn.push_back(d->get_to_name());
+      dv.push_back(d->get_max());
+    } else {
+      vfrom = d->get_from_name();
+      vto = d->get_to_name();
+      lo = d->get_min();
+      hi = d->get_max();
+    }
+  for (auto* p : w.params) floating.push_back(p->get_name());
+  std::unique_ptr<ComputeGraphNode<kT, eT>> integral = w.pdf->definite_integral()->substitute(dn, dv)->simplify();
+  integral->rename_variable(vfrom, "morefit_from");
+  integral->rename_variable(vto, "morefit_to");
+  std::vector<std::string> bnames;
+  std::vector<std::unique_ptr<ComputeGraphNode<kT, eT>>> bexprs;
+  std::unique_ptr<ComputeGraphNode<kT, eT>> sym =
+      integral->optimize_buffering_constant_terms(bnames, bexprs, floating, "morefit_parambuffer_", 2.0);
+  std::vector<std::pair<std::string, std::string>> bufs;
+  for (size_t i = 0; i < bnames.size(); i++) bufs.push_back({bnames[i], bexprs[i]->get_kernel()});
+  std::vector<std::string> sparams = floating;
+  for (auto& b : bnames) sparams.push_back(b);
+
+  std::ifstream pyf(out_py), cf(out_c);
+  std::stringstream pys, cs;
+  pys << pyf.rdbuf();
+  cs << cf.rdbuf();
+  std::vector<std::string> tex;
+  for (auto* d : w.pdf->dimensions()) tex.push_back(d->get_tex());
+  std::vector<double> truth;
+  for (auto* p : w.params) truth.push_back(p->get_value());
+  char hash[32];
+  std::snprintf(hash, sizeof hash, "%016llx", (unsigned long long)ev_hash);
+  std::string js = "{\"workload\":" + jstr(w.name) + ",\"nevents\":" + std::to_string(n) +
+                   ",\"events_fnv1a\":" + jstr(hash) + ",\"variable\":" + jstr(var) +
+                   ",\"nbins\":" + std::to_string(nbins) +
+                   ",\"pdf_bin_multiplier\":" + std::to_string(popts.pdf_bin_multiplier) +
+                   ",\"range\":" + jvec({lo, hi}) + ",\"parameters\":" + jsvec(floating) +
+                   ",\"truth\":" + jvec(truth) + ",\"reference_kernel\":{\"inputs\":" + jsvec(rk.inputs) +
+                   ",\"params\":" + jsvec(rk.params) + ",\"exprs\":" + jsvec(rk.exprs) +
+                   "},\"pdf_y\":" + jvec(pdf_y) + ",\"integral\":{\"inputs\":" +
+                   jsvec({"morefit_from", "morefit_to"}) + ",\"params\":" + jsvec(sparams) +
+                   ",\"exprs\":" + jsvec({sym->get_kernel()}) + ",\"buffers\":" + jpairs(bufs) +
+                   "},\"tex\":" + jsvec(tex) + ",\"py\":" + jstr(pys.str()) + ",\"C\":" + jstr(cs.str()) +
+                   "}\n";
+  FILE* f = std::fopen(out_json.c_str(), "w");
+  std::fputs(js.c_str(), f);
+  std::fclose(f);
+  std::fprintf(stderr, "plot %s %s n=%u bins=%u events_fnv1a=%s\n", which.c_str(), var.c_str(), n, nbins, hash);
+  return 0;
+}
+
 int main(int argc, char** argv) {
   install_capture();
   if (argc >= 5 && std::string(argv[1]) == "golden")
@@ -716,10 +838,13 @@ int main(int argc, char** argv) {
   if (argc >= 6 && std::string(argv[1]) == "bench")
     return cmd_bench(argv[2], unsigned(std::stoul(argv[3])), unsigned(std::stoul(argv[4])),
                      unsigned(std::stoul(argv[5])));
+  if (argc >= 8 && std::string(argv[1]) == "plot")
+    return cmd_plot(argv[2], unsigned(std::stoul(argv[3])), argv[4], unsigned(std::stoul(argv[5])), argv[6], argv[7]);
   if (argc >= 7 && std::string(argv[1]) == "toys")
     return cmd_toys(argv[2], unsigned(std::stoul(argv[3])), std::stod(argv[4]), std::stod(argv[5]), argv[6]);
   std::fprintf(stderr, "usage: refkit golden <mass|mass_w|cbpoly|pwave|spwave> <n> <out.json> [events.bin]\n"
                        "       refkit bench <mass|pwave|spwave> <n> <nthreads> <nevals>\n"
-                       "       refkit toys <pwave> <ntoys> <mean events> <jitter> <out.json>\n");
+                       "       refkit toys <pwave> <ntoys> <mean events> <jitter> <out.json>\n"
+                       "       refkit plot <workload> <n> <variable> <nbins> <out.py> <out.json>\n");
   return 2;
 }

@@ -29,6 +29,13 @@ def main():
         for k in ("weight", "fisher_buffers"):
             if k in g:
                 spec[k] = g[k]
+        # plotter integrals per variable (oracle/refkit plot), parameters symbolic
+        for f in sorted(HERE.glob(f"plot_{wl}_*.json")):
+            pg = json.loads(f.read_text())
+            if pg["workload"] != wl:
+                continue
+            spec.setdefault("integrals", {})[pg["variable"]] = pg["integral"]
+            spec["tex"] = pg["tex"]
         spec["ranges"] = [RANGES[wl][d] for d in g["dimensions"]]
         spec["seed"] = g["seed"]
         (OUT / f"{wl}.json").write_text(json.dumps(spec, indent=1) + "\n")
