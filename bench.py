@@ -458,6 +458,8 @@ def ours(args):
                    "live": live, "capacity_all_at_once": cap, "serial_fits_per_s": serial,
                    "capacity_over_serial": cap["fits_per_s"] / serial}
 
+    extras = None if args.no_extras else extra_rows(backend)
+
     # ---------------- CPU baseline (rank 0, N=1 only) ----------------
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -506,6 +508,7 @@ def ours(args):
                                  "d2h_bytes_per_step": nout * 8,
                                  "what": "events resident; parameters in, sums out (the fitter's per-evaluation path)"},
                 "native_fp64": native, "mixed": mixed, "spwave_10M": spw, "toys": toys, "serving": serving,
+                "extras": extras,
                 "cpu_baseline": cpu,
                 "clocks": clk.summary(),
                 "gpu_launches": args.steps, "nll_truth": float(-2.0 * res64[0])}
@@ -606,6 +609,79 @@ def variants(args):
         del sets
 
 
+def extra_rows(backend):
+    """The rows around the headline path, each timed once on 1M events:
+    weighted fit (Fisher kernel, corrected covariance), the Crystal Ball +
+    polynomial model, one plot (integral kernel + GPU histogram + text), and
+    event input from a file (page-cached .npy streamed to HBM)."""
+    import tempfile
+    from morefit_gb300.eventio import save_event_vector, upload_event_file
+    from morefit_gb300.plotter import Plotter, PlotterOptions
+    from morefit_gb300.workloads import Likelihood, generate_events, load_spec
+    n = 1_000_000
+    out = {}
+
+    def rate(fn, k):
+        fn()
+        backend.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(k):
+            fn()
+        return k / (time.perf_counter() - t0)
+
+    # weighted mass fit: the mass events plus w_i = 0.5 + frac(i * 0.618...)
+    mw = load_spec("mass_w")
+    ev = generate_events(backend, load_spec("mass"), n, seed=11).download()
+    f = np.arange(n, dtype=np.float64) * 0.6180339887498949
+    evw = np.vstack([ev, 0.5 + (f - np.floor(f))])
+    lw = Likelihood(backend, mw, np.float64)
+    lw.set_data(evw)
+    limits = [(5200.0, 5400.0), (5.0, 50.0), (0.0, 1.0), (-0.01, 0.01)]
+    t0 = time.perf_counter()
+    r = lw.fit(limits=limits)
+    fit_ms = (time.perf_counter() - t0) * 1e3
+    out["weighted_mass_1M"] = {
+        "fisher_evals_per_s": rate(lambda: lw.sums("lh_fisher_kernel", mw["truth"]), 50),
+        "grad_evals_per_s": rate(lambda: lw.sums("lh_grad_kernel", mw["truth"]), 50),
+        "fit_ms": fit_ms, "converged": bool(r.converged[0]), "evaluations": int(r.evaluations),
+        "what": "synchronous evaluations (parameters in, sums out); fit = damped Newton from the truth + "
+                "-2 H^-1 F H^-1 covariance"}
+    # Crystal Ball + polynomial
+    cb = load_spec("cbpoly")
+    lc = Likelihood(backend, cb, np.float64)
+    lc.set_device_data(generate_events(backend, cb, n, seed=12))
+    t0 = time.perf_counter()
+    rc = lc.fit(limits=[(-0.2, 0.4), (0.01, 0.2), (0.5, 5.0), (1.5, 10.0), (-1.0, 1.0), (-1.0, 1.0), (0.0, 1.0)])
+    out["cbpoly_1M"] = {"grad_evals_per_s": rate(lambda: lc.sums("lh_grad_kernel", cb["truth"]), 50),
+                        "hessian_evals_per_s": rate(lambda: lc.sums("lh_hessian_kernel", cb["truth"]), 20),
+                        "fit_ms": (time.perf_counter() - t0) * 1e3, "converged": bool(rc.converged[0])}
+    with tempfile.TemporaryDirectory() as td:
+        # plot of the mass model over 1M device-resident events
+        mass = load_spec("mass")
+        cols = generate_events(backend, mass, n, seed=13)
+        pl = Plotter(PlotterOptions(plotter="matplotlib", plot_pulls=True), backend)
+        name = str(Path(td) / "mass_m.py")
+        out["plot_mass_1M"] = {"plots_per_s": rate(lambda: pl.plot(mass, mass["truth"], cols, "m", name, 100), 20),
+                               "what": "1000 integral bins (native FP64 kernel) + 100-bin GPU histogram + pulls + "
+                                       "matplotlib text"}
+        # event file: 10M P-wave events, 3 FP64 columns
+        pw = load_spec("pwave")
+        big = generate_events(backend, pw, 10 * n, seed=14).download()
+        fpath = Path(td) / "pwave_10M.npy"
+        save_event_vector(fpath, big)
+        dims = pw["dimensions"]
+        holder = {}
+
+        def load():
+            holder["c"] = upload_event_file(backend, fpath, dims)
+        per_s = rate(load, 3)
+        out["file_load_10M"] = {"GBs": big.nbytes * per_s / 1e9, "bytes": int(big.nbytes),
+                                "what": "2-D SoA .npy (page cache warm) streamed through two 8 MiB page-locked "
+                                        "chunks into HBM (mf_events_load_file)",
+                                "exact": bool(np.array_equal(holder["c"].download()[:, :1000], big[:, :1000]))}
+    return out
+
+
 def C_stream(backend):
     import ctypes as C
     from morefit_gb300 import _lib as L
@@ -634,6 +710,7 @@ def main():
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-native", action="store_true")
+    ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--variants", action="store_true", help="time every kernel variant instead")
     ap.add_argument("--variant-list", default="")
     ap.add_argument("--sets", type=int, default=5)

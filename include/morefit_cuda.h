@@ -130,6 +130,20 @@ int mf_events_upload_f64_as(mf_buffer* buf, int elem_type, const double* host, u
  * OpenCL backend copies blocking (CL_TRUE, include/compute_opencl.hh:359,411). */
 int mf_events_upload_async(mf_buffer* buf, int elem_type, const void* host, uint32_t ncols, uint64_t n,
                            uint64_t host_stride, uint64_t dev_stride);
+
+/* Loads event columns from a file into buf (the on-disk input of the
+ * reference, load_event_vector, include/eventvector.hh:297-332, reads a ROOT
+ * TTree; this reads plain SoA files, e.g. the data of a 2-D .npy array):
+ * at byte `offset` the file holds columns of file_stride values of file_elem
+ * (MF_F64/MF_F32) each; file columns cols[0..ncols) become device columns
+ * 0..ncols-1 (stride dev_stride, dev_elem), first n events of each, with the
+ * padding events zero-filled; FP64 values stored as FP32 are rounded to
+ * nearest. The file is read in 8 MiB chunks into two page-locked staging
+ * buffers of the context, the read of one chunk overlapping the copy of the
+ * other; returns once the data are on the device. A file shorter than the
+ * columns it should hold is an MF_ERR_INVALID error. */
+int mf_events_load_file(mf_buffer* buf, int dev_elem, uint64_t dev_stride, const char* path, uint64_t offset,
+                        int file_elem, uint64_t file_stride, uint32_t ncols, const uint32_t* cols, uint64_t n);
 int mf_buffer_d2h_async(const mf_buffer* buf, uint64_t offset, void* dst, uint64_t nbytes);
 
 /* ---- kernels ----

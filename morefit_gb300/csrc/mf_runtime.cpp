@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 #include <nvrtc.h>
 
+#include <fcntl.h>
 #include <unistd.h>
 
 #include <algorithm>
@@ -204,6 +205,10 @@ struct mf_context {
   // cudaMalloc / cudaFree (which synchronises the device) for each
   std::multimap<uint64_t, void*> free_cache;
   uint64_t cached = 0, cache_limit = 0;
+  // page-locked staging of the file loader: two chunks, each reused once
+  // the copy out of it (recorded event) has completed
+  void* load_stage[2] = {nullptr, nullptr};
+  cudaEvent_t load_done[2] = {nullptr, nullptr};
 };
 
 // A copy of a buffer's columns in the layout a REDUCE kernel reads (folded
@@ -295,6 +300,10 @@ void release_context(mf_context* c) {
   if (c->out_host) cudaFreeHost(c->out_host);
   if (c->status_host) cudaFreeHost(c->status_host);
   if (c->stage_dev) cudaFree(c->stage_dev);
+  for (int i = 0; i < 2; i++) {
+    if (c->load_stage[i]) cudaFreeHost(c->load_stage[i]);
+    if (c->load_done[i]) cudaEventDestroy(c->load_done[i]);
+  }
   for (auto& [sz, q] : c->free_cache) cudaFree(q);
   cudaStreamDestroy(c->stream);
   delete c;
@@ -683,6 +692,88 @@ int mf_events_upload_f64_as(mf_buffer* b, int elem, const double* host, uint32_t
   for (uint32_t c = 0; c < ncols; c++)
     for (uint64_t i = 0; i < n; i++) tmp[size_t(c) * n + i] = float(host[c * hs + i]);
   return mf_events_upload(b, MF_F32, tmp.data(), ncols, n, n, ds);
+}
+
+// Reads `bytes` at `off` of fd, retrying short reads; false at end of file.
+static bool read_fully(int fd, void* dst, uint64_t bytes, uint64_t off) {
+  char* p = static_cast<char*>(dst);
+  while (bytes) {
+    const ssize_t r = pread(fd, p, size_t(std::min<uint64_t>(bytes, uint64_t(1) << 30)), off_t(off));
+    if (r <= 0) return false;
+    p += r;
+    off += uint64_t(r);
+    bytes -= uint64_t(r);
+  }
+  return true;
+}
+
+int mf_events_load_file(mf_buffer* b, int dev_elem, uint64_t dev_stride, const char* path, uint64_t offset,
+                        int file_elem, uint64_t file_stride, uint32_t ncols, const uint32_t* cols, uint64_t n) {
+  if (!b || !path || (ncols && !cols)) return fail(MF_ERR_INVALID, "null argument");
+  if ((dev_elem != MF_F64 && dev_elem != MF_F32) || (file_elem != MF_F64 && file_elem != MF_F32))
+    return fail(MF_ERR_INVALID, "element types must be MF_F64 or MF_F32");
+  if (n > file_stride) return fail(MF_ERR_INVALID, "more events requested than a file column holds");
+  if (dev_stride < n) return fail(MF_ERR_INVALID, "device column stride smaller than the number of events");
+  const uint64_t fes = elem_size(file_elem), des = elem_size(dev_elem);
+  if (uint64_t(ncols) * dev_stride * des > b->size)
+    return fail(MF_ERR_INVALID, "buffer smaller than ncols x dev_stride elements");
+  mf_context* c = b->ctx;
+  MF_CUDA_TRY(cudaSetDevice(c->device));
+  constexpr uint64_t kChunk = uint64_t(8) << 20;  // bytes per staging chunk
+  for (int i = 0; i < 2; i++) {
+    if (!c->load_stage[i]) MF_CUDA_TRY(cudaHostAlloc(&c->load_stage[i], kChunk, cudaHostAllocDefault));
+    if (!c->load_done[i]) MF_CUDA_TRY(cudaEventCreateWithFlags(&c->load_done[i], cudaEventDisableTiming));
+  }
+  const int fd = open(path, O_RDONLY);
+  if (fd < 0) return fail(MF_ERR_INVALID, std::string("cannot open ") + path);
+  const uint64_t rows = kChunk / std::max(fes, des);
+  std::vector<unsigned char> conv(fes != des ? size_t(rows * fes) : 0);
+  char* dev = static_cast<char*>(b->ptr);
+  bool recorded[2] = {false, false};
+  int slot = 0, rc = MF_OK;
+  b->gen++;
+  for (uint32_t j = 0; j < ncols && rc == MF_OK; j++) {
+    for (uint64_t r0 = 0; r0 < n && rc == MF_OK; r0 += rows) {
+      const uint64_t m = std::min(rows, n - r0);
+      // the staging chunk is free again once its previous copy has completed
+      if (recorded[slot] && cudaEventSynchronize(c->load_done[slot]) != cudaSuccess) {
+        rc = fail(MF_ERR_CUDA, "waiting for a staging copy failed");
+        break;
+      }
+      void* st = c->load_stage[slot];
+      const uint64_t foff = offset + (uint64_t(cols[j]) * file_stride + r0) * fes;
+      if (!read_fully(fd, fes == des ? st : conv.data(), m * fes, foff)) {
+        rc = fail(MF_ERR_INVALID, std::string("file too short: ") + path);
+        break;
+      }
+      if (fes != des) {
+        if (file_elem == MF_F64) {
+          const double* s = reinterpret_cast<const double*>(conv.data());
+          float* d = static_cast<float*>(st);
+          for (uint64_t i = 0; i < m; i++) d[i] = float(s[i]);
+        } else {
+          const float* s = reinterpret_cast<const float*>(conv.data());
+          double* d = static_cast<double*>(st);
+          for (uint64_t i = 0; i < m; i++) d[i] = double(s[i]);
+        }
+      }
+      if (cudaMemcpyAsync(dev + (uint64_t(j) * dev_stride + r0) * des, st, m * des, cudaMemcpyHostToDevice,
+                          c->stream) != cudaSuccess ||
+          cudaEventRecord(c->load_done[slot], c->stream) != cudaSuccess) {
+        rc = fail(MF_ERR_CUDA, "staging copy failed");
+        break;
+      }
+      recorded[slot] = true;
+      slot ^= 1;
+    }
+    if (rc == MF_OK && dev_stride > n &&
+        cudaMemsetAsync(dev + (uint64_t(j) * dev_stride + n) * des, 0, (dev_stride - n) * des, c->stream) !=
+            cudaSuccess)
+      rc = fail(MF_ERR_CUDA, "padding fill failed");
+  }
+  close(fd);
+  MF_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return rc;
 }
 
 static int lower_desc(const mf_kernel_desc* d, mf::LoweredKernel& lk);
