@@ -202,7 +202,10 @@ typedef struct mf_kernel_desc {
  * the kernel, made on first need, and returns those sums
  * (mf_kernel_fallback_count counts such calls). The asynchronous and batched
  * entry points (mf_kernel_reduce_async, mf_kernel_reduce_many) return the
- * double-float sums as they are. */
+ * double-float sums as they are. Every REDUCE kernel, native FP64 included,
+ * combines its per-thread partials across threads and blocks in
+ * double-float, so the sums themselves must stay below 3.4e38 in magnitude
+ * (likelihood, gradient and Hessian sums are many orders below). */
 #define MF_FLAG_NATIVE_F64 1u
 /* FP64 columns, FP32 per-event arithmetic with FP64 sums (the mixed-precision
  * form for raw observables that need their FP64 storage, e.g. a mass with a

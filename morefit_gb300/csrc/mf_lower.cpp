@@ -545,7 +545,11 @@ __device__ __forceinline__ mf_dw mf_dw_rcp(mf_dw a) {
   const float e = __fsub_rn(__fsub_rn(__fsub_rn(1.0f, p), pe), __fmul_rn(a.l, r));
   return mf_fast_two_sum(r, __fmul_rn(r, e));
 }
-__device__ __forceinline__ double mf_dw_to_double(mf_dw a) { return (double)a.h + (double)a.l; }
+// An infinite high word is the value (its low word is NaN after inf - inf
+// in the error terms of a sum).
+__device__ __forceinline__ double mf_dw_to_double(mf_dw a) {
+  return isinf(a.h) ? (double)a.h : (double)a.h + (double)a.l;
+}
 __device__ __forceinline__ mf_dw mf_dw_from_double(double x) {
   const float h = __double2float_rn(x);
   return mf_dw_make(h, __double2float_rn(x - (double)h));
@@ -744,6 +748,79 @@ __device__ __forceinline__ mf_dw mf_dw_log(mf_dw a, const float4* __restrict__ t
   if (a.h == inf) r = mf_dw_make(inf, 0.0f);
   return r;
 }
+// exp of a double-float value by Tang's table-driven method (P. T. P. Tang,
+// ACM TOMS 15 (1989) 144-157): x = (64k + j) ln2/64 + r with ln2/64 split as
+// C1 + C2 + C3 (C1 of 9 significant bits, so N*C1 is exact for |N| < 2^13),
+// |r| <= ln2/128 (+ a rounding); exp(r) - 1 = r + r^2/2 + r^3/6 in
+// double-float plus r^4/24 + r^5/120 + r^6/720 in FP32 (below 4e-11);
+// exp(x) = 2^k * T_j * (1 + (exp(r) - 1)) with T_j = 2^(j/64) from the table,
+// 2^k applied as two exact power-of-two factors. Relative error ~2^-46 for
+// results from 2^-100 to 2^128 (where the low word is a normal float); below
+// 2^-100 the low word loses bits (an absolute error of a few 2^-149, the
+// resolution of any double-float value there) and results under 2^-149 are
+// 0; above 2^128 the result is +inf; NaN stays NaN.
+__device__ __forceinline__ mf_dw mf_dw_exp(mf_dw a, const float2* __restrict__ tab) {
+  const float x = fminf(fmaxf(a.h, -104.0f), 89.0f);
+  // N = x * 64/ln2 rounded to an integer (|N| < 2^14) without a conversion:
+  // adding 1.5*2^23 leaves the integer in the low significand bits
+  const float tn = __fmaf_rn(x, 0x1.715476p+6f, 12582912.0f);
+  const int Ni = __float_as_int(tn) - 0x4b400000;
+  const float N = __fsub_rn(tn, 12582912.0f);
+  const int j = Ni & 63;
+  const int k = (Ni - j) >> 6;
+  const float t1 = __fmaf_rn(-N, 0x1.63p-7f, x);  // exact
+  const float p2 = __fmul_rn(N, -0x1.bd0106p-19f);
+  const float p2e = __fmaf_rn(N, -0x1.bd0106p-19f, -p2);
+  mf_dw r = mf_two_sum(t1, -p2);
+  r = mf_fast_two_sum(r.h, __fadd_rn(r.l, __fsub_rn(__fmaf_rn(-N, 0x1.cf79acp-46f, a.l), p2e)));
+  const mf_dw r2 = mf_dw_mul(r, r);
+  const mf_dw r3 = mf_dw_mul(r2, r);
+  mf_dw t3 = mf_dw_mul(r3, mf_dw_make(0x1.555556p-3f, -0x1.555556p-28f));
+  const float q = __fmul_rn(__fmul_rn(r2.h, r2.h),
+                            __fmaf_rn(r.h, __fmaf_rn(r.h, 0x1.6c16c2p-10f, 0x1.111112p-7f), 0x1.555556p-5f));
+  t3 = mf_fast_two_sum(t3.h, __fadd_rn(t3.l, q));
+  mf_dw e = mf_dw_add(r, mf_dw_make(0.5f * r2.h, 0.5f * r2.l));
+  e = mf_dw_add(e, t3);
+  const float2 T = tab[j];
+  const mf_dw Tj = mf_dw_make(T.x, T.y);
+  mf_dw y = mf_dw_add(Tj, mf_dw_mul(Tj, e));
+  const int k1 = k >> 1, k2 = k - k1;  // both in [-76, 64]
+  const float s1 = __int_as_float((k1 + 127) << 23), s2 = __int_as_float((k2 + 127) << 23);
+  y = mf_dw_make(__fmul_rn(__fmul_rn(y.h, s1), s2), __fmul_rn(__fmul_rn(y.l, s1), s2));
+  if (a.h > 89.0f) y = mf_dw_make(__int_as_float(0x7f800000), 0.0f);
+  if (a.h < -104.0f) y = mf_dw_make(0.0f, 0.0f);
+  if (a.h != a.h) y = mf_dw_make(a.h, a.h);
+  return y;
+}
+// a^b = exp(b ln|a|) in double-float. a < 0: for integer b the sign follows
+// b's parity, otherwise NaN; a = 0: 0 for b > 0, +inf for b < 0; b = 0: 1
+// (also for a NaN). Relative error ~|b ln a| 2^-46.
+__device__ __forceinline__ mf_dw mf_dw_pow(mf_dw a, mf_dw b, const float4* __restrict__ ltab,
+                                           const float2* __restrict__ etab) {
+  const bool neg = a.h < 0.0f;
+  const mf_dw aa = neg ? mf_dw_neg(a) : a;
+  mf_dw r = mf_dw_exp(mf_dw_mul(b, mf_dw_log(aa, ltab)), etab);
+  // integer b and its parity from the significand bits (|v| < 2^23: v + 2^23
+  // holds v's integer part in its last bits; |v| >= 2^23 is an integer)
+  const float bh = fabsf(b.h), bl = fabsf(b.l);
+  const float th = __fadd_rn(bh, 8388608.0f), tl = __fadd_rn(bl, 8388608.0f);
+  const bool int_h = bh >= 8388608.0f || __fsub_rn(th, 8388608.0f) == bh;
+  const bool int_l = bl >= 8388608.0f || __fsub_rn(tl, 8388608.0f) == bl;
+  const bool int_b = int_h && int_l;
+  const bool odd = bh < 8388608.0f ? (__float_as_int(th) & 1) != 0
+                                   : (bh < 16777216.0f ? (__float_as_int(b.h) & 1) != 0
+                                                       : (bl < 8388608.0f && (__float_as_int(tl) & 1) != 0));
+  if (neg) r = int_b ? (odd ? mf_dw_neg(r) : r) : mf_dw_make(__int_as_float(0x7fc00000), 0.0f);
+  if (a.h == 0.0f) r = mf_dw_make(b.h > 0.0f ? 0.0f : __int_as_float(0x7f800000), 0.0f);
+  if (b.h == 0.0f) r = mf_dw_make(1.0f, 0.0f);
+  return r;
+}
+// Comparisons of normalized double-float values (lexicographic on (h, l)).
+__device__ __forceinline__ bool mf_dw_gt(mf_dw a, mf_dw b) { return a.h > b.h || (a.h == b.h && a.l > b.l); }
+__device__ __forceinline__ bool mf_dw_lt(mf_dw a, mf_dw b) { return a.h < b.h || (a.h == b.h && a.l < b.l); }
+__device__ __forceinline__ bool mf_dw_ge(mf_dw a, mf_dw b) { return a.h > b.h || (a.h == b.h && a.l >= b.l); }
+__device__ __forceinline__ bool mf_dw_le(mf_dw a, mf_dw b) { return a.h < b.h || (a.h == b.h && a.l <= b.l); }
+__device__ __forceinline__ bool mf_dw_eq(mf_dw a, mf_dw b) { return a.h == b.h && a.l == b.l; }
 __device__ __forceinline__ mf_dw mf_dw_shfl_xor(mf_dw a, int o) {
   return mf_dw_make(__shfl_xor_sync(0xffffffffu, a.h, o), __shfl_xor_sync(0xffffffffu, a.l, o));
 }
@@ -781,8 +858,46 @@ __device__ __forceinline__ bool mf_mbar_wait_bounded(unsigned long long* b, unsi
 }
 )CUDA";
 
+// 2^(j/64), j = 0..63, as double-float pairs {hi, lo} (hi the nearest float,
+// lo the nearest float to the remainder), computed in 60-digit decimal
+// arithmetic: the table of mf_dw_exp.
+const char* const kExp2Table[64] = {
+    "{0x1p+0f, 0x0p+0f}", "{0x1.02c9a4p+0f, -0x1.887fap-28f}",
+    "{0x1.059b0ep+0f, -0x1.9d4f52p-25f}", "{0x1.087452p+0f, -0x1.e2990ep-26f}",
+    "{0x1.0b5586p+0f, 0x1.9f3122p-25f}", "{0x1.0e3ec4p+0f, -0x1.a585ccp-25f}",
+    "{0x1.11301ep+0f, -0x1.fdb496p-25f}", "{0x1.1429aap+0f, 0x1.d525bcp-25f}",
+    "{0x1.172b84p+0f, -0x1.c15742p-27f}", "{0x1.1a35bep+0f, 0x1.6df96ep-25f}",
+    "{0x1.1d4874p+0f, -0x1.d2e8cap-25f}", "{0x1.2063b8p+0f, 0x1.0c519ap-25f}",
+    "{0x1.2387a6p+0f, 0x1.ceac48p-25f}", "{0x1.26b456p+0f, 0x1.789f38p-26f}",
+    "{0x1.29e9ep+0f, -0x1.5c0424p-25f}", "{0x1.2d285ap+0f, 0x1.b900c2p-26f}",
+    "{0x1.306fep+0f, 0x1.4636e2p-25f}", "{0x1.33c08cp+0f, -0x1.b37d2p-25f}",
+    "{0x1.371a74p+0f, -0x1.18aac6p-25f}", "{0x1.3a7db4p+0f, -0x1.634c02p-25f}",
+    "{0x1.3dea64p+0f, 0x1.824684p-25f}", "{0x1.4160a2p+0f, 0x1.f72e2ap-28f}",
+    "{0x1.44e086p+0f, 0x1.8624b4p-30f}", "{0x1.486a2cp+0f, -0x1.47d866p-25f}",
+    "{0x1.4bfdaep+0f, -0x1.593abcp-25f}", "{0x1.4f9b28p+0f, -0x1.2c5a6cp-25f}",
+    "{0x1.5342b6p+0f, -0x1.2c561p-25f}", "{0x1.56f474p+0f, -0x1.295b04p-25f}",
+    "{0x1.5ab07ep+0f, -0x1.5bd5ecp-27f}", "{0x1.5e76f2p+0f, -0x1.4a5bd6p-25f}",
+    "{0x1.6247ecp+0f, -0x1.f8b55p-25f}", "{0x1.662388p+0f, 0x1.2a9112p-27f}",
+    "{0x1.6a09e6p+0f, 0x1.9fcef4p-26f}", "{0x1.6dfb24p+0f, -0x1.cd72e8p-27f}",
+    "{0x1.71f75ep+0f, 0x1.1d8beep-25f}", "{0x1.75feb6p+0f, -0x1.37b306p-25f}",
+    "{0x1.7a1148p+0f, -0x1.829fdp-25f}", "{0x1.7e2f34p+0f, -0x1.261634p-25f}",
+    "{0x1.82589ap+0f, -0x1.accc7cp-26f}", "{0x1.868d9ap+0f, -0x1.2edb44p-26f}",
+    "{0x1.8ace54p+0f, 0x1.15506ep-27f}", "{0x1.8f1aeap+0f, -0x1.baa232p-26f}",
+    "{0x1.93737cp+0f, -0x1.e64744p-25f}", "{0x1.97d82ap+0f, -0x1.0d8d84p-31f}",
+    "{0x1.9c4918p+0f, 0x1.51f848p-27f}", "{0x1.a0c668p+0f, -0x1.2886a6p-26f}",
+    "{0x1.a5503cp+0f, -0x1.b83b54p-25f}", "{0x1.a9e6b6p+0f, -0x1.50c048p-25f}",
+    "{0x1.ae89fap+0f, -0x1.a94b14p-26f}", "{0x1.b33a2cp+0f, -0x1.ec3a82p-26f}",
+    "{0x1.b7f77p+0f, -0x1.a09438p-25f}", "{0x1.bcc1eap+0f, -0x1.f687c6p-25f}",
+    "{0x1.c199bep+0f, -0x1.3d56b2p-27f}", "{0x1.c67f12p+0f, 0x1.cafa2ap-25f}",
+    "{0x1.cb720ep+0f, -0x1.8837ccp-27f}", "{0x1.d072d4p+0f, 0x1.40f13p-25f}",
+    "{0x1.d5818ep+0f, -0x1.822dbcp-27f}", "{0x1.da9e6p+0f, 0x1.ed9942p-27f}",
+    "{0x1.dfc974p+0f, -0x1.908c94p-25f}", "{0x1.e502eep+0f, 0x1.e2cffep-26f}",
+    "{0x1.ea4afap+0f, 0x1.52486cp-27f}", "{0x1.efa1bep+0f, 0x1.cc2b44p-25f}",
+    "{0x1.f50766p+0f, -0x1.246ebp-26f}", "{0x1.fa7c18p+0f, 0x1.9e90d8p-28f}"};
+
 // The 128-entry table of mf_dw_log: for c_j = 1 + (2j+1)/256,
-// {hi(ln c_j), lo(ln c_j), 1/c_j, c_j} as exact float literals.
+// {hi(ln c_j), lo(ln c_j), 1/c_j, c_j} as exact float literals; and the
+// 64-entry table of mf_dw_exp.
 std::string dw_log_table() {
   std::ostringstream o;
   {
@@ -803,6 +918,9 @@ std::string dw_log_table() {
     std::snprintf(b, sizeof b, "  {%af, %af, %af, %af},\n", double(lh), double(ll), double(ic), c);
     o << b;
   }
+  o << "};\n";
+  o << "__device__ const float2 mf_dw_exptab_g[64] = {\n";
+  for (const char* row : kExp2Table) o << "  " << row << ",\n";
   o << "};\n";
   return o.str();
 }
@@ -989,9 +1107,16 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
         if (!live[i] || n.uniform || (n.op != Op::Add && n.op != Op::Sub)) continue;
         if (is_leafish(n.a) && is_leafish(n.b) && (ns[n.a].op == Op::Input || ns[n.b].op == Op::Input)) dnode[i] = 1;
       }
-    bool has_log = false;
-    for (size_t i = 0; i < ns.size(); i++)
-      if (live[i] && !ns[i].uniform && ns[i].op == Op::Log) has_log = true;
+    // Double-float exp and pow (table-driven, FP32 pipe) in REDUCE kernels,
+    // whose non-finite sums are re-evaluated in native FP64 by the runtime;
+    // STORE kernels write columns and keep FP64 exp / pow (full FP64 range).
+    const bool dw_exp = kind == Kind::Reduce;
+    bool has_log = false, has_exp = false;
+    for (size_t i = 0; i < ns.size(); i++) {
+      if (!live[i] || ns[i].uniform) continue;
+      if (ns[i].op == Op::Log || (dw_exp && ns[i].op == Op::Pow)) has_log = true;
+      if (dw_exp && (ns[i].op == Op::Exp || ns[i].op == Op::Pow)) has_exp = true;
+    }
     // The double-float library is always present: every cross-thread sum
     // (warp, block, grid) runs in double-float on the FP32 pipe.
     s << dw_log_table() << kDwPrelude << (kind == Kind::Reduce ? kBulkPrelude : "");
@@ -1159,8 +1284,22 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
           const std::string sn = "e" + std::to_string(it->second.first), cn = "e" + std::to_string(it->second.second);
           return "mf_dw " + sn + ", " + cn + "; mf_dw_sincos(" + A + ", &" + sn + ", &" + cn + ");";
         }
-        case Op::Pow: return lhs + "mf_dw_from_double(pow(" + D(A) + ", " + D(B) + "));";
-        case Op::Cmp: return lhs + "(" + D(A) + " " + cmp_str(n.cmp) + " " + D(B) + ");";
+        case Op::Pow:
+          if (dw_exp) return lhs + "mf_dw_pow(" + A + ", " + B + ", mf_logtab, mf_exptab);";
+          return lhs + "mf_dw_from_double(pow(" + D(A) + ", " + D(B) + "));";
+        case Op::Exp:
+          if (dw_exp) return lhs + "mf_dw_exp(" + A + ", mf_exptab);";
+          return lhs + "mf_dw_from_double(exp(" + D(A) + "));";
+        case Op::Cmp:
+          switch (n.cmp) {
+            case CmpOp::Gt: return lhs + "mf_dw_gt(" + A + ", " + B + ");";
+            case CmpOp::Lt: return lhs + "mf_dw_lt(" + A + ", " + B + ");";
+            case CmpOp::Ge: return lhs + "mf_dw_ge(" + A + ", " + B + ");";
+            case CmpOp::Le: return lhs + "mf_dw_le(" + A + ", " + B + ");";
+            case CmpOp::Eq: return lhs + "mf_dw_eq(" + A + ", " + B + ");";
+            case CmpOp::Ne: return lhs + "!mf_dw_eq(" + A + ", " + B + ");";
+          }
+          break;
         case Op::Select: return lhs + "(" + A + " ? " + B + " : " + Cc + ");";
         default:
           if (is_unary_fn(n.op)) return lhs + "mf_dw_from_double(" + fn_name(n.op, false) + "(" + D(A) + "));";
@@ -1334,10 +1473,14 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
         << "    __syncthreads();\n  }\n";
     };
     auto load_table = [&](std::ostringstream& o) {
-      if (ar != Ar::DW || !has_log) return;
-      o << "  __shared__ float4 mf_logtab[128];\n"
-        << "  for (int q = threadIdx.x; q < 128; q += MF_BLOCK) mf_logtab[q] = mf_dw_logtab_g[q];\n"
-        << "  __syncthreads();\n";
+      if (ar != Ar::DW || (!has_log && !has_exp)) return;
+      if (has_log)
+        o << "  __shared__ float4 mf_logtab[128];\n"
+          << "  for (int q = threadIdx.x; q < 128; q += MF_BLOCK) mf_logtab[q] = mf_dw_logtab_g[q];\n";
+      if (has_exp)
+        o << "  __shared__ float2 mf_exptab[64];\n"
+          << "  for (int q = threadIdx.x; q < 64; q += MF_BLOCK) mf_exptab[q] = mf_dw_exptab_g[q];\n";
+      o << "  __syncthreads();\n";
     };
     auto input_value = [&](const std::string& raw) {
       if (ar == Ar::DW) return (pair ? "mf_dw_pair(" : "mf_dw_split(") + raw + ")";

@@ -240,6 +240,66 @@ def test_reference_stream_full_size_sums(backend, workload, n):
             assert_sums_close(got, ref, _abs_scale(g, name, ev, p), what=f"{workload} n={n} {name}")
 
 
+def _per_value(backend, expr, cols, names):
+    """One REDUCE output per value: a double-float REDUCE kernel over ragged
+    segments of one event each."""
+    from morefit_gb300.backend import CUDABlock
+    blk = CUDABlock(backend, np.float64)
+    blk.MakeComputeKernel("t", 0, names, ["r0"], [], [expr], True)
+    blk.CopyToInputBuffer(cols)
+    n = cols.shape[1]
+    blk.SetNevents(n)
+    out = blk.SubmitSegments(np.arange(n, dtype=np.uint64), np.ones(n, dtype=np.uint32), np.zeros((n, 0)))
+    return out[:, 0], blk.kernel.fallback_count()
+
+
+def test_double_float_exp_and_pow(backend):
+    """exp and pow of double-float values in REDUCE kernels (table-driven
+    exp on the FP32 pipe) against FP64: exp within 3e-14 relative over the
+    FP32 normal range; pow within (|b ln a| + 1) * 3e-14; the IEEE special
+    cases; results beyond the FP32 range come from the native-FP64 kernel.
+    Below 2^-100 the low word of a double-float value is subnormal: those
+    results are checked to an absolute 2^-147."""
+    rng = np.random.default_rng(17)
+    x = np.concatenate([rng.uniform(-87.0, 88.5, 20000), [0.0, -0.0, 1e-30, -1e-30, 1e-5, 0.5, 1.0, -1.0,
+                                                          0.00541, -0.00541, 88.0, -87.0]]).astype(np.float32)
+    got, fb = _per_value(backend, "exp(x)", x.astype(np.float64)[None, :], ["x"])
+    ref = np.exp(x.astype(np.float64))
+    # full precision while the low word is a normal float (results >= 2^-100);
+    # below, a double-float value resolves about 2^-149
+    full = ref >= 2.0 ** -100
+    rel = np.abs(got - ref) / ref
+    assert rel[full].max() < 3e-14, (rel[full].max(), x[full][np.argmax(rel[full])])
+    assert np.all(np.abs(got - ref)[~full] <= 4 * 2.0 ** -149 + 3e-14 * ref[~full])
+    assert fb == 0
+    # an intermediate beyond the double-float range (the sums themselves are
+    # combined in double-float and stay below 3.4e38): re-evaluated in FP64
+    big = np.array([89.5, 95.0, 300.0], dtype=np.float64)
+    got, fb = _per_value(backend, "(exp(x)*exp(-(x)))", big[None, :], ["x"])
+    assert fb == 1 and np.allclose(got, 1.0, rtol=1e-15)
+    tiny, _ = _per_value(backend, "exp(x)", np.array([[-110.0, -1e4]]), ["x"])
+    assert np.all(tiny == 0.0)
+    # pow: positive bases, real exponents
+    a = rng.uniform(1e-3, 30.0, 20000).astype(np.float32).astype(np.float64)
+    b = rng.uniform(-8.0, 8.0, 20000).astype(np.float32).astype(np.float64)
+    got, _ = _per_value(backend, "pow(a,b)", np.vstack([a, b]), ["a", "b"])
+    ref = np.power(a, b)
+    rel = np.abs(got - ref) / ref
+    bound = (np.abs(b * np.log(a)) + 1.0) * 3e-14
+    assert np.all(rel <= bound), (rel / bound).max()
+    # negative bases with integer exponents, zero, special exponents
+    a = np.array([-2.0, -2.0, -3.5, -0.5, 0.0, 0.0, 0.0, 7.0, -7.0, -2.0, 1.0])
+    b = np.array([3.0, 4.0, 2.0, -3.0, 2.5, -1.5, 0.0, 0.0, 0.0, 0.5, 123.25])
+    got, _ = _per_value(backend, "pow(a,b)", np.vstack([a, b]), ["a", "b"])
+    with np.errstate(invalid="ignore", divide="ignore"):
+        ref = np.power(a, b)
+    fin = np.isfinite(ref)
+    np.testing.assert_allclose(got[fin], ref[fin], rtol=1e-13)
+    # an infinite term leaves a compensated sum non-finite (inf or NaN: the
+    # reference's Kahan step turns inf into NaN at the next term as well)
+    assert not np.isfinite(got[~fin]).any()
+
+
 def test_double_float_range_falls_back_to_native_fp64(backend):
     """At the 1000-event cbpoly minimum (alpha 0.95, n 8.5) the Hessian's tail
     terms reach pow(base, n)^4 ~ 1e52, beyond the FP32 exponent range of a
