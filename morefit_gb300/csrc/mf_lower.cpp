@@ -821,6 +821,27 @@ __device__ __forceinline__ bool mf_dw_lt(mf_dw a, mf_dw b) { return a.h < b.h ||
 __device__ __forceinline__ bool mf_dw_ge(mf_dw a, mf_dw b) { return a.h > b.h || (a.h == b.h && a.l >= b.l); }
 __device__ __forceinline__ bool mf_dw_le(mf_dw a, mf_dw b) { return a.h < b.h || (a.h == b.h && a.l <= b.l); }
 __device__ __forceinline__ bool mf_dw_eq(mf_dw a, mf_dw b) { return a.h == b.h && a.l == b.l; }
+// A sum of logarithms as the logarithm of a running product (per thread):
+// m * 2^e with m kept in [1, 2) by an exact power-of-two rescaling and the
+// binary exponent e in an integer, so each factor costs one double-float
+// product instead of a logarithm. A factor that is not positive (or NaN), or
+// a product outside the FP32 normal range, makes m NaN for good; the
+// thread's sum is then NaN, as a sum of the logs would be non-finite.
+__device__ __forceinline__ void mf_dw_logprod(mf_dw& m, int& e, mf_dw p) {
+  const mf_dw q = mf_dw_mul(m, p);
+  const int ex = (int)((__float_as_uint(q.h) >> 23) & 0xffu);
+  const float sc = __uint_as_float((unsigned)(254 - ex) << 23);  // 2^(127 - ex) for ex in [1, 253]
+  const bool ok = p.h > 0.0f && ex > 0 && ex < 254;
+  m = ok ? mf_dw_make(__fmul_rn(q.h, sc), __fmul_rn(q.l, sc)) : mf_dw_make(__int_as_float(0x7fc00000), 0.0f);
+  e += ex - 127;
+}
+// log(m * 2^e) = log(m) + e ln2, ln2 as a double-float pair (e exact in FP32);
+// a thread without factors (m = 1, e = 0) contributes exactly 0.
+__device__ __forceinline__ mf_dw mf_dw_logprod_log(mf_dw m, int e, const float4* __restrict__ tab) {
+  if (e == 0 && m.h == 1.0f && m.l == 0.0f) return mf_dw_make(0.0f, 0.0f);
+  const mf_dw el = mf_dw_mul(mf_dw_make((float)e, 0.0f), mf_dw_make(MF_LN2_HI, MF_LN2_LO));
+  return mf_dw_add(mf_dw_log(m, tab), el);
+}
 __device__ __forceinline__ mf_dw mf_dw_shfl_xor(mf_dw a, int o) {
   return mf_dw_make(__shfl_xor_sync(0xffffffffu, a.h, o), __shfl_xor_sync(0xffffffffu, a.l, o));
 }
@@ -1174,6 +1195,7 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
     std::vector<char> skip(ns.size(), 0);
     std::map<int, std::vector<std::pair<int, int>>> chains;  // chain root -> its terms (a, b)
     std::vector<std::pair<int, int>> fused(roots.size(), {-1, -1});
+    std::vector<int> logprod(roots.size(), -1);  // output j = log(node) summed as a running product
     if (ar == Ar::DW && kind == Kind::Reduce) {
       for (size_t i = 0; i < ns.size(); i++) {
         if (!live[i] || ns[i].uniform || ns[i].op == Op::Input) continue;
@@ -1228,6 +1250,12 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
         const Node& n = ns[r];
         if (n.op == Op::Mul && !n.uniform && uses[r] == 1 && !chains.count(r) && !skip[r]) {
           fused[j] = {n.a, n.b};
+          skip[r] = 1;
+        }
+        // an output that is the logarithm of a per-event value, used nowhere
+        // else: sum of logs = log of the product (one multiply per event)
+        if (n.op == Op::Log && !n.uniform && uses[r] == 1 && !skip[r]) {
+          logprod[j] = n.a;
           skip[r] = 1;
         }
       }
@@ -1430,6 +1458,14 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
         o << "  double acc[MF_NOUT];\n#pragma unroll\n  for (int j = 0; j < MF_NOUT; j++) acc[j] = 0.0;\n";
       else
         o << "  mf_dw acc[MF_NOUT];\n#pragma unroll\n  for (int j = 0; j < MF_NOUT; j++) acc[j] = mf_dw_make(0.0f, 0.0f);\n";
+      for (int j = 0; j < M; j++)
+        if (logprod[j] >= 0) o << "  mf_dw lpm" << j << " = mf_dw_make(1.0f, 0.0f);\n  int lpe" << j << " = 0;\n";
+    };
+    // Per-thread partials of the log-product outputs, before the block reduction.
+    auto acc_finish = [&](std::ostringstream& o) {
+      for (int j = 0; j < M; j++)
+        if (logprod[j] >= 0)
+          o << "  acc[" << j << "] = mf_dw_logprod_log(lpm" << j << ", lpe" << j << ", mf_logtab);\n";
     };
     auto acc_add = [&](std::ostringstream& o, const std::string& ind) {
       for (int j = 0; j < M; j++) {
@@ -1438,6 +1474,8 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
           o << ind << "mf_kahan_f32(acc[" << j << "], cmp[" << j << "], " << r << ");\n";
         else if (ar == Ar::F64)
           o << ind << "acc[" << j << "] += " << r << ";\n";
+        else if (logprod[j] >= 0)
+          o << ind << "mf_dw_logprod(lpm" << j << ", lpe" << j << ", " << eref(logprod[j]) << ");\n";
         else if (fused[j].first >= 0)
           o << ind << "mf_dw_acc_mul(acc[" << j << "], " << eref(fused[j].first) << ", " << eref(fused[j].second)
             << ");\n";
@@ -1494,6 +1532,7 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
     s << "extern \"C\" __global__ void __launch_bounds__(MF_BLOCK) " << out.entry << "(const " << DT
       << "* __restrict__ data, mf_u64 stride, mf_u64 n, mf_args P, float2* __restrict__ partials,"
       << " unsigned* __restrict__ counter, double* __restrict__ out, unsigned* __restrict__ status) {\n";
+    const auto body_mark = s.tellp();
     s << "  mf_launch_dependents();  // the next evaluation may start its event loop on SMs this grid frees\n";
     load_table(s);
     prologue(s, "P.");
@@ -1588,35 +1627,27 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
       s << "  }\n";
     }
     s << "  __shared__ float2 red[MF_NOUT][MF_BLOCK / 32];\n  __shared__ bool am_last;\n";
+    acc_finish(s);
     block_reduce(s);
-    s << R"CUDA(  // Launched as a programmatic dependent of the previous evaluation on the
-  // stream (batched evaluations), this grid ran its event loop while that
-  // one finished; the scratch below is shared, so wait for it to complete.
-  mf_grid_dependency_wait();
-  for (int j = threadIdx.x; j < MF_NOUT; j += MF_BLOCK) partials[(mf_u64)blockIdx.x * MF_NOUT + j] = mf_blk[j];
-  // Completion count with release/acquire semantics: the barrier orders the
-  // block's partial writes before thread 0's release; the last block's
-  // acquire plus the barrier orders its reads of every partial after.
-  __syncthreads();
-  if (threadIdx.x == 0) am_last = (mf_atom_add_acq_rel(counter, 1u) == gridDim.x - 1);
-  __syncthreads();
-  if (!am_last) return;
-  // Fixed-order double-float combine of the block partials by the whole last
-  // block: thread t takes blocks t, t + MF_BLOCK, ... for every output (all
-  // loads of a round issued before the adds), then a warp tree and a pass
-  // over the warps in order. The order depends only on the grid size.
-  {
+    // the per-block work, shared by the single-evaluation and the batched entry
+    const std::string body_text = s.str().substr(size_t(body_mark));
+    // Fixed-order double-float combine of mf_nb partial rows (partials) into
+    // out[]: thread t takes rows t, t + MF_BLOCK, ... for every output (all
+    // loads of a round issued before the adds), then a warp tree and a pass
+    // over the warps in order. The order depends only on mf_nb, the grid size
+    // of the evaluation. Uses red[][], lane and warp.
+    const std::string combine_text = R"CUDA(  {
     mf_dw s[MF_NOUT];
 #pragma unroll
     for (int j = 0; j < MF_NOUT; j++) s[j] = mf_dw_make(0.0f, 0.0f);
-    for (unsigned b0 = 0; b0 < gridDim.x; b0 += MF_Q * MF_BLOCK) {
+    for (unsigned b0 = 0; b0 < mf_nb; b0 += MF_Q * MF_BLOCK) {
       float2 v[MF_Q][MF_NOUT];
 #pragma unroll
       for (int q = 0; q < MF_Q; q++) {
         const unsigned b = b0 + q * MF_BLOCK + threadIdx.x;
 #pragma unroll
         for (int j = 0; j < MF_NOUT; j++)
-          v[q][j] = b < gridDim.x ? __ldcg(partials + (mf_u64)b * MF_NOUT + j) : make_float2(0.0f, 0.0f);
+          v[q][j] = b < mf_nb ? __ldcg(partials + (mf_u64)b * MF_NOUT + j) : make_float2(0.0f, 0.0f);
       }
 #pragma unroll
       for (int q = 0; q < MF_Q; q++)
@@ -1637,9 +1668,47 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
       out[j] = mf_dw_to_double(b);
     }
   }
-  if (threadIdx.x == 0) *counter = 0u;
-}
 )CUDA";
+    s << R"CUDA(  // Launched as a programmatic dependent of the previous evaluation on the
+  // stream (batched evaluations), this grid ran its event loop while that
+  // one finished; the scratch below is shared, so wait for it to complete.
+  mf_grid_dependency_wait();
+  for (int j = threadIdx.x; j < MF_NOUT; j += MF_BLOCK) partials[(mf_u64)blockIdx.x * MF_NOUT + j] = mf_blk[j];
+  // Completion count with release/acquire semantics: the barrier orders the
+  // block's partial writes before thread 0's release; the last block's
+  // acquire plus the barrier orders its reads of every partial after.
+  __syncthreads();
+  if (threadIdx.x == 0) am_last = (mf_atom_add_acq_rel(counter, 1u) == gridDim.x - 1);
+  __syncthreads();
+  if (!am_last) return;
+  const unsigned mf_nb = gridDim.x;
+)CUDA" << combine_text << "  if (threadIdx.x == 0) *counter = 0u;\n}\n";
+    // ---- batched evaluations: per-block partials only, then one combine ----
+    // Evaluation e of a batch writes its partial rows to its own slot of the
+    // batch's partial buffer without counting or combining, so consecutive
+    // evaluations' grids overlap (each waits for its predecessor only after
+    // its own work); <entry>_combine then reduces every evaluation's rows
+    // (one block each, the same fixed order: the sums equal the
+    // single-evaluation entry's).
+    s << "extern \"C\" __global__ void __launch_bounds__(MF_BLOCK) " << out.entry << "_part(const " << DT
+      << "* __restrict__ data, mf_u64 stride, mf_u64 n, mf_args P, float2* __restrict__ partials,"
+      << " unsigned* __restrict__ status) {\n"
+      << body_text
+      << "  for (int j = threadIdx.x; j < MF_NOUT; j += MF_BLOCK) partials[(mf_u64)blockIdx.x * MF_NOUT + j] = mf_blk[j];\n"
+      << "  // complete only after the previous evaluation's grid: completions stay in\n"
+      << "  // stream order, so the combine launch after the last evaluation sees every partial\n"
+      << "  mf_grid_dependency_wait();\n"
+      << "}\n";
+    s << "extern \"C\" __global__ void __launch_bounds__(MF_BLOCK) " << out.entry
+      << "_combine(const float2* __restrict__ partials_all, mf_u64 pstride, const unsigned* __restrict__ grids,"
+      << " double* __restrict__ out_all, unsigned count) {\n"
+      << "  const unsigned e = blockIdx.x;\n  if (e >= count) return;\n"
+      << "  const unsigned mf_nb = grids[e];\n"
+      << "  const float2* __restrict__ partials = partials_all + (mf_u64)e * pstride;\n"
+      << "  double* __restrict__ out = out_all + (mf_u64)e * MF_NOUT;\n"
+      << "  __shared__ float2 red[MF_NOUT][MF_BLOCK / 32];\n"
+      << "  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;\n"
+      << combine_text << "}\n";
 
     // ---- ragged segments: one block per segment ----
     s << "extern \"C\" __global__ void __launch_bounds__(MF_BLOCK) " << out.entry << "_segments(const " << DT
@@ -1659,6 +1728,7 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
     body(s, "    ");
     acc_add(s, "    ");
     s << "  }\n";
+    acc_finish(s);
     block_reduce(s);
     s << R"CUDA(  for (int j = threadIdx.x; j < MF_NOUT; j += MF_BLOCK)
     out[(mf_u64)seg * MF_NOUT + j] = mf_dw_to_double(mf_dw_make(mf_blk[j].x, mf_blk[j].y));

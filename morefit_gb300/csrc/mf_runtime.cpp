@@ -209,6 +209,12 @@ struct mf_context {
   // the copy out of it (recorded event) has completed
   void* load_stage[2] = {nullptr, nullptr};
   cudaEvent_t load_done[2] = {nullptr, nullptr};
+  // batched evaluations: one slot of per-block partials per evaluation of a
+  // chunk, and the chunk's grid sizes
+  float2* ring = nullptr;
+  size_t ring_cap = 0;  // float2
+  unsigned* ring_grids = nullptr;
+  size_t ring_grids_cap = 0;
 };
 
 // A copy of a buffer's columns in the layout a REDUCE kernel reads (folded
@@ -270,6 +276,8 @@ struct mf_kernel {
   cudaKernel_t fn = nullptr;
   cudaKernel_t fn_seg = nullptr;
   cudaKernel_t fn_prep = nullptr;  // REDUCE kernels reading prepared columns
+  cudaKernel_t fn_part = nullptr;     // REDUCE: per-block partials only (batched evaluations)
+  cudaKernel_t fn_combine = nullptr;  // REDUCE: one block per batched evaluation
   uint64_t prep_key = 0;
   int blocks_per_sm = 1;
   int max_input = -1;
@@ -300,6 +308,8 @@ void release_context(mf_context* c) {
   if (c->out_host) cudaFreeHost(c->out_host);
   if (c->status_host) cudaFreeHost(c->status_host);
   if (c->stage_dev) cudaFree(c->stage_dev);
+  if (c->ring) cudaFree(c->ring);
+  if (c->ring_grids) cudaFree(c->ring_grids);
   for (int i = 0; i < 2; i++) {
     if (c->load_stage[i]) cudaFreeHost(c->load_stage[i]);
     if (c->load_done[i]) cudaEventDestroy(c->load_done[i]);
@@ -800,13 +810,21 @@ int mf_kernel_build(mf_context* c, const mf_kernel_desc* d, mf_kernel** out) {
   MF_CUDA_TRY(cudaLibraryGetKernel(&k->fn, k->lib, k->lowered.entry.c_str()));
   if (d->kind == MF_KERNEL_REDUCE || d->kind == MF_KERNEL_GENERATE)
     MF_CUDA_TRY(cudaLibraryGetKernel(&k->fn_seg, k->lib, (k->lowered.entry + "_segments").c_str()));
+  if (d->kind == MF_KERNEL_REDUCE) {
+    MF_CUDA_TRY(cudaLibraryGetKernel(&k->fn_part, k->lib, (k->lowered.entry + "_part").c_str()));
+    MF_CUDA_TRY(cudaLibraryGetKernel(&k->fn_combine, k->lib, (k->lowered.entry + "_combine").c_str()));
+  }
   if (k->lowered.prep) {
     MF_CUDA_TRY(cudaLibraryGetKernel(&k->fn_prep, k->lib, (k->lowered.entry + "_prep").c_str()));
     k->prep_key = prep_key(k.get());
   }
-  if (k->lowered.smem_bytes > 48 * 1024)
+  if (k->lowered.smem_bytes > 48 * 1024) {
     MF_CUDA_TRY(cudaFuncSetAttribute(reinterpret_cast<const void*>(k->fn), cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      int(k->lowered.smem_bytes)));
+    if (k->fn_part)
+      MF_CUDA_TRY(cudaFuncSetAttribute(reinterpret_cast<const void*>(k->fn_part),
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, int(k->lowered.smem_bytes)));
+  }
   int nb = 0;
   MF_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, reinterpret_cast<const void*>(k->fn),
                                                             k->lowered.block, k->lowered.smem_bytes));
@@ -1109,6 +1127,80 @@ int launch_reduce(mf_kernel* k, const void* data, uint64_t stride, uint64_t n, c
   return MF_OK;
 }
 
+// Batched evaluations in chunks of up to kChunk: evaluation e of a chunk
+// writes its per-block partials to slot e of the context's partial buffer
+// (the _part entry, no waiting, no counter), consecutive grids overlapping
+// as programmatic dependent launches; one _combine launch per chunk then
+// reduces each evaluation's partials in the fixed order of the
+// single-evaluation entry. A chunk's first launch waits for everything
+// before it on the stream (its slots were the previous chunk's).
+int launch_batched(mf_kernel* k, uint32_t count, const void* const* data, const uint64_t* strides,
+                   const uint64_t* ns, const double* params, mf_buffer* out) {
+  constexpr uint32_t kChunk = 256;
+  mf_context* c = k->ctx;
+  int maxgrid = 1;
+  for (uint32_t i = 0; i < count; i++) maxgrid = std::max(maxgrid, grid_for(k, ns[i]));
+  const uint32_t chunk = std::min(count, kChunk);
+  const uint64_t pstride = uint64_t(maxgrid) * k->n_outputs;  // float2 per evaluation
+  if (c->ring_cap < chunk * pstride) {
+    if (c->ring) {
+      MF_CUDA_TRY(cudaStreamSynchronize(c->stream));
+      cudaFree(c->ring);
+    }
+    c->ring = nullptr;
+    c->ring_cap = 0;
+    MF_CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&c->ring), size_t(chunk * pstride) * sizeof(float2)));
+    c->ring_cap = size_t(chunk * pstride);
+  }
+  if (c->ring_grids_cap < kChunk) {
+    MF_CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&c->ring_grids), kChunk * sizeof(unsigned)));
+    c->ring_grids_cap = kChunk;
+  }
+  const size_t ab = k->lowered.args_bytes();
+  std::vector<unsigned char> pv(ab, 0);
+  std::vector<unsigned> grids(chunk);
+  unsigned* status = c->status;
+  for (uint32_t first = 0; first < count; first += chunk) {
+    const uint32_t m = std::min(chunk, count - first);
+    for (uint32_t i = 0; i < m; i++) {
+      const uint32_t e = first + i;
+      grids[i] = unsigned(grid_for(k, ns[e]));
+      try {
+        k->lowered.fill_args(params + uint64_t(e) * k->n_params, k->n_params, pv.data());
+      } catch (const std::exception& ex) {
+        return fail(MF_ERR_INVALID, std::string("parameter evaluation: ") + ex.what());
+      }
+      const void* d = data[e];
+      uint64_t stride = strides[e], n = ns[e];
+      float2* slot = c->ring + uint64_t(i) * pstride;
+      void* args[] = {const_cast<void**>(&d), &stride, &n, pv.data(), &slot, &status};
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(grids[i]);
+      cfg.blockDim = dim3(k->lowered.block);
+      cfg.dynamicSmemBytes = k->lowered.smem_bytes;
+      cfg.stream = c->stream;
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+      attr[0].val.programmaticStreamSerializationAllowed = 1;
+      cfg.attrs = attr;
+      cfg.numAttrs = i > 0 ? 1 : 0;
+      MF_CUDA_TRY(cudaLaunchKernelExC(&cfg, reinterpret_cast<const void*>(k->fn_part), args));
+    }
+    // pageable source: the copy is staged before the call returns
+    MF_CUDA_TRY(cudaMemcpyAsync(c->ring_grids, grids.data(), m * sizeof(unsigned), cudaMemcpyHostToDevice,
+                                c->stream));
+    const float2* ring = c->ring;
+    uint64_t ps = pstride;
+    const unsigned* g = c->ring_grids;
+    double* o = static_cast<double*>(out->ptr) + uint64_t(first) * k->n_outputs;
+    uint32_t mm = m;
+    void* cargs[] = {const_cast<float2**>(&ring), &ps, const_cast<unsigned**>(&g), &o, &mm};
+    MF_CUDA_TRY(cudaLaunchKernel(reinterpret_cast<const void*>(k->fn_combine), dim3(m), dim3(k->lowered.block),
+                                 cargs, 0, c->stream));
+  }
+  return MF_OK;
+}
+
 }  // namespace mfi
 
 namespace {
@@ -1224,6 +1316,7 @@ int mf_kernel_reduce_many(mf_kernel* k, uint32_t count, const mf_buffer* const* 
     rc = prepare_input(k, inputs[i], strides[i], &data[i]);
     if (rc) return rc;
   }
+  if (!one_by_one && count > 1) return mfi::launch_batched(k, count, data.data(), strides, ns, params, out);
   for (uint32_t i = 0; i < count; i++) {
     if (one_by_one) {
       rc = prepare_input(k, inputs[i], strides[i], &data[i]);

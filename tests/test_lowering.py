@@ -27,8 +27,11 @@ def test_shared_subexpressions_evaluated_once():
     assert body.count("__drcp_rn(") == 2
     dw = _src(g, "lh_grad_kernel", L.MF_F64)
     body = _entry(dw, "void __launch_bounds__(MF_BLOCK) mf_reduce(")
-    # double-float kernel: two events per thread, one log and one reciprocal each
-    assert body.count("mf_dw_log(") == 2 and body.count("mf_dw_rcp(") == 2
+    # double-float kernel: two events per thread, one reciprocal each; the
+    # NLL output log(p) is summed as the log of a running product (one factor
+    # per event, one logarithm per thread)
+    assert body.count("mf_dw_log(") == 0 and body.count("mf_dw_rcp(") == 2
+    assert body.count("mf_dw_logprod(") == 2 and body.count("mf_dw_logprod_log(") == 1
     assert " log(" not in body
     # the event loop reads the 9 folded basis columns as float pairs
     assert "data + (mf_u64)8 * stride" in body and "data + (mf_u64)9 * stride" not in body
