@@ -54,9 +54,12 @@ def _peaks():
 
 # dram__bytes_read.sum + dram__bytes_write.sum of one lh_grad launch (FP64
 # storage, double-float arithmetic, 9 prepared columns, 1M events) from the
-# full ncu capture summarised in profiles/mf_reduce_lh_grad_pwave_1M.md.
-NCU_TRAFFIC_F64 = 72.046336e6 + 0.542976e6
-NCU_TRAFFIC_SOURCE = "ncu --set full, one launch, profiles/mf_reduce_lh_grad_pwave_1M.md"
+# full ncu capture summarised in profiles/mf_reduce_part_lh_grad_pwave_1M.md
+# (mf_reduce_part: the entry batched evaluations launch).
+NCU_TRAFFIC_F64 = 72.026368e6 + 0.440832e6
+NCU_TRAFFIC_SOURCE = "ncu --set full, one mf_reduce_part launch, profiles/mf_reduce_part_lh_grad_pwave_1M.md"
+# evaluations per combine launch of mf_kernel_reduce_many (mf_runtime.cpp, launch_batched)
+COMBINE_CHUNK = 256
 
 
 class ClockSampler:
@@ -511,7 +514,9 @@ def ours(args):
                 "extras": extras,
                 "cpu_baseline": cpu,
                 "clocks": clk.summary(),
-                "gpu_launches": args.steps, "nll_truth": float(-2.0 * res64[0])}
+                # K per-evaluation launches plus one combine per COMBINE_CHUNK
+                "gpu_launches": args.steps + math.ceil(args.steps / COMBINE_CHUNK),
+                "nll_truth": float(-2.0 * res64[0])}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
