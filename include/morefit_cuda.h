@@ -395,6 +395,11 @@ int mf_expr_set_free(mf_expr_set* set);
  * (include/random.hh:355-362), row t = the state after t jump() calls
  * (include/random.hh:395-420). out is SoA [4][nrows]. */
 int mf_seed_rows(uint64_t seed, uint32_t nrows, uint32_t* out);
+/* Independent xoshiro128++ states for generations that need no reference
+ * partition (toy datasets at their own truths, serving): row r = the upper
+ * halves of four SplitMix64 outputs from (seed mod 2^32) * 2^32 + r.
+ * out is SoA [4][nrows]. */
+int mf_splitmix_seed_rows(uint64_t seed, uint32_t nrows, uint32_t* out);
 
 /* Work partition of the reference's accelerator generator for n events with
  * at most max_workitems generator threads (compute_opencl.hh:437-445,

@@ -441,6 +441,9 @@ std::vector<char> reachable(const std::vector<Node>& ns, const std::vector<int>&
 struct Emitter {
   const std::vector<Node>& ns;
   bool f32;  // arithmetic type float
+  // FP64 bodies: exp, log, sqrt, sin, cos and pow through the double-float
+  // functions (mf_fast_*, FP32 pipe) instead of FP64 calls
+  bool fast = false;
   std::string T() const { return f32 ? "float" : "double"; }
   std::string ref(int id, const std::string& pfx) const {
     const Node& n = ns[id];
@@ -461,9 +464,18 @@ struct Emitter {
       case Op::Div: return lhs + A(n.a) + " / " + A(n.b) + ";";
       case Op::Neg: return lhs + "-" + A(n.a) + ";";
       case Op::Rcp: return lhs + fn_name(Op::Rcp, f32) + "(" + A(n.a) + ");";
-      case Op::Pow: return lhs + fn_name(Op::Pow, f32) + "(" + A(n.a) + ", " + A(n.b) + ");";
+      case Op::Pow:
+        if (fast && !f32) return lhs + "mf_fast_pow(" + A(n.a) + ", " + A(n.b) + ");";
+        return lhs + fn_name(Op::Pow, f32) + "(" + A(n.a) + ", " + A(n.b) + ");";
       case Op::Cmp: return lhs + "(" + A(n.a) + " " + cmp_str(n.cmp) + " " + A(n.b) + ");";
       case Op::Select: return lhs + "(" + A(n.a) + " ? " + A(n.b) + " : " + A(n.c) + ");";
+      case Op::Exp:
+      case Op::Log:
+      case Op::Sqrt:
+      case Op::Sin:
+      case Op::Cos:
+        if (fast && !f32) return lhs + "mf_fast_" + fn_name(n.op, false) + "(" + A(n.a) + ");";
+        return lhs + fn_name(n.op, f32) + "(" + A(n.a) + ");";
       default:
         if (is_unary_fn(n.op)) return lhs + fn_name(n.op, f32) + "(" + A(n.a) + ");";
         throw std::runtime_error("emit: unexpected node");
@@ -1789,6 +1801,19 @@ __device__ __forceinline__ unsigned mf_xoshiro(unsigned* s) {
   return r;
 }
 )CUDA";
+    if (!ar32) {
+      s << dw_log_table() << kDwPrelude;
+      s << R"CUDA(__device__ __forceinline__ double mf_fast_join(mf_dw a) { return mf_dw_to_double_bits(a); }
+__device__ __forceinline__ double mf_fast_exp(double x) { return mf_fast_join(mf_dw_exp(mf_dw_split_rn(x), mf_dw_exptab_g)); }
+__device__ __forceinline__ double mf_fast_log(double x) { return mf_fast_join(mf_dw_log(mf_dw_split_rn(x), mf_dw_logtab_g)); }
+__device__ __forceinline__ double mf_fast_sqrt(double x) { return mf_fast_join(mf_dw_sqrt(mf_dw_split_rn(x))); }
+__device__ __forceinline__ double mf_fast_sin(double x) { return mf_fast_join(mf_dw_sin(mf_dw_split_rn(x))); }
+__device__ __forceinline__ double mf_fast_cos(double x) { return mf_fast_join(mf_dw_cos(mf_dw_split_rn(x))); }
+__device__ __forceinline__ double mf_fast_pow(double a, double b) {
+  return mf_fast_join(mf_dw_pow(mf_dw_split_rn(a), mf_dw_split_rn(b), mf_dw_logtab_g, mf_dw_exptab_g));
+}
+)CUDA";
+    }
     s << "extern \"C\" __global__ void __launch_bounds__(MF_BLOCK) " << out.entry
       << "(const unsigned* __restrict__ seeds, unsigned nseeds, mf_u64 n, mf_u64 nper, mf_par P, " << ST
       << "* __restrict__ outp, mf_u64 out_stride, unsigned* __restrict__ status, unsigned long long max_tries) {\n";
@@ -1807,6 +1832,14 @@ __device__ __forceinline__ unsigned mf_xoshiro(unsigned* s) {
     };
     const char* mul = ar32 ? "__fmul_rn" : "__dmul_rn";
     const char* add = ar32 ? "__fadd_rn" : "__dadd_rn";
+    // FP64 generation: the density's exp/log/sqrt/sin/cos/pow through the
+    // double-float functions (FP32 pipe; relative error ~1e-14), and the
+    // accept decision maxprob*u < p recomputed with the density in exact
+    // FP64 (the code the reference runs) whenever |maxprob*u - p| is within
+    // 1e-9 * maxprob or p is NaN. Elsewhere the fast density is far inside
+    // that margin of the exact one, so every decision -- and every generated
+    // event -- equals the FP64 one.
+    const bool fast_density = !ar32;
     auto accept_reject = [&]() {
       s << "  unsigned long long tries = 0;\n";
       s << "  for (mf_u64 i = from; i < to; i++) {\n    for (;;) {\n";
@@ -1816,8 +1849,20 @@ __device__ __forceinline__ unsigned mf_xoshiro(unsigned* s) {
           << mul << "(" << fmt_const(printed15(gen->hi[d] - gen->lo[d]), ar32) << ", (" << AT
           << ")(mf_xoshiro(st) * 2.3283064365386963e-10)));\n";
       }
-      emit_body(s, "      ");
-      s << "      if (" << mul << "(maxprob, (" << AT << ")(mf_xoshiro(st) * 2.3283064365386963e-10)) < r0) {\n";
+      if (fast_density) {
+        em.fast = true;
+        emit_body(s, "      ");
+        em.fast = false;
+        s << "      const double mf_ug = " << mul << "(maxprob, (double)(mf_xoshiro(st) * 2.3283064365386963e-10));\n";
+        s << "      double mf_p = r0;\n";
+        s << "      if (!(fabs(mf_ug - mf_p) > 1e-9 * maxprob)) {  // near the boundary: exact FP64 density\n";
+        emit_body(s, "        ");
+        s << "        mf_p = r0;\n      }\n";
+        s << "      if (mf_ug < mf_p) {\n";
+      } else {
+        emit_body(s, "      ");
+        s << "      if (" << mul << "(maxprob, (" << AT << ")(mf_xoshiro(st) * 2.3283064365386963e-10)) < r0) {\n";
+      }
       for (int d = 0; d < D; d++)
         s << "        outp[(mf_u64)" << d << " * out_stride + i] = (" << ST << ")x" << d << ";\n";
       s << "        break;\n      }\n    }\n  }\n}\n";

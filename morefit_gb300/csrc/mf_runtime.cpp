@@ -973,6 +973,20 @@ int mf_expr_set_free(mf_expr_set* set) {
   return MF_OK;
 }
 
+int mf_splitmix_seed_rows(uint64_t seed, uint32_t nrows, uint32_t* out) {
+  if (!out && nrows) return fail(MF_ERR_INVALID, "null argument");
+  for (uint32_t r = 0; r < nrows; r++) {
+    uint64_t sm = (seed & 0xffffffffULL) * (1ULL << 32) + r;
+    for (int k = 0; k < 4; k++) {
+      uint64_t z = (sm += 0x9e3779b97f4a7c15ULL);
+      z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+      z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+      out[uint64_t(k) * nrows + r] = uint32_t((z ^ (z >> 31)) >> 32);
+    }
+  }
+  return MF_OK;
+}
+
 int mf_seed_rows(uint64_t seed, uint32_t nrows, uint32_t* out) {
   if (!out && nrows) return fail(MF_ERR_INVALID, "null argument");
   // Splitmix64 seeding of four 32-bit words (upper halves), then xoshiro128++

@@ -31,23 +31,8 @@ import numpy as np
 
 from . import _lib as L
 from .backend import CUDABackend, CUDABlock, DeviceColumns
-from .workloads import Likelihood, load_spec
+from .workloads import Likelihood, load_spec, splitmix_seed_rows
 
-
-def splitmix_seed_rows(nrows: int, seed: int) -> np.ndarray:
-    """xoshiro128++ states (SoA [4][nrows]) seeded independently per stream:
-    the upper halves of four SplitMix64 outputs from seed * 2^32 + row."""
-    with np.errstate(over="ignore"):
-        st = np.uint64(seed & 0xFFFFFFFF) * np.uint64(1 << 32) + np.arange(nrows, dtype=np.uint64)
-        out = np.zeros((4, nrows), dtype=np.uint32)
-        for k in range(4):
-            st = st + np.uint64(0x9E3779B97F4A7C15)
-            z = st
-            z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
-            z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
-            z = z ^ (z >> np.uint64(31))
-            out[k] = (z >> np.uint64(32)).astype(np.uint32)
-    return out
 
 MODEL_LIMITS = {
     "mass": [(5200.0, 5400.0), (5.0, 50.0), (0.0, 1.0), (-0.01, 0.01)],

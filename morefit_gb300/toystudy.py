@@ -32,7 +32,7 @@ import re
 
 from . import _lib as L
 from .backend import CUDABackend, CUDABlock, DeviceColumns, eval_expressions_batch
-from .workloads import DEFAULT_SEED, Likelihood, generate_events, seed_rows
+from .workloads import DEFAULT_SEED, Likelihood, generate_events, splitmix_seed_rows
 
 # Parameter limits of the K*mumu P-wave fit (Fl in [0, 1], the rest in [-1, 1]),
 # as the reference's benchmark drivers declare them.
@@ -172,12 +172,18 @@ def pwave_maxprob(theta: np.ndarray) -> np.ndarray:
 def generate_segments(backend: CUDABackend, spec: dict, theta: np.ndarray, counts, maxprob: np.ndarray,
                       seed: int = DEFAULT_SEED, threads_per_seg: int = 16) -> DeviceColumns:
     """Events of many datasets, dataset s at parameters theta[s] (one launch):
-    dataset s owns events [begin[s], begin[s] + counts[s]) of the returned block."""
+    dataset s owns events [begin[s], begin[s] + counts[s]) of the returned block.
+    Stream r of segment s is seeded independently (SplitMix64 of seed and the
+    stream's index), so a segment's events depend only on its own streams."""
     expr, params, bufs = density_expression(spec)
     gk = next(k for k in spec["kernels"] if k.get("generate"))
-    blk = CUDABlock(backend, np.float64)
-    blk.MakeGenerateKernel("gen_segments", 0, [], gk["outputs"], params, [expr], 1.0,
-                           ranges=list(zip(gk["lo"], gk["hi"])))
+    cache = backend.__dict__.setdefault("_gen_segment_blocks", {})  # built once per backend and model
+    blk = cache.get((spec["workload"], expr))
+    if blk is None:
+        blk = CUDABlock(backend, np.float64)
+        blk.MakeGenerateKernel("gen_segments", 0, [], gk["outputs"], params, [expr], 1.0,
+                               ranges=list(zip(gk["lo"], gk["hi"])))
+        cache[(spec["workload"], expr)] = blk
     theta = np.ascontiguousarray(theta, dtype=np.float64)
     nfloat = theta.shape[1]
     rows = theta if len(params) == nfloat else np.concatenate(
@@ -186,7 +192,7 @@ def generate_segments(backend: CUDABackend, spec: dict, theta: np.ndarray, count
     begins = np.concatenate([[0], np.cumsum(counts, dtype=np.uint64)[:-1]]).astype(np.uint64)
     nseg = len(counts)
     nthreads = nseg * threads_per_seg
-    seeds = np.ascontiguousarray(seed_rows(nthreads, seed), dtype=np.uint32)
+    seeds = np.ascontiguousarray(splitmix_seed_rows(nthreads, seed), dtype=np.uint32)
     out = DeviceColumns(backend, L.MF_F64)
     out.ensure(len(gk["outputs"]), int(counts.sum()))
     mp = np.ascontiguousarray(maxprob, dtype=np.float64)

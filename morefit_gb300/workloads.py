@@ -246,6 +246,16 @@ def seed_rows(nrows: int, seed: int = DEFAULT_SEED) -> np.ndarray:
     return out
 
 
+def splitmix_seed_rows(nrows: int, seed: int) -> np.ndarray:
+    """xoshiro128++ states (SoA [4][nrows]) seeded independently per stream:
+    the upper halves of four SplitMix64 outputs from seed * 2^32 + row (for
+    generations that need independent streams rather than the reference's
+    jump partition, which seed_rows reproduces)."""
+    out = np.zeros((4, nrows), dtype=np.uint32)
+    L.check(L.lib.mf_splitmix_seed_rows(seed, nrows, out.ctypes.data_as(C.POINTER(C.c_uint32))))
+    return out
+
+
 def generate_partition(n: int, max_workitems: int = MAX_GENERATOR_WORKITEMS):
     nper, nseeds = C.c_uint64(), C.c_uint32()
     L.check(L.lib.mf_generate_partition(n, max_workitems, C.byref(nper), C.byref(nseeds)))

@@ -24,8 +24,9 @@
 // Usage:
 //   refkit golden <workload> <nevents> <out.json> [events.bin]
 //   refkit bench  <mass|pwave|spwave> <nevents> <nthreads> <nevals>
-//   refkit toys   <pwave> <ntoys> <mean events> <jitter> <out.json>
+//   refkit toys   <pwave> <ntoys> <mean events> <jitter> <out.json> [seed]
 //   refkit plot   <workload> <nevents> <variable> <nbins> <out.py> <out.json>
+//   refkit fitfile <workload> <datasets.bin> <out.json>
 #define MOREFIT_H 1  // keep graph.hh from pulling in the OpenCL/LLVM backends
 #include <cassert>
 #include <chrono>
@@ -669,14 +670,15 @@ static int cmd_bench(const std::string& which, unsigned n, unsigned nthreads, un
 // Each toy is generated at its truth (the generate kernel is rebuilt per toy
 // because the generator substitutes the parameter values into it,
 // generator.hh:145) and fitted from it (MIGRAD + HESSE). Writes the pulls.
-static int cmd_toys(const std::string& which, unsigned ntoys, double mean, double jitter, const std::string& out) {
+static int cmd_toys(const std::string& which, unsigned ntoys, double mean, double jitter, const std::string& out,
+                    uint64_t seed = 229387429) {
   compute_options copts;
   copts.llvm_nthreads = 1;
   copts.print_kernel = false;
   backendT backend(&copts);
   Workload w = make_workload(which);
   Xoshiro128pp rnd;
-  rnd.setSeed(int64_t(229387429));
+  rnd.setSeed(int64_t(seed));
   generator_options gen_opts;
   gen_opts.rndtype = generator_options::randomization_type::on_accelerator;
   gen_opts.print_level = 0;
@@ -685,7 +687,7 @@ static int cmd_toys(const std::string& which, unsigned ntoys, double mean, doubl
   fitter<kT, eT, backendT, blockT> fit(&fopts, &backend);
   std::vector<double> base;
   for (auto* p : w.params) base.push_back(p->get_value());
-  uint64_t sm = 0x746f79737475ULL;
+  uint64_t sm = 0x746f79737475ULL + (seed - 229387429);
   auto uni = [&sm]() {
     sm += 0x9e3779b97f4a7c15ULL;
     uint64_t z = sm;
@@ -831,8 +833,54 @@ static int cmd_plot(const std::string& which, unsigned n, const std::string& var
   return 0;
 }
 
+// Fits datasets from a file with the reference's fitter: the file holds, per
+// dataset, uint32 n, npar doubles (truth, also the start point) and the SoA
+// events (ndims x n doubles). Writes values and errors per dataset.
+static int cmd_fitfile(const std::string& which, const std::string& in, const std::string& out) {
+  compute_options copts;
+  copts.llvm_nthreads = 1;
+  copts.print_kernel = false;
+  backendT backend(&copts);
+  Workload w = make_workload(which);
+  fitter_options fopts = make_fit_opts(w);
+  fitter<kT, eT, backendT, blockT> fit(&fopts, &backend);
+  FILE* f = std::fopen(in.c_str(), "rb");
+  if (!f) return 2;
+  const size_t npar = w.params.size(), nd = w.dims.size();
+  std::string vals = "[", errs = "[";
+  std::ostringstream sink;
+  auto* old = std::cout.rdbuf(sink.rdbuf());
+  for (unsigned t = 0;; t++) {
+    uint32_t n = 0;
+    if (std::fread(&n, 4, 1, f) != 1) break;
+    std::vector<double> truth(npar);
+    if (std::fread(truth.data(), 8, npar, f) != npar) break;
+    EventVector<kT, eT> data(w.dims, n);
+    if (std::fread(data.get_data(), 8, nd * n, f) != nd * n) break;
+    for (size_t i = 0; i < npar; i++) {
+      w.params[i]->set_value(truth[i]);
+      w.params[i]->set_start_value(truth[i]);
+    }
+    fit.fit(w.pdf, w.params, &data, t > 0);
+    std::vector<double> v, e;
+    for (auto* p : w.params) {
+      v.push_back(p->get_value());
+      e.push_back(p->get_error());
+    }
+    vals += std::string(t ? "," : "") + jvec(v);
+    errs += std::string(t ? "," : "") + jvec(e);
+  }
+  std::cout.rdbuf(old);
+  std::fclose(f);
+  FILE* o = std::fopen(out.c_str(), "w");
+  std::fputs(("{\"values\":" + vals + "],\"errors\":" + errs + "]}\n").c_str(), o);
+  std::fclose(o);
+  return 0;
+}
+
 int main(int argc, char** argv) {
   install_capture();
+  if (argc >= 5 && std::string(argv[1]) == "fitfile") return cmd_fitfile(argv[2], argv[3], argv[4]);
   if (argc >= 5 && std::string(argv[1]) == "golden")
     return cmd_golden(argv[2], unsigned(std::stoul(argv[3])), argv[4], argc > 5 ? argv[5] : "");
   if (argc >= 6 && std::string(argv[1]) == "bench")
@@ -841,10 +889,12 @@ int main(int argc, char** argv) {
   if (argc >= 8 && std::string(argv[1]) == "plot")
     return cmd_plot(argv[2], unsigned(std::stoul(argv[3])), argv[4], unsigned(std::stoul(argv[5])), argv[6], argv[7]);
   if (argc >= 7 && std::string(argv[1]) == "toys")
-    return cmd_toys(argv[2], unsigned(std::stoul(argv[3])), std::stod(argv[4]), std::stod(argv[5]), argv[6]);
+    return cmd_toys(argv[2], unsigned(std::stoul(argv[3])), std::stod(argv[4]), std::stod(argv[5]), argv[6],
+                    argc > 7 ? std::stoull(argv[7]) : 229387429ULL);
   std::fprintf(stderr, "usage: refkit golden <mass|mass_w|cbpoly|pwave|spwave> <n> <out.json> [events.bin]\n"
                        "       refkit bench <mass|pwave|spwave> <n> <nthreads> <nevals>\n"
-                       "       refkit toys <pwave> <ntoys> <mean events> <jitter> <out.json>\n"
-                       "       refkit plot <workload> <n> <variable> <nbins> <out.py> <out.json>\n");
+                       "       refkit toys <pwave> <ntoys> <mean events> <jitter> <out.json> [seed]\n"
+                       "       refkit plot <workload> <n> <variable> <nbins> <out.py> <out.json>\n"
+                       "       refkit fitfile <workload> <datasets.bin> <out.json>\n");
   return 2;
 }

@@ -19,6 +19,7 @@ K="$ROOT/oracle/_ref/refkit"
 "$K" golden spwave 2000 "$HERE/spwave_n2000.json" "$HERE/spwave_n2000_events.f64"
 "$K" golden spwave 20000 "$HERE/spwave_n20000.json"
 "$K" toys pwave 1000 2000 0.1 "$HERE/toys_pwave_ref.json"
+python3 "$HERE/make_stuck_toys.py"
 # the reference's plotter (matplotlib and ROOT text, per-bin integrals)
 T="$(mktemp -d)"
 for wv in mass:m mass_w:m cbpoly:x pwave:ctl pwave:ctk pwave:phi; do

@@ -3,6 +3,8 @@
 Golden files were written by oracle/refkit: the reference's generator,
 fitter and Minuit2 running on the reference's kernel text (make_golden.sh).
 """
+from pathlib import Path
+
 import numpy as np
 import pytest
 
@@ -109,3 +111,22 @@ def test_weighted_covariance_reproduces_reference_errors(n):
     # the correction is not the unweighted 2 H^-1
     plain = np.sqrt(np.diag(2.0 * np.linalg.inv(np.reshape(pt["hessian"], (npar, npar)))))
     assert np.abs(plain / np.array(g["fit"]["errors"]) - 1.0).max() > 0.01
+
+
+def test_reference_fitter_returns_the_start_point_on_some_toys(oracle_lib):
+    """On these P-wave toy datasets (tests/golden/make_stuck_toys.py) the
+    reference's fitter, started at the truth, returns the truth unmoved and
+    reports success; the gradient of -2 ln L there is far from zero, so the
+    point is not a minimum. About one toy in ten behaves so (74 of the 1000
+    reference toys in toys_pwave_ref.json have all pulls exactly 0)."""
+    g = load_golden("toys_pwave_stuck.json")
+    raw = np.fromfile(Path(__file__).parent / "golden" / "toys_pwave_stuck_events.f64")
+    ev = raw.reshape(3, -1)
+    begins = np.concatenate([[0], np.cumsum(g["counts"])[:-1]])
+    for k, n in enumerate(g["counts"]):
+        assert g["ref_values"][k] == g["truths"][k]
+        basis = oracle_lib.pwave_basis(ev[:, begins[k]:begins[k] + n])
+        grad = -2.0 * oracle_lib.pwave_nll_grad(basis, np.array(g["truths"][k]))[1:]
+        assert np.abs(grad).max() > 50.0, grad
+    ref = np.array(load_golden("toys_pwave_ref.json")["pulls"])
+    assert 0.03 < np.all(ref == 0.0, axis=1).mean() < 0.15
