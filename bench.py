@@ -344,6 +344,25 @@ def ours(args):
     e2e_run(ke)
     e2e_s = (time.perf_counter() - t0) / ke
     e2e_rel = float(np.max(np.abs(res[:ke, 0] - res64[0])) / abs(res64[0]))
+
+    # the same steps with the raw events read in place from page-locked host
+    # memory by the precompute kernel (no separate copy to HBM)
+    def e2e_mapped_run(k):
+        for i in range(k):
+            b, lk, ob = lanes[i % 2]
+            if i >= 2:
+                b.synchronize()
+            lk.set_data_mapped(host_pinned)
+            lk.sums_async("lh_grad_kernel", truth, ob, 0)
+            L.check(L.lib.mf_buffer_d2h_async(ob, 0, res[i].ctypes.data, nout * 8))
+        for b, _, _ in lanes:
+            b.synchronize()
+
+    e2e_mapped_run(args.warmup)
+    t0 = time.perf_counter()
+    e2e_mapped_run(ke)
+    e2e_mapped_s = (time.perf_counter() - t0) / ke
+    e2e_mapped_rel = float(np.max(np.abs(res[:ke, 0] - res64[0])) / abs(res64[0]))
     # sequential form: one step at a time, each waiting for its result (latency)
     like = lanes[0][1]
     for _ in range(3):
@@ -478,7 +497,22 @@ def ours(args):
             s_cpu = gk.reduce(cols, pvh, nthreads)
             nev += 1
         cpu_s = (time.perf_counter() - t0) / nev
-        cpu = {"value": 1.0 / cpu_s, "unit": "evals/s", "cores": nthreads, "kind": "port",
+        # configuration C1: the reference's mass lh_grad kernel text on 100k events, all host threads
+        mspec = load_spec("mass")
+        mk = {k["name"]: k for k in mspec["kernels"]}
+        mev = generate_events(backend, mspec, 100_000, seed=229387429).download()
+        mgk = SpecKernel(mk["lh_grad_kernel"])
+        mlike = Likelihood(backend, mspec, np.float64)
+        mpv = mlike.param_vector("lh_grad_kernel", mspec["truth"])
+        mgk.reduce(mev, mpv, nthreads)
+        t0 = time.perf_counter()
+        mdone = 0
+        while time.perf_counter() - t0 < 3.0:
+            mgk.reduce(mev, mpv, nthreads)
+            mdone += 1
+        c1_cpu = {"value": mdone / (time.perf_counter() - t0), "unit": "evals/s", "cores": nthreads,
+                  "sample": f"{mdone} NLL+grad evaluations of the mass model over 100k events (~3 s)"}
+        cpu = {"value": 1.0 / cpu_s, "unit": "evals/s", "cores": nthreads, "kind": "port", "c1_mass_100k": c1_cpu,
                "sample": f"{nev} NLL+grad evaluations over all {n} events of dataset 0 "
                          f"(~{args.cpu_seconds:.0f} s); the reference's lh_grad kernel text compiled by gcc -O3",
                "nll_rel_diff_vs_gpu": abs(s_cpu[0] - float(like.sums('lh_grad_kernel', truth)[0])) / abs(s_cpu[0])}
@@ -504,6 +538,11 @@ def ours(args):
                         "what": "per step: upload raw events from page-locked host memory, precompute, prepare, "
                                 "NLL+grad, read sums to host; steps pipelined over two streams",
                         "nll_rel_diff_vs_device": e2e_rel},
+                "e2e_mapped": {"value": world / e2e_mapped_s, "unit": "evals/s",
+                               "h2d_bytes_per_step": int(host.nbytes), "d2h_bytes_per_step": nout * 8,
+                               "what": "the same steps, the precompute kernel reading the raw events in place from "
+                                       "page-locked host memory (mf_buffer_wrap_host) instead of a copy to HBM",
+                               "nll_rel_diff_vs_device": e2e_mapped_rel},
                 "e2e_sequential": {"value": world / seq_s, "unit": "evals/s",
                                    "h2d_bytes_per_step": int(host.nbytes), "d2h_bytes_per_step": nout * 8,
                                    "what": "the same step, one at a time, each waiting for its result"},
@@ -619,7 +658,9 @@ def extra_rows(backend):
     weighted fit (Fisher kernel, corrected covariance), the Crystal Ball +
     polynomial model, one plot (integral kernel + GPU histogram + text), and
     event input from a file (page-cached .npy streamed to HBM)."""
+    import ctypes as C
     import tempfile
+    from morefit_gb300 import _lib as L
     from morefit_gb300.eventio import save_event_vector, upload_event_file
     from morefit_gb300.plotter import Plotter, PlotterOptions
     from morefit_gb300.workloads import Likelihood, generate_events, load_spec
@@ -633,6 +674,45 @@ def extra_rows(backend):
         for _ in range(k):
             fn()
         return k / (time.perf_counter() - t0)
+
+    # configuration C1: the 1D mass fit, 100k events, 4 parameters
+    mass = load_spec("mass")
+    c1 = generate_events(backend, mass, 100_000, seed=229387429)
+    lm = Likelihood(backend, mass, np.float64)
+    lm.set_device_data(c1)
+    mlim = [(5200.0, 5400.0), (5.0, 50.0), (0.0, 1.0), (-0.01, 0.01)]
+    lm.fit(limits=mlim)  # warm: kernels built
+    t0 = time.perf_counter()
+    rm = lm.fit(limits=mlim)
+    c1_fit_ms = (time.perf_counter() - t0) * 1e3
+    kern = lm.blocks["lh_grad_kernel"].kernel
+    pv = lm.param_vector("lh_grad_kernel", mass["truth"])
+    nb = 2000
+    out_buf = L.c_buf()
+    L.check(L.lib.mf_buffer_alloc(backend.handle, nb * kern.nout * 8, C.byref(out_buf)))
+    inp = lm.blocks["lh_grad_kernel"].input
+    ins = (L.c_buf * nb)(*([inp.buf] * nb))
+    st = np.full(nb, inp.stride, dtype=np.uint64)
+    ns = np.full(nb, 100_000, dtype=np.uint64)
+    rows = np.ascontiguousarray(np.tile(pv, (nb, 1)))
+    u64p = C.POINTER(C.c_uint64)
+
+    def batch():
+        L.check(L.lib.mf_kernel_reduce_many(kern.handle, nb, ins, st.ctypes.data_as(u64p), ns.ctypes.data_as(u64p),
+                                            L.dptr(rows), len(pv), out_buf))
+        backend.synchronize()
+    batch()
+    t0 = time.perf_counter()
+    batch()
+    batched = nb / (time.perf_counter() - t0)
+    L.lib.mf_buffer_free(out_buf)
+    out["c1_mass_100k"] = {
+        "fit_ms": c1_fit_ms, "converged": bool(rm.converged[0]), "evaluations": int(rm.evaluations),
+        "grad_evals_per_s": rate(lambda: lm.sums("lh_grad_kernel", mass["truth"]), 200),
+        "batched_evals_per_s": batched,
+        "what": "Gaussian + exponential mass fit, 100k events, FP64 (double-float), 4 parameters: damped Newton "
+                "fit from the truth; synchronous evaluations; batched evaluations (2000 per call, one 0.8 MB "
+                "dataset, L2-resident)"}
 
     # weighted mass fit: the mass events plus w_i = 0.5 + frac(i * 0.618...)
     mw = load_spec("mass_w")

@@ -90,6 +90,14 @@ uint64_t mf_buffer_size(const mf_buffer* buf);
  * through it is invisible to the prepared copies REDUCE kernels keep (see
  * mf_kernel_read_layout) until mf_buffer_mark_modified is called. */
 void* mf_buffer_device_ptr(const mf_buffer* buf);
+/* A buffer over caller-owned host memory that kernels read in place (the GPU
+ * reads it over the host link while it computes; no copy to HBM): page-locked
+ * memory is used through its mapped device address, other memory is
+ * registered (mapped) until the buffer is freed. The memory must stay valid
+ * while the buffer exists; mf_buffer_free releases the buffer, not the memory.
+ * Counted in no HBM budget. For event blocks read once per step (the raw
+ * events of a precompute kernel). */
+int mf_buffer_wrap_host(mf_context* ctx, void* host, uint64_t nbytes, mf_buffer** out);
 /* Declares that the buffer's contents changed outside the library (device
  * writes through mf_buffer_device_ptr, another library's kernels). Every
  * write made through this API (copies, memsets, uploads, STORE/GENERATE

@@ -137,6 +137,7 @@ _proto("mf_kernel_read_layout", C.c_int, c_ker, C.POINTER(C.c_uint32), C.POINTER
 _proto("mf_kernel_reduce_segments", C.c_int, c_ker, c_buf, C.c_uint64, C.c_uint32, C.POINTER(C.c_uint64),
        C.POINTER(C.c_uint32), c_dbl_p, C.c_uint32, c_dbl_p)
 _proto("mf_kernel_fallback_count", C.c_int, c_ker, C.POINTER(C.c_uint64))
+_proto("mf_buffer_wrap_host", C.c_int, c_ctx, C.c_void_p, C.c_uint64, C.POINTER(c_buf))
 _proto("mf_events_load_file", C.c_int, c_buf, C.c_int, C.c_uint64, C.c_char_p, C.c_uint64, C.c_int, C.c_uint64,
        C.c_uint32, C.POINTER(C.c_uint32), C.c_uint64)
 _proto("mf_histogram", C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_uint64, C.c_double, C.c_double, C.c_uint32,
@@ -181,5 +182,5 @@ def exported_symbols() -> list[str]:
         "mf_compile_check", "mf_buffer_mark_modified", "mf_kernel_read_layout", "mf_events_upload_async",
         "mf_buffer_d2h_async", "mf_kernel_store_async", "mf_eval_expressions_batch", "mf_kernel_generate_segments",
         "mf_expr_set_create", "mf_expr_set_eval", "mf_expr_set_free", "mf_kernel_fallback_count",
-        "mf_histogram", "mf_events_load_file", "mf_splitmix_seed_rows",
+        "mf_histogram", "mf_events_load_file", "mf_splitmix_seed_rows", "mf_buffer_wrap_host",
     ]

@@ -67,6 +67,7 @@ class DeviceColumns:
         self.backend = backend
         self.elem = elem
         self.buf = None
+        self._host = None  # the host array of a wrap_host block
         self.ncols = 0
         self.n = 0
         self.stride = 0
@@ -78,8 +79,10 @@ class DeviceColumns:
     def ensure(self, ncols: int, n: int) -> None:
         stride = int(L.lib.mf_column_stride(n))
         need = max(1, ncols) * stride * self.itemsize
-        if self.buf is None or L.lib.mf_buffer_size(self.buf) < need:
+        # a block over host memory (wrap_host) is never an upload target
+        if self.buf is None or self._host is not None or L.lib.mf_buffer_size(self.buf) < need:
             self.free()
+            self._host = None
             b = L.c_buf()
             L.check(L.lib.mf_buffer_alloc(self.backend.handle, need, C.byref(b)))
             self.buf = b
@@ -97,6 +100,21 @@ class DeviceColumns:
         want = np.float32 if self.elem == L.MF_F32 else np.float64
         ev = np.ascontiguousarray(ev, dtype=want)
         L.check(L.lib.mf_events_upload(self.buf, self.elem, ev.ctypes.data, ncols, n, n, self.stride))
+
+    @classmethod
+    def wrap_host(cls, backend: CUDABackend, events: np.ndarray) -> "DeviceColumns":
+        """A block over a host SoA array (ncols, n) that kernels read in place
+        over the host link (mf_buffer_wrap_host); column stride n. The array
+        is kept alive by the block."""
+        ev = events if events.ndim == 2 else events[None, :]
+        if not ev.flags.c_contiguous or ev.dtype not in (np.float64, np.float32):
+            raise ValueError("wrap_host needs a C-contiguous FP64 or FP32 array")
+        cols = cls(backend, L.MF_F64 if ev.dtype == np.float64 else L.MF_F32)
+        b = L.c_buf()
+        L.check(L.lib.mf_buffer_wrap_host(backend.handle, ev.ctypes.data, ev.nbytes, C.byref(b)))
+        cols.buf, cols.ncols, cols.n, cols.stride = b, ev.shape[0], ev.shape[1], ev.shape[1]
+        cols._host = ev
+        return cols
 
     def download(self) -> np.ndarray:
         out = np.empty((self.ncols, self.n), dtype=np.float32 if self.elem == L.MF_F32 else np.float64)

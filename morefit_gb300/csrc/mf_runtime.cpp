@@ -233,6 +233,10 @@ struct mf_buffer {
   uint64_t size = 0;
   uint64_t gen = 1;  // write generation: bumped by every write through the library
   mutable std::vector<mf_derived> derived;
+  // host memory the device reads in place (mf_buffer_wrap_host): not owned;
+  // `registered` when this library registered it and unregisters on free
+  void* host = nullptr;
+  bool registered = false;
 };
 
 // Owned copy of a kernel description (its strings and arrays), kept by
@@ -591,10 +595,39 @@ int mf_buffer_free(mf_buffer* b) {
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
   free_derived(b);
-  ctx_free(c, b->ptr, std::max<uint64_t>((b->size + 255) & ~uint64_t(255), 256));
-  c->allocated -= (b->size + 255) & ~uint64_t(255);
+  if (b->host) {
+    if (b->registered) cudaHostUnregister(b->host);
+  } else {
+    ctx_free(c, b->ptr, std::max<uint64_t>((b->size + 255) & ~uint64_t(255), 256));
+    c->allocated -= (b->size + 255) & ~uint64_t(255);
+  }
   delete b;
   release_context(c);
+  return MF_OK;
+}
+
+int mf_buffer_wrap_host(mf_context* c, void* host, uint64_t nbytes, mf_buffer** out) {
+  if (!c || !host || !out) return fail(MF_ERR_INVALID, "null argument");
+  *out = nullptr;
+  MF_CUDA_TRY(cudaSetDevice(c->device));
+  auto b = std::make_unique<mf_buffer>();
+  b->ctx = c;
+  b->size = nbytes;
+  b->host = host;
+  void* d = nullptr;
+  if (cudaHostGetDevicePointer(&d, host, 0) != cudaSuccess) {
+    cudaGetLastError();  // not page-locked yet: register it (mapped) for this buffer's lifetime
+    MF_CUDA_TRY(cudaHostRegister(host, nbytes, cudaHostRegisterMapped));
+    b->registered = true;
+    const cudaError_t e = cudaHostGetDevicePointer(&d, host, 0);
+    if (e != cudaSuccess) {
+      cudaHostUnregister(host);
+      return fail(MF_ERR_CUDA, std::string("cudaHostGetDevicePointer: ") + cudaGetErrorString(e));
+    }
+  }
+  b->ptr = d;
+  c->refs++;
+  *out = b.release();
   return MF_OK;
 }
 

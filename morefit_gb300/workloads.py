@@ -120,6 +120,30 @@ class Likelihood:
         for b in self.blocks.values():
             b.SetNevents(self.nevents)
 
+    def set_data_mapped(self, events: np.ndarray) -> None:
+        """set_data without a copy to HBM: the precompute kernel (or, without
+        one, the column preparation) reads `events` (contiguous FP64,
+        page-locked) in place over the host link while it computes. Enqueued
+        without host waits; `events` must stay valid and unchanged until the
+        backend is synchronized."""
+        ev = events if events.ndim == 2 else events[None, :]
+        cached = self.__dict__.get("_mapped")
+        if cached is None or cached._host is not ev:
+            cached = DeviceColumns.wrap_host(self.backend, ev)
+            self._mapped = cached
+        else:
+            L.check(L.lib.mf_buffer_mark_modified(cached.buf))
+        self.pre.input = cached
+        self.nevents = ev.shape[1]
+        if self.has_precompute:
+            self.pre.SetNevents(self.nevents)
+            self.pre.SubmitKernelAsync()
+        else:
+            for b in self.blocks.values():
+                b.SetupInputBuffer(self.pre, True)
+        for b in self.blocks.values():
+            b.SetNevents(self.nevents)
+
     def sums_async(self, kernel: str, theta, out, out_index: int = 0) -> None:
         """Enqueues one evaluation whose sums land in row `out_index` of device buffer `out`."""
         b = self.blocks[kernel]

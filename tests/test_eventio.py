@@ -72,3 +72,33 @@ def test_streamed_upload_matches_in_memory_upload(tmp_path, oracle_lib):
             upload_event_file(b, tmp_path / "short.npy", dims)
     finally:
         b.close()
+
+
+@pytest.mark.gpu
+def test_mapped_host_events_give_the_same_sums(oracle_lib):
+    """Events read in place from host memory (mf_buffer_wrap_host: the
+    precompute kernel, or for the mass model the column preparation, reads
+    them over the host link) give the same sums, bit for bit, as events
+    copied to HBM; plain (pageable) arrays are registered for the purpose."""
+    from morefit_gb300.backend import CUDABackend
+    from morefit_gb300.workloads import Likelihood, load_spec
+    b = CUDABackend(0)
+    try:
+        for wl, n in (("pwave", 200000), ("mass", 100000)):
+            ev = np.ascontiguousarray(oracle_lib.generate(wl, n))
+            spec = load_spec(wl)
+            a = Likelihood(b, spec, np.float64)
+            a.set_data(ev)
+            m = Likelihood(b, spec, np.float64)
+            m.set_data_mapped(ev)
+            b.synchronize()
+            for kern in ("lh_kernel", "lh_grad_kernel"):
+                assert np.array_equal(a.sums(kern, spec["truth"]), m.sums(kern, spec["truth"])), (wl, kern)
+            # a second step over the same (re-written) host array
+            ev[...] = oracle_lib.generate(wl, n, seed=4)
+            m.set_data_mapped(ev)
+            a.set_data(ev)
+            b.synchronize()
+            assert np.array_equal(a.sums("lh_grad_kernel", spec["truth"]), m.sums("lh_grad_kernel", spec["truth"]))
+    finally:
+        b.close()
