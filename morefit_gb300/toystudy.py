@@ -222,14 +222,46 @@ class ToyStudy:
     ``clip``; otherwise every toy has ``nevents`` events (the reference draws
     Poisson counts only for extended PDFs)."""
 
+    # threads per block (= per segment) tried for the segment kernels
+    BLOCK_CANDIDATES = (64, 128, 256)
+    TUNE_MIN_TOYS = 512
+
     def __init__(self, backend: CUDABackend, spec: dict, kernelT=np.float64, limits=None,
-                 seed: int = DEFAULT_SEED, generator_threads: int = 65536):
+                 seed: int = DEFAULT_SEED, generator_threads: int = 65536, block: int = 0):
+        """``block``: threads per segment of the segment kernels; 0 = tuned on
+        the first study of at least TUNE_MIN_TOYS toys (the candidate whose
+        F + gradient launch over that study's toys is fastest on the device),
+        256 until then."""
         self.backend = backend
         self.spec = spec
         self.kernelT = kernelT
         self.limits = limits if limits is not None else PWAVE_LIMITS
         self.seed = seed
         self.generator_threads = generator_threads
+        self.block = block
+        self.tuning = None
+        self._likes = {}
+
+    def _likelihood(self, block: int) -> Likelihood:
+        if block not in self._likes:  # kernels built once per block size
+            self._likes[block] = Likelihood(self.backend, self.spec, self.kernelT, block=block)
+        return self._likes[block]
+
+    def _tune(self, cols, begins, counts, truth) -> None:
+        import time
+        idx = np.arange(len(counts))
+        times = {}
+        for blk in self.BLOCK_CANDIDATES:
+            like = self._likelihood(blk)
+            like.set_device_data(cols)
+            sl = SegmentLikelihood(like, begins, counts)
+            sl.value_and_gradient(idx, truth)  # makes the prepared copy
+            t0 = time.perf_counter()
+            for _ in range(3):
+                sl.value_and_gradient(idx, truth)
+            times[blk] = (time.perf_counter() - t0) / 3
+        self.block = min(times, key=times.get)
+        self.tuning = {"block": self.block, "launch_s": times, "toys": len(counts)}
 
     def serial_fits_per_s(self, result: "ToyResult", ntoys: int = 32) -> float:
         """The per-fit serial baseline: the first ``ntoys`` toys of ``result``'s
@@ -267,7 +299,9 @@ class ToyStudy:
             truth = np.tile(base, (nruns, 1))
             cols = generate_events(self.backend, self.spec, total, seed=self.seed,
                                    max_workitems=self.generator_threads, kernelT=np.float64)
-        like = Likelihood(self.backend, self.spec, self.kernelT)
+        if self.block == 0 and nruns >= self.TUNE_MIN_TOYS:
+            self._tune(cols, begins, counts, truth)
+        like = self._likelihood(self.block or 256)
         like.set_device_data(cols)
         self.backend.synchronize()
         t1 = time.perf_counter()
