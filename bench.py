@@ -144,6 +144,22 @@ def dist_env():
     return rank, world, local
 
 
+def replica_value(ms: float, steps: int):
+    """Whole-job rate of N independent replicas: the slowest rank's time
+    (all-reduce MAX over the process group, when there is one) and
+    world x steps evaluations per second of it. Returns (ms, value)."""
+    import torch
+    import torch.distributed as dist
+    world = 1
+    if dist.is_available() and dist.is_initialized():
+        world = dist.get_world_size()
+        dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+        t = torch.tensor([ms], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, world * steps / (ms / 1e3)
+
+
 def reference_arm(args):
     """The reference's CPU path: its kernel text through the CPU backend's loop, all host threads."""
     rank, world, _ = dist_env()
@@ -273,11 +289,7 @@ def ours(args):
     sets64, bytes64, nsets64 = make_sets(np.float64)
     with ClockSampler(local) as clk:
         ms64, res64 = timed_device(sets64, args.steps, args.warmup, clk)
-    if world > 1:
-        t = torch.tensor([ms64], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms64 = float(t.item())
-    value = world * args.steps / (ms64 / 1e3)
+    ms64, value = replica_value(ms64, args.steps)
     avg_launch_s = ms64 / 1e3 / args.steps
     hbm_peak, peak_kind = _peaks()
     achieved = bytes64 / avg_launch_s / 1e9

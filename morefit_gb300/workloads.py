@@ -193,6 +193,30 @@ class Likelihood:
         b.SubmitKernel()
         return b.CopyFromKahanBuffer()
 
+    def sums_many(self, kernel: str, thetas) -> np.ndarray:
+        """The sums at several parameter points (rows of ``thetas``) in one
+        batched call (mf_kernel_reduce_many: consecutive evaluations overlap,
+        one combine per chunk); each row equals ``sums(kernel, theta)`` bit
+        for bit. Returns (npoints, noutputs)."""
+        b = self.blocks[kernel]
+        k = b.kernel
+        rows = np.ascontiguousarray(self.param_rows(kernel, thetas))
+        count = rows.shape[0]
+        out = L.c_buf()
+        L.check(L.lib.mf_buffer_alloc(self.backend.handle, count * k.nout * 8, C.byref(out)))
+        try:
+            ins = (L.c_buf * count)(*([b.input.buf] * count))
+            strides = np.full(count, b.input.stride, dtype=np.uint64)
+            ns = np.full(count, self.nevents, dtype=np.uint64)
+            u64p = C.POINTER(C.c_uint64)
+            L.check(L.lib.mf_kernel_reduce_many(k.handle, count, ins, strides.ctypes.data_as(u64p),
+                                                ns.ctypes.data_as(u64p), L.dptr(rows), rows.shape[1], out))
+            res = np.empty((count, k.nout))
+            L.check(L.lib.mf_buffer_d2h(out, 0, res.ctypes.data, res.nbytes))
+        finally:
+            L.lib.mf_buffer_free(out)
+        return res
+
     def likelihood(self, theta) -> float:
         return -2.0 * float(self.sums("lh_kernel", theta)[0])
 
