@@ -56,7 +56,7 @@ def _peaks():
 # storage, double-float arithmetic, 9 prepared columns, 1M events) from the
 # full ncu capture summarised in profiles/mf_reduce_part_lh_grad_pwave_1M.md
 # (mf_reduce_part: the entry batched evaluations launch).
-NCU_TRAFFIC_F64 = 72.026368e6 + 0.440832e6
+NCU_TRAFFIC_F64 = 72.349440e6 + 0.755968e6
 NCU_TRAFFIC_SOURCE = "ncu --set full, one mf_reduce_part launch, profiles/mf_reduce_part_lh_grad_pwave_1M.md"
 # evaluations per combine launch of mf_kernel_reduce_many (mf_runtime.cpp, launch_batched)
 COMBINE_CHUNK = 256
