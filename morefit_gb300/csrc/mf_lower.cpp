@@ -1550,7 +1550,7 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
     // ---- single-dataset reduce ----
     s << "extern \"C\" __global__ void __launch_bounds__(MF_BLOCK) " << out.entry << "(const " << DT
       << "* __restrict__ data, mf_u64 stride, mf_u64 n, mf_args P, float2* __restrict__ partials,"
-      << " unsigned* __restrict__ counter, double* __restrict__ out, unsigned* __restrict__ status) {\n";
+      << " unsigned* __restrict__ counter, double* __restrict__ out, unsigned* __restrict__ status, unsigned seq) {\n";
     const auto body_mark = s.tellp();
     s << "  mf_launch_dependents();  // the next evaluation may start its event loop on SMs this grid frees\n";
     load_table(s);
@@ -1701,7 +1701,17 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
   __syncthreads();
   if (!am_last) return;
   const unsigned mf_nb = gridDim.x;
-)CUDA" << combine_text << "  if (threadIdx.x == 0) *counter = 0u;\n}\n";
+)CUDA" << combine_text << R"CUDA(  if (threadIdx.x == 0) *counter = 0u;
+  // Synchronous evaluation (seq != 0): out[] is mapped host memory; publish
+  // completion in the mapped word status[1] after every output is visible
+  // system-wide, so the host can read the sums without a stream synchronize.
+  if (seq != 0u) {
+    __threadfence_system();
+    __syncthreads();
+    if (threadIdx.x == 0) *reinterpret_cast<volatile unsigned*>(status + 1) = seq;
+  }
+}
+)CUDA";
     // ---- batched evaluations: per-block partials only, then one combine ----
     // Evaluation e of a batch writes its partial rows to its own slot of the
     // batch's partial buffer without counting or combining, so consecutive
@@ -1934,8 +1944,10 @@ void LoweredKernel::fill_args(const double* params, size_t np, unsigned char* ou
   std::memset(out, 0, args_bytes());
   double* d = reinterpret_cast<double*>(out);
   float* f = reinterpret_cast<float*>(out + size_t(nd) * 8);
-  std::vector<double> memo(nodes.size(), 0.0);
-  std::vector<char> done(nodes.size(), 0);
+  thread_local std::vector<double> memo;
+  thread_local std::vector<char> done;
+  memo.assign(nodes.size(), 0.0);
+  done.assign(nodes.size(), 0);
   for (const auto& sl : slots) {
     const double v = eval_memo(nodes, sl.node, params, np, memo, done);
     switch (sl.kind) {

@@ -13,6 +13,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cctype>
 #include <cmath>
 #include <cstdio>
@@ -192,7 +193,8 @@ struct mf_context {
   size_t partials_cap = 0;  // doubles
   unsigned* counter = nullptr;
   unsigned* status = nullptr;       // device-visible alias of status_host
-  unsigned* status_host = nullptr;  // mapped pinned host word: kernel error flags
+  unsigned* status_host = nullptr;  // mapped pinned host words: [0] kernel error flags, [1] sync completion
+  unsigned sync_seq = 0;            // sequence number of the last synchronous evaluation
   // mapped pinned host memory the kernels write results into
   double* out_host = nullptr;
   double* out_dev = nullptr;
@@ -296,7 +298,7 @@ struct mf_kernel {
 namespace mfi {
 int launch_reduce(mf_kernel* k, const void* data, uint64_t stride, uint64_t n, const double* params,
                   double* partials, unsigned* counter, double* out, cudaStream_t stream, int grid_cap,
-                  bool dependent = false);
+                  bool dependent = false, unsigned seq = 0);
 }
 
 // ---------------------------------------------------------------- helpers --
@@ -367,6 +369,24 @@ int check_status(mf_context* c) {
   cudaMemsetAsync(c->counter, 0, sizeof(unsigned), c->stream);  // a block that gave up may have left it set
   cudaStreamSynchronize(c->stream);
   return fail(MF_ERR_TIMEOUT, "a kernel gave up waiting for its input tiles (status " + std::to_string(st) + ")");
+}
+
+// Waits for the synchronous evaluation `seq`: its combining block stores
+// seq in the mapped word status[1] once the sums are visible to the host.
+// The host spins on that word (a stream synchronize costs about 1.6 us more
+// per call); past kSyncSpinUs, or if the launch failed, it falls back to a
+// stream synchronize, which also reports any asynchronous error.
+int wait_sync_word(mf_context* c, unsigned seq) {
+  constexpr auto kSyncSpinUs = std::chrono::microseconds(500);
+  const auto t0 = std::chrono::steady_clock::now();
+  unsigned spins = 0;
+  while (__atomic_load_n(c->status_host + 1, __ATOMIC_ACQUIRE) != seq) {
+    if ((++spins & 255u) == 0 && std::chrono::steady_clock::now() - t0 > kSyncSpinUs) {
+      MF_CUDA_TRY(cudaStreamSynchronize(c->stream));
+      break;
+    }
+  }
+  return MF_OK;
 }
 
 int ensure_scratch(mf_context* c, size_t partial_doubles, size_t out_doubles) {
@@ -1148,18 +1168,19 @@ int grid_for(const mf_kernel* k, uint64_t n) {
 // waits for it before it touches the shared scratch.
 int launch_reduce(mf_kernel* k, const void* data, uint64_t stride, uint64_t n, const double* params,
                   double* partials, unsigned* counter, double* out, cudaStream_t stream, int grid_cap,
-                  bool dependent) {
+                  bool dependent, unsigned seq) {
   int grid = grid_for(k, n);
   if (grid_cap > 0) grid = std::min(grid, grid_cap);
   // argument struct: parameter-only values evaluated here, pre-rounded for the kernel's arithmetic
-  std::vector<unsigned char> pv(k->lowered.args_bytes(), 0);
+  thread_local std::vector<unsigned char> pv;
+  pv.assign(k->lowered.args_bytes(), 0);
   try {
     k->lowered.fill_args(params, k->n_params, pv.data());
   } catch (const std::exception& e) {
     return fail(MF_ERR_INVALID, std::string("parameter evaluation: ") + e.what());
   }
   unsigned* status = k->ctx->status;
-  void* args[] = {const_cast<void**>(&data), &stride, &n, pv.data(), &partials, &counter, &out, &status};
+  void* args[] = {const_cast<void**>(&data), &stride, &n, pv.data(), &partials, &counter, &out, &status, &seq};
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(grid);
   cfg.blockDim = dim3(k->lowered.block);
@@ -1292,9 +1313,12 @@ int mf_kernel_reduce(mf_kernel* k, const mf_buffer* in, uint64_t stride, uint64_
   const void* data = nullptr;
   rc = prepare_input(k, in, stride, &data);
   if (rc) return rc;
-  rc = mfi::launch_reduce(k, data, stride, n, params, c->partials, c->counter, c->out_dev, c->stream, 0);
+  if (++c->sync_seq == 0u) c->sync_seq = 1u;  // 0 means "asynchronous" to the kernel
+  rc = mfi::launch_reduce(k, data, stride, n, params, c->partials, c->counter, c->out_dev, c->stream, 0, false,
+                          c->sync_seq);
   if (rc) return rc;
-  MF_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  rc = wait_sync_word(c, c->sync_seq);
+  if (rc) return rc;
   std::memcpy(sums, c->out_host, k->n_outputs * sizeof(double));
   rc = check_status(c);
   if (rc || !k->desc || all_finite(sums, k->n_outputs)) return rc;

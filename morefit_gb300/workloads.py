@@ -187,8 +187,14 @@ class Likelihood:
         return np.concatenate([th, self._exprs(kernel).eval(th)], axis=1)
 
     def sums(self, kernel: str, theta=None, param_vector=None) -> np.ndarray:
+        if param_vector is None:
+            calls = self.__dict__.setdefault("_sync_calls", {})
+            call = calls.get(kernel)
+            if call is None:
+                call = calls[kernel] = _SyncEvaluation(self, kernel)
+            return call(theta)
         b = self.blocks[kernel]
-        pv = self.param_vector(kernel, theta) if param_vector is None else np.asarray(param_vector, np.float64)
+        pv = np.asarray(param_vector, np.float64)
         b.CopyToParameterBuffer(pv)
         b.SubmitKernel()
         return b.CopyFromKahanBuffer()
@@ -263,6 +269,41 @@ class Likelihood:
         if self.weight is not None:
             r.errors[0] = np.sqrt(np.abs(np.diag(self.corrected_covariance(r.values[0]))))
         return r
+
+
+class _SyncEvaluation:
+    """One synchronous evaluation of a REDUCE kernel at the floating
+    parameter values, the fitter's per-call path (fitter.hh:1054-1151) with
+    the host work cut to two C calls: the parameter vector [floating
+    values..., parameter buffers...] lives in one preallocated array whose
+    hoisted buffers mf_expr_set_eval writes in place, and the sums land in a
+    second one; both pointers are made once."""
+
+    __slots__ = ("like", "block", "handle", "ntheta", "nparams", "pv", "out", "exprs", "pv_p", "bufs_p", "out_p")
+
+    def __init__(self, like: Likelihood, kernel: str):
+        b = like.blocks[kernel]
+        k = b.kernel
+        self.like, self.block, self.handle = like, b, k.handle
+        self.ntheta = len(like.params)
+        self.nparams = self.ntheta + len(like.buffers[kernel])
+        if self.nparams != k.nparams:
+            raise ValueError(f"{kernel}: {k.nparams} kernel parameters, {self.nparams} in the parameter vector")
+        self.pv = np.zeros(max(1, self.nparams))
+        self.out = np.zeros(k.nout)
+        self.exprs = like._exprs(kernel) if self.nparams > self.ntheta else None
+        self.pv_p = L.dptr(self.pv)
+        self.bufs_p = C.cast(self.pv.ctypes.data + 8 * self.ntheta, L.c_dbl_p)
+        self.out_p = L.dptr(self.out)
+
+    def __call__(self, theta) -> np.ndarray:
+        self.pv[:self.ntheta] = theta
+        if self.exprs is not None:
+            L.check(L.lib.mf_expr_set_eval(self.exprs.handle, 1, self.pv_p, self.bufs_p))
+        b = self.block
+        L.check(L.lib.mf_kernel_reduce(self.handle, b.input.buf, b.input.stride, b.nevents, self.pv_p, self.nparams,
+                                       self.out_p))
+        return self.out.copy()
 
 
 class _WholeDataset:

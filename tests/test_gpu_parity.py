@@ -172,6 +172,26 @@ def test_deterministic(backend):
     assert np.array_equal(a, b)
 
 
+@pytest.mark.parametrize("workload", ["pwave", "mass", "mass_w"])
+def test_sync_evaluation_equals_parameter_vector_path(backend, workload):
+    """sums(kernel, theta), whose hoisted parameter buffers are evaluated in
+    place in a preallocated vector, equals the evaluation from the explicit
+    parameter vector bit for bit; that vector matches the fitter's own
+    (fitter.hh:1059-1072) to rounding."""
+    from morefit_gb300.workloads import Likelihood
+    g = load_golden(f"{workload}_n1000.json")
+    like = Likelihood(backend, g, np.float64)
+    like.set_data(golden_events(workload, 1000))
+    names = [k for k in KERNELS + ("lh_fisher_kernel",) if k in like.blocks]
+    for pt in g["points"]:
+        for name in names:
+            pv = like.param_vector(name, pt["params"])
+            np.testing.assert_allclose(pv, pt["kernel_params"][name], rtol=1e-13, atol=0)
+            a = like.sums(name, pt["params"])
+            assert np.array_equal(a, like.sums(name, param_vector=pv)), (workload, name)
+            assert np.array_equal(a, like.sums(name, pt["params"]))
+
+
 @pytest.mark.parametrize("workload,n", [("pwave", 1000), ("mass", 1000), ("pwave", 1000000), ("mass", 100000),
                                         ("spwave", 20000), ("cbpoly", 100000)])
 def test_mixed_precision_parameter_shift(backend, oracle_lib, workload, n):
