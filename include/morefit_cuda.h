@@ -253,7 +253,9 @@ int mf_kernel_read_layout(const mf_kernel* k, uint32_t* columns, uint32_t* bytes
  * to FP64 at the warp level. Results are deterministic for a given n.
  * params: n_params FP64 values (converted to the element type on the device
  * side for FP32 kernels). input: column stride `stride` events; base and
- * stride must satisfy the MF_COLUMN_ALIGN layout.
+ * stride must satisfy the MF_COLUMN_ALIGN layout. Synchronous: the last
+ * block writes the sums to mapped host memory and then a completion word the
+ * call spins on (a stream synchronize after 500 us, or on a launch error).
  * Replaces SubmitKernel + Finish + CopyFromKahanBuffer
  * (include/compute.hh:134-148, include/fitter.hh:1076-1096). */
 int mf_kernel_reduce(mf_kernel* k, const mf_buffer* input, uint64_t stride, uint64_t n, const double* params,
