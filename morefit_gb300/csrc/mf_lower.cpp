@@ -441,9 +441,6 @@ std::vector<char> reachable(const std::vector<Node>& ns, const std::vector<int>&
 struct Emitter {
   const std::vector<Node>& ns;
   bool f32;  // arithmetic type float
-  // FP64 bodies: exp, log, sqrt, sin, cos and pow through the double-float
-  // functions (mf_fast_*, FP32 pipe) instead of FP64 calls
-  bool fast = false;
   std::string T() const { return f32 ? "float" : "double"; }
   std::string ref(int id, const std::string& pfx) const {
     const Node& n = ns[id];
@@ -464,18 +461,14 @@ struct Emitter {
       case Op::Div: return lhs + A(n.a) + " / " + A(n.b) + ";";
       case Op::Neg: return lhs + "-" + A(n.a) + ";";
       case Op::Rcp: return lhs + fn_name(Op::Rcp, f32) + "(" + A(n.a) + ");";
-      case Op::Pow:
-        if (fast && !f32) return lhs + "mf_fast_pow(" + A(n.a) + ", " + A(n.b) + ");";
-        return lhs + fn_name(Op::Pow, f32) + "(" + A(n.a) + ", " + A(n.b) + ");";
+      case Op::Pow: return lhs + fn_name(Op::Pow, f32) + "(" + A(n.a) + ", " + A(n.b) + ");";
       case Op::Cmp: return lhs + "(" + A(n.a) + " " + cmp_str(n.cmp) + " " + A(n.b) + ");";
       case Op::Select: return lhs + "(" + A(n.a) + " ? " + A(n.b) + " : " + A(n.c) + ");";
       case Op::Exp:
       case Op::Log:
       case Op::Sqrt:
       case Op::Sin:
-      case Op::Cos:
-        if (fast && !f32) return lhs + "mf_fast_" + fn_name(n.op, false) + "(" + A(n.a) + ");";
-        return lhs + fn_name(n.op, f32) + "(" + A(n.a) + ");";
+      case Op::Cos: return lhs + fn_name(n.op, f32) + "(" + A(n.a) + ");";
       default:
         if (is_unary_fn(n.op)) return lhs + fn_name(n.op, f32) + "(" + A(n.a) + ");";
         throw std::runtime_error("emit: unexpected node");
@@ -1818,19 +1811,7 @@ __device__ __forceinline__ unsigned mf_xoshiro(unsigned* s) {
   return r;
 }
 )CUDA";
-    if (!ar32) {
-      s << dw_log_table() << kDwPrelude;
-      s << R"CUDA(__device__ __forceinline__ double mf_fast_join(mf_dw a) { return mf_dw_to_double_bits(a); }
-__device__ __forceinline__ double mf_fast_exp(double x) { return mf_fast_join(mf_dw_exp(mf_dw_split_rn(x), mf_dw_exptab_g)); }
-__device__ __forceinline__ double mf_fast_log(double x) { return mf_fast_join(mf_dw_log(mf_dw_split_rn(x), mf_dw_logtab_g)); }
-__device__ __forceinline__ double mf_fast_sqrt(double x) { return mf_fast_join(mf_dw_sqrt(mf_dw_split_rn(x))); }
-__device__ __forceinline__ double mf_fast_sin(double x) { return mf_fast_join(mf_dw_sin(mf_dw_split_rn(x))); }
-__device__ __forceinline__ double mf_fast_cos(double x) { return mf_fast_join(mf_dw_cos(mf_dw_split_rn(x))); }
-__device__ __forceinline__ double mf_fast_pow(double a, double b) {
-  return mf_fast_join(mf_dw_pow(mf_dw_split_rn(a), mf_dw_split_rn(b), mf_dw_logtab_g, mf_dw_exptab_g));
-}
-)CUDA";
-    }
+    if (!ar32) s << dw_log_table() << kDwPrelude;
     s << "extern \"C\" __global__ void __launch_bounds__(MF_BLOCK) " << out.entry
       << "(const unsigned* __restrict__ seeds, unsigned nseeds, mf_u64 n, mf_u64 nper, mf_par P, " << ST
       << "* __restrict__ outp, mf_u64 out_stride, unsigned* __restrict__ status, unsigned long long max_tries) {\n";
@@ -1849,15 +1830,104 @@ __device__ __forceinline__ double mf_fast_pow(double a, double b) {
     };
     const char* mul = ar32 ? "__fmul_rn" : "__dmul_rn";
     const char* add = ar32 ? "__fadd_rn" : "__dadd_rn";
-    // FP64 generation: the density's exp/log/sqrt/sin/cos/pow through the
-    // double-float functions (FP32 pipe; relative error ~1e-14), and the
-    // accept decision maxprob*u < p recomputed with the density in exact
-    // FP64 (the code the reference runs) whenever |maxprob*u - p| is within
-    // 1e-9 * maxprob or p is NaN. Elsewhere the fast density is far inside
-    // that margin of the exact one, so every decision -- and every generated
-    // event -- equals the FP64 one.
+    // FP64 generation: the density is evaluated in double-float (FP32
+    // pairs on the FP32 pipe, which GB300 issues at 64x its FP64 rate:
+    // proposals split with integer operations, parameter-only values
+    // converted once per thread, tables from global memory), and the accept
+    // decision maxprob*u < p is recomputed with the density in exact FP64
+    // (the code the reference runs) whenever |maxprob*u - p| is within
+    // 1e-9 * maxprob or p is not finite. The double-float density is within
+    // about 1e-13 of the exact one when its intermediates stay inside the
+    // FP32 exponent range (2^-100 to 3.4e38 in magnitude, or zero), far
+    // inside that margin, so every decision -- and every generated event --
+    // equals the FP64 one. Only the proposals, the bound and the comparison
+    // stay on the FP64 pipe.
     const bool fast_density = !ar32;
+    auto wref = [&](int id) -> std::string {
+      const Node& n = ns[id];
+      if (n.op == Op::Const) {
+        const float h = float(n.value);
+        const float l = float(n.value - double(h));
+        char b[96];
+        std::snprintf(b, sizeof b, "mf_dw_make(%af, %af)", double(h), double(l));
+        return b;
+      }
+      if (n.op == Op::Input) return "xw" + std::to_string(n.index);
+      if (n.op == Op::Param) return "pw" + std::to_string(n.index);
+      if (n.uniform) return "uw" + std::to_string(id);
+      return "w" + std::to_string(id);
+    };
+    // sin and cos of one operand share a reduction: operand -> (sin node, cos node)
+    std::map<int, std::pair<int, int>> wsincos;
+    {
+      std::map<int, int> sin_of, cos_of;
+      for (size_t i = 0; i < ns.size(); i++) {
+        if (!live[i] || ns[i].uniform) continue;
+        if (ns[i].op == Op::Sin) sin_of[ns[i].a] = int(i);
+        if (ns[i].op == Op::Cos) cos_of[ns[i].a] = int(i);
+      }
+      for (auto& [a, si] : sin_of) {
+        auto c = cos_of.find(a);
+        if (c != cos_of.end()) wsincos[a] = {si, c->second};
+      }
+    }
+    auto wstmt = [&](int id) -> std::string {
+      const Node& n = ns[id];
+      const std::string lhs = "const " + std::string(n.op == Op::Cmp ? "bool" : "mf_dw") + " w" + std::to_string(id) + " = ";
+      const std::string A = n.a >= 0 ? wref(n.a) : "", B = n.b >= 0 ? wref(n.b) : "", Cc = n.c >= 0 ? wref(n.c) : "";
+      auto D = [](const std::string& v) { return "mf_dw_to_double(" + v + ")"; };
+      switch (n.op) {
+        case Op::Add: return lhs + "mf_dw_add(" + A + ", " + B + ");";
+        case Op::Sub: return lhs + "mf_dw_sub(" + A + ", " + B + ");";
+        case Op::Mul: return lhs + "mf_dw_mul(" + A + ", " + B + ");";
+        case Op::Div: return lhs + "mf_dw_mul(" + A + ", mf_dw_rcp(" + B + "));";
+        case Op::Neg: return lhs + "mf_dw_neg(" + A + ");";
+        case Op::Rcp: return lhs + "mf_dw_rcp(" + A + ");";
+        case Op::Log: return lhs + "mf_dw_log(" + A + ", mf_dw_logtab_g);";
+        case Op::Exp: return lhs + "mf_dw_exp(" + A + ", mf_dw_exptab_g);";
+        case Op::Pow: return lhs + "mf_dw_pow(" + A + ", " + B + ", mf_dw_logtab_g, mf_dw_exptab_g);";
+        case Op::Sqrt: return lhs + "mf_dw_sqrt(" + A + ");";
+        case Op::Sin:
+        case Op::Cos: {
+          auto it = wsincos.find(n.a);
+          if (it == wsincos.end()) return lhs + (n.op == Op::Sin ? "mf_dw_sin(" : "mf_dw_cos(") + A + ");";
+          if (id != std::min(it->second.first, it->second.second)) return "";  // defined with the first of the two
+          const std::string sn = "w" + std::to_string(it->second.first), cn = "w" + std::to_string(it->second.second);
+          return "mf_dw " + sn + ", " + cn + "; mf_dw_sincos(" + A + ", &" + sn + ", &" + cn + ");";
+        }
+        case Op::Cmp:
+          switch (n.cmp) {
+            case CmpOp::Gt: return lhs + "mf_dw_gt(" + A + ", " + B + ");";
+            case CmpOp::Lt: return lhs + "mf_dw_lt(" + A + ", " + B + ");";
+            case CmpOp::Ge: return lhs + "mf_dw_ge(" + A + ", " + B + ");";
+            case CmpOp::Le: return lhs + "mf_dw_le(" + A + ", " + B + ");";
+            case CmpOp::Eq: return lhs + "mf_dw_eq(" + A + ", " + B + ");";
+            case CmpOp::Ne: return lhs + "!mf_dw_eq(" + A + ", " + B + ");";
+          }
+          break;
+        case Op::Select: return lhs + "(" + A + " ? " + B + " : " + Cc + ");";
+        default:
+          if (is_unary_fn(n.op)) return lhs + "mf_dw_from_double(" + fn_name(n.op, false) + "(" + D(A) + "));";
+      }
+      throw std::runtime_error("emit: unexpected node");
+    };
+    // parameter-only values the double-float density reads, converted once per thread
+    auto emit_uniform_pairs = [&]() {
+      std::set<int> uni;
+      auto note = [&](int k) {
+        if (k >= 0 && ns[k].uniform && ns[k].op != Op::Const) uni.insert(k);
+      };
+      for (size_t i = 0; i < ns.size(); i++) {
+        if (!live[i] || ns[i].uniform || ns[i].op == Op::Input) continue;
+        note(ns[i].a);
+        note(ns[i].b);
+        note(ns[i].c);
+      }
+      for (int r : roots) note(r);
+      for (int k : uni) s << "  const mf_dw " << wref(k) << " = mf_dw_from_double(" << em.ref(k, "u") << ");\n";
+    };
     auto accept_reject = [&]() {
+      if (fast_density) emit_uniform_pairs();
       s << "  unsigned long long tries = 0;\n";
       s << "  for (mf_u64 i = from; i < to; i++) {\n    for (;;) {\n";
       s << "      if (++tries > max_tries) { atomicOr(status, 1u); return; }\n";
@@ -1867,12 +1937,15 @@ __device__ __forceinline__ double mf_fast_pow(double a, double b) {
           << ")(mf_xoshiro(st) * 2.3283064365386963e-10)));\n";
       }
       if (fast_density) {
-        em.fast = true;
-        emit_body(s, "      ");
-        em.fast = false;
+        for (int d = 0; d < D; d++) s << "      const mf_dw xw" << d << " = mf_dw_split_rn(x" << d << ");\n";
+        for (size_t i = 0; i < ns.size(); i++) {
+          if (!live[i] || ns[i].uniform || ns[i].op == Op::Input) continue;
+          const std::string st = wstmt(int(i));
+          if (!st.empty()) s << "      " << st << "\n";
+        }
         s << "      const double mf_ug = " << mul << "(maxprob, (double)(mf_xoshiro(st) * 2.3283064365386963e-10));\n";
-        s << "      double mf_p = r0;\n";
-        s << "      if (!(fabs(mf_ug - mf_p) > 1e-9 * maxprob)) {  // near the boundary: exact FP64 density\n";
+        s << "      double mf_p = mf_dw_to_double_bits(" << wref(roots[0]) << ");\n";
+        s << "      if (!(fabs(mf_ug - mf_p) > 1e-9 * maxprob) || isinf(mf_p)) {  // exact FP64 density\n";
         emit_body(s, "        ");
         s << "        mf_p = r0;\n      }\n";
         s << "      if (mf_ug < mf_p) {\n";
