@@ -410,6 +410,14 @@ int mf_seed_rows(uint64_t seed, uint32_t nrows, uint32_t* out);
  * halves of four SplitMix64 outputs from (seed mod 2^32) * 2^32 + r.
  * out is SoA [4][nrows]. */
 int mf_splitmix_seed_rows(uint64_t seed, uint32_t nrows, uint32_t* out);
+/* Host linear algebra of batched fits (many small Newton systems; the
+ * reference solves one fit at a time inside Minuit2): for each of n
+ * symmetric p x p matrices H_t (row-major, back to back), Cholesky-factors
+ * H_t and, where it is positive definite (ok[t] = 1), writes x_t = H_t^-1 g_t
+ * (when g and x are given) and diag(H_t^-1) to dinv (when given). ok[t] = 0
+ * leaves x_t and dinv_t unwritten. p <= 64. */
+int mf_spd_solve_batch(uint32_t n, uint32_t p, const double* h, const double* g, double* x, double* dinv,
+                       unsigned char* ok);
 
 /* Work partition of the reference's accelerator generator for n events with
  * at most max_workitems generator threads (compute_opencl.hh:437-445,

@@ -148,6 +148,8 @@ _proto("mf_kernel_generate", C.c_int, c_ker, C.POINTER(C.c_uint32), C.c_uint32, 
 _proto("mf_eval_expressions", C.c_int, C.c_uint32, c_char_pp, c_dbl_p, C.c_uint32, c_char_pp, c_dbl_p)
 _proto("mf_seed_rows", C.c_int, C.c_uint64, C.c_uint32, C.POINTER(C.c_uint32))
 _proto("mf_splitmix_seed_rows", C.c_int, C.c_uint64, C.c_uint32, C.POINTER(C.c_uint32))
+_proto("mf_spd_solve_batch", C.c_int, C.c_uint32, C.c_uint32, c_dbl_p, c_dbl_p, c_dbl_p, c_dbl_p,
+       C.POINTER(C.c_uint8))
 _proto("mf_generate_partition", C.c_int, C.c_uint64, C.c_uint32, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32))
 _proto("mf_lower_source", C.c_int, C.POINTER(KernelDesc), C.c_char_p, C.c_size_t, C.POINTER(C.c_size_t))
 _proto("mf_compile_check", C.c_int, C.POINTER(KernelDesc), C.POINTER(C.c_int), C.POINTER(C.c_int))
@@ -183,4 +185,5 @@ def exported_symbols() -> list[str]:
         "mf_buffer_d2h_async", "mf_kernel_store_async", "mf_eval_expressions_batch", "mf_kernel_generate_segments",
         "mf_expr_set_create", "mf_expr_set_eval", "mf_expr_set_free", "mf_kernel_fallback_count",
         "mf_histogram", "mf_events_load_file", "mf_splitmix_seed_rows", "mf_buffer_wrap_host",
+        "mf_spd_solve_batch",
     ]

@@ -1437,6 +1437,21 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
       out.host_args = true;
       out.nodes = ns;
       out.slots = slots;
+      {
+        // nodes reachable from the slots, in id order: a node's operands
+        // always have smaller ids (hash-consed construction)
+        std::vector<char> need(ns.size(), 0);
+        for (const auto& sl : slots) need[sl.node] = 1;
+        for (size_t i = ns.size(); i-- > 0;) {
+          if (!need[i]) continue;
+          for (int c : {ns[i].a, ns[i].b, ns[i].c}) {
+            if (c >= int(i)) throw std::runtime_error("lowering: operand after its node");
+            if (c >= 0) need[c] = 1;
+          }
+        }
+        for (size_t i = 0; i < ns.size(); i++)
+          if (need[i]) out.eval_order.push_back(int(i));
+      }
       out.nd = std::max(1, nd);
       out.nf = std::max(1, nf);
     }
@@ -1984,45 +1999,32 @@ __device__ __forceinline__ unsigned mf_xoshiro(unsigned* s) {
   return out;
 }
 
-namespace {
-double eval_memo(const std::vector<Node>& ns, int id, const double* params, size_t np, std::vector<double>& memo,
-                 std::vector<char>& done) {
-  if (done[id]) return memo[id];
-  const Node& n = ns[id];
-  double v = 0.0;
-  switch (n.op) {
-    case Op::Const: v = n.value; break;
-    case Op::Param: v = size_t(n.index) < np ? params[n.index] : 0.0; break;
-    case Op::Input: throw std::runtime_error("input column in a parameter-only value");
-    case Op::Add: case Op::Sub: case Op::Mul: case Op::Div: case Op::Pow:
-      v = apply_binary(n.op, eval_memo(ns, n.a, params, np, memo, done), eval_memo(ns, n.b, params, np, memo, done));
-      break;
-    case Op::Cmp:
-      v = apply_cmp(n.cmp, eval_memo(ns, n.a, params, np, memo, done), eval_memo(ns, n.b, params, np, memo, done)) ? 1.0
-                                                                                                                 : 0.0;
-      break;
-    case Op::Select:
-      v = eval_memo(ns, n.a, params, np, memo, done) != 0.0 ? eval_memo(ns, n.b, params, np, memo, done)
-                                                            : eval_memo(ns, n.c, params, np, memo, done);
-      break;
-    default: v = apply_unary(n.op, eval_memo(ns, n.a, params, np, memo, done)); break;
-  }
-  memo[id] = v;
-  done[id] = 1;
-  return v;
-}
-}  // namespace
 
 void LoweredKernel::fill_args(const double* params, size_t np, unsigned char* out) const {
   std::memset(out, 0, args_bytes());
   double* d = reinterpret_cast<double*>(out);
   float* f = reinterpret_cast<float*>(out + size_t(nd) * 8);
-  thread_local std::vector<double> memo;
-  thread_local std::vector<char> done;
-  memo.assign(nodes.size(), 0.0);
-  done.assign(nodes.size(), 0);
+  // Straight-line evaluation of the nodes the slots read (both arms of a
+  // select are evaluated; their values only feed the select), into a scratch
+  // array of which only those entries are written and read.
+  thread_local std::vector<double> val;
+  if (val.size() < nodes.size()) val.resize(nodes.size());
+  for (int id : eval_order) {
+    const Node& n = nodes[id];
+    double v;
+    switch (n.op) {
+      case Op::Const: v = n.value; break;
+      case Op::Param: v = size_t(n.index) < np ? params[n.index] : 0.0; break;
+      case Op::Input: throw std::runtime_error("input column in a parameter-only value");
+      case Op::Add: case Op::Sub: case Op::Mul: case Op::Div: case Op::Pow: v = apply_binary(n.op, val[n.a], val[n.b]); break;
+      case Op::Cmp: v = apply_cmp(n.cmp, val[n.a], val[n.b]) ? 1.0 : 0.0; break;
+      case Op::Select: v = val[n.a] != 0.0 ? val[n.b] : val[n.c]; break;
+      default: v = apply_unary(n.op, val[n.a]); break;
+    }
+    val[id] = v;
+  }
   for (const auto& sl : slots) {
-    const double v = eval_memo(nodes, sl.node, params, np, memo, done);
+    const double v = val[sl.node];
     switch (sl.kind) {
       case UniformSlot::Double: d[sl.offset] = v; break;
       case UniformSlot::Float: f[sl.offset] = float(v); break;

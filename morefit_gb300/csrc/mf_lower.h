@@ -100,6 +100,7 @@ struct LoweredKernel {
   bool host_args = false;
   std::vector<Node> nodes;         // the DAG, for host evaluation of the slots
   std::vector<UniformSlot> slots;
+  std::vector<int> eval_order;     // parameter-only nodes the slots read, operands first
   int nd = 1, nf = 1;              // array lengths in the struct (>= 1)
   size_t args_bytes() const { return (size_t(nd) * 8 + size_t(nf) * 4 + 7) / 8 * 8; }
   // Fills the argument struct for one parameter vector (params: n_params doubles).

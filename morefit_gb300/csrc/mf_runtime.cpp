@@ -992,6 +992,81 @@ struct mf_expr_set {
   mf_expr_set(const std::vector<std::string>& names) : dag({}, names), n_names(uint32_t(names.size())) {}
 };
 
+namespace {
+// mf_spd_solve_batch for orders up to kSpdLaneOrder: kSpdLanes matrices in
+// lockstep, the lane index innermost, so that the factorisations' dependent
+// multiply-add chains of different matrices overlap (and vectorise). Lanes
+// beyond nb factor the identity; a lane that meets a non-positive pivot
+// continues on 1.0 and is reported in ok[] (its outputs are not written).
+constexpr uint32_t kSpdLanes = 8, kSpdLaneOrder = 16;
+void spd_lanes(uint32_t nb, uint32_t p, const double* h, const double* g, double* x, double* dinv,
+               unsigned char* ok) {
+  constexpr uint32_t B = kSpdLanes;
+  double lf[kSpdLaneOrder][kSpdLaneOrder][B], rd[kSpdLaneOrder][B], y[kSpdLaneOrder][B], v[B];
+  bool pd[B];
+  for (uint32_t b = 0; b < B; b++) pd[b] = true;
+  auto elem = [&](uint32_t b, uint32_t i, uint32_t j) {
+    return b < nb ? h[(size_t(b) * p + i) * p + j] : (i == j ? 1.0 : 0.0);
+  };
+  for (uint32_t i = 0; i < p; i++) {
+    for (uint32_t j = 0; j < i; j++) {
+      for (uint32_t b = 0; b < B; b++) v[b] = elem(b, i, j);
+      for (uint32_t k = 0; k < j; k++)
+        for (uint32_t b = 0; b < B; b++) v[b] -= lf[i][k][b] * lf[j][k][b];
+      for (uint32_t b = 0; b < B; b++) lf[i][j][b] = v[b] * rd[j][b];
+    }
+    for (uint32_t b = 0; b < B; b++) v[b] = elem(b, i, i);
+    for (uint32_t k = 0; k < i; k++)
+      for (uint32_t b = 0; b < B; b++) v[b] -= lf[i][k][b] * lf[i][k][b];
+    for (uint32_t b = 0; b < B; b++) {
+      if (!(v[b] > 0.0)) {
+        pd[b] = false;
+        v[b] = 1.0;
+      }
+      lf[i][i][b] = std::sqrt(v[b]);
+      rd[i][b] = 1.0 / lf[i][i][b];
+    }
+  }
+  for (uint32_t b = 0; b < nb; b++) ok[b] = pd[b] ? 1 : 0;
+  if (g) {
+    double xs[kSpdLaneOrder][B];
+    for (uint32_t i = 0; i < p; i++) {
+      for (uint32_t b = 0; b < B; b++) v[b] = b < nb ? g[size_t(b) * p + i] : 0.0;
+      for (uint32_t k = 0; k < i; k++)
+        for (uint32_t b = 0; b < B; b++) v[b] -= lf[i][k][b] * y[k][b];
+      for (uint32_t b = 0; b < B; b++) y[i][b] = v[b] * rd[i][b];
+    }
+    for (uint32_t i = p; i-- > 0;) {
+      for (uint32_t b = 0; b < B; b++) v[b] = y[i][b];
+      for (uint32_t k = i + 1; k < p; k++)
+        for (uint32_t b = 0; b < B; b++) v[b] -= lf[k][i][b] * xs[k][b];
+      for (uint32_t b = 0; b < B; b++) xs[i][b] = v[b] * rd[i][b];
+    }
+    for (uint32_t b = 0; b < nb; b++)
+      if (pd[b])
+        for (uint32_t i = 0; i < p; i++) x[size_t(b) * p + i] = xs[i][b];
+  }
+  if (dinv) {
+    // diag(H^-1)[i] = sum over r >= i of (L^-1)[r][i]^2
+    for (uint32_t i = 0; i < p; i++) {
+      double sum[B];
+      for (uint32_t b = 0; b < B; b++) sum[b] = 0.0;
+      for (uint32_t r = i; r < p; r++) {
+        for (uint32_t b = 0; b < B; b++) v[b] = r == i ? 1.0 : 0.0;
+        for (uint32_t k = i; k < r; k++)
+          for (uint32_t b = 0; b < B; b++) v[b] -= lf[r][k][b] * y[k][b];
+        for (uint32_t b = 0; b < B; b++) {
+          y[r][b] = v[b] * rd[r][b];
+          sum[b] += y[r][b] * y[r][b];
+        }
+      }
+      for (uint32_t b = 0; b < nb; b++)
+        if (pd[b]) dinv[size_t(b) * p + i] = sum[b];
+    }
+  }
+}
+}  // namespace
+
 extern "C" {
 
 int mf_expr_set_create(uint32_t n_names, const char* const* names, uint32_t n_exprs, const char* const* exprs,
@@ -1023,6 +1098,75 @@ int mf_expr_set_eval(const mf_expr_set* set, uint32_t n_rows, const double* valu
 
 int mf_expr_set_free(mf_expr_set* set) {
   delete set;
+  return MF_OK;
+}
+
+int mf_spd_solve_batch(uint32_t n, uint32_t p, const double* h, const double* g, double* x, double* dinv,
+                       unsigned char* ok) {
+  if (p == 0 || p > 64) return fail(MF_ERR_INVALID, "matrix order must be 1 to 64");
+  if (n && (!h || !ok || (!g) != (!x))) return fail(MF_ERR_INVALID, "null argument");
+  if (p <= kSpdLaneOrder) {
+    for (uint32_t t = 0; t < n; t += kSpdLanes) {
+      const uint32_t nb = std::min<uint32_t>(kSpdLanes, n - t);
+      spd_lanes(nb, p, h + size_t(t) * p * p, g ? g + size_t(t) * p : nullptr, x ? x + size_t(t) * p : nullptr,
+                dinv ? dinv + size_t(t) * p : nullptr, ok + t);
+    }
+    return MF_OK;
+  }
+  // larger orders: one matrix at a time. lf: lower Cholesky factor (row
+  // stride 64); rd[i] = 1 / L[i][i]
+  double lf[64 * 64], rd[64], y[64];
+  for (uint32_t t = 0; t < n; t++) {
+    const double* a = h + size_t(t) * p * p;
+    bool pd = true;
+    for (uint32_t i = 0; i < p && pd; i++) {
+      double* li = lf + i * 64;
+      for (uint32_t j = 0; j < i; j++) {
+        const double* lj = lf + j * 64;
+        double v = a[i * p + j];
+        for (uint32_t k = 0; k < j; k++) v -= li[k] * lj[k];
+        li[j] = v * rd[j];
+      }
+      double v = a[i * p + i];
+      for (uint32_t k = 0; k < i; k++) v -= li[k] * li[k];
+      if (!(v > 0.0)) {
+        pd = false;
+        break;
+      }
+      li[i] = std::sqrt(v);
+      rd[i] = 1.0 / li[i];
+    }
+    ok[t] = pd ? 1 : 0;
+    if (!pd) continue;
+    if (g) {
+      const double* gt = g + size_t(t) * p;
+      double* xt = x + size_t(t) * p;
+      for (uint32_t i = 0; i < p; i++) {
+        double v = gt[i];
+        for (uint32_t k = 0; k < i; k++) v -= lf[i * 64 + k] * y[k];
+        y[i] = v * rd[i];
+      }
+      for (uint32_t i = p; i-- > 0;) {
+        double v = y[i];
+        for (uint32_t k = i + 1; k < p; k++) v -= lf[k * 64 + i] * xt[k];
+        xt[i] = v * rd[i];
+      }
+    }
+    if (dinv) {
+      // diag(H^-1)[i] = sum over r >= i of (L^-1)[r][i]^2; column i of L^-1 by forward substitution
+      double* dt = dinv + size_t(t) * p;
+      for (uint32_t i = 0; i < p; i++) {
+        double sum = 0.0;
+        for (uint32_t r = i; r < p; r++) {
+          double v = r == i ? 1.0 : 0.0;
+          for (uint32_t k = i; k < r; k++) v -= lf[r * 64 + k] * y[k];
+          y[r] = v * rd[r];
+          sum += y[r] * y[r];
+        }
+        dt[i] = sum;
+      }
+    }
+  }
   return MF_OK;
 }
 

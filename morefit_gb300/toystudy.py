@@ -14,7 +14,7 @@ precompute launch hoists the event-only columns of all toys. The fit is a
 batched Newton iteration on F = -2 sum log p: each iteration evaluates F and
 its gradient for every active toy in one ragged-segment launch (one block per
 toy, mf_kernel_reduce_segments), the Hessian in a second, solves the 8x8
-systems on the host, and tries the step with a third (F only), halving it per
+systems on the host (Cholesky vectorised over the toys), and tries the step with a third (F only), halving it per
 toy until F does not increase. Parameters are kept inside their limits.
 Converged toys (Newton decrement g^T H^-1 g / 2 below ``tol``) leave the
 active set. Errors are sqrt(diag(2 H^-1)) at the minimum (errordef 1 on
@@ -78,13 +78,53 @@ class SegmentLikelihood:
     def hessian(self, idx, theta):
         s = self._submit("lh_hessian_kernel", idx, theta)
         npar = theta.shape[1]
-        h = np.zeros((len(idx), npar, npar))
-        k = 0
-        for i in range(npar):
-            for j in range(i + 1):
-                h[:, i, j] = h[:, j, i] = -2.0 * s[:, k]
-                k += 1
+        i, j = np.tril_indices(npar)  # row-major lower triangle: the kernel's output order
+        h = np.empty((len(idx), npar, npar))
+        h[:, i, j] = -2.0 * s
+        h[:, j, i] = -2.0 * s
         return h
+
+
+def _spd_solve(h: np.ndarray, g: np.ndarray | None):
+    """Cholesky solves of a batch of symmetric matrices h (n, p, p) in the
+    library (mf_spd_solve_batch): (x = h^-1 g or None, diag(h^-1), ok)."""
+    h = np.ascontiguousarray(h, dtype=np.float64)
+    n, p, _ = h.shape
+    ok = np.zeros(n, dtype=np.uint8)
+    dinv = np.zeros((n, p))
+    x = None
+    gp = xp = None
+    if g is not None:
+        g = np.ascontiguousarray(g, dtype=np.float64)
+        x = np.zeros((n, p))
+        gp, xp = L.dptr(g), L.dptr(x)
+    L.check(L.lib.mf_spd_solve_batch(n, p, L.dptr(h), gp, xp, L.dptr(dinv), ok.ctypes.data_as(C.POINTER(C.c_uint8))))
+    return x, dinv, ok.astype(bool)
+
+
+def _newton_steps(h: np.ndarray, g: np.ndarray) -> np.ndarray:
+    """-H^-1 g per toy: Cholesky where H is positive definite, LAPACK's
+    pivoted solve for the others."""
+    x, _, ok = _spd_solve(h, g)
+    step = -x
+    bad = np.nonzero(~ok)[0]
+    if bad.size:
+        try:
+            step[bad] = -np.linalg.solve(h[bad], g[bad][..., None])[..., 0]
+        except np.linalg.LinAlgError:
+            for t in bad:
+                step[t] = -np.linalg.lstsq(h[t], g[t], rcond=None)[0]
+    return step
+
+
+def _inverse_diagonal(h: np.ndarray) -> np.ndarray:
+    """diag(H^-1) per toy: from the Cholesky factor where H is positive
+    definite, LAPACK's inverse for the others."""
+    _, diag, ok = _spd_solve(h, None)
+    bad = np.nonzero(~ok)[0]
+    if bad.size:
+        diag[bad] = np.einsum("tii->ti", np.linalg.inv(h[bad]))
+    return diag
 
 
 def fit_segments(sl: SegmentLikelihood, theta0: np.ndarray, limits, tol: float = 1e-9, max_iter: int = 50,
@@ -106,12 +146,7 @@ def fit_segments(sl: SegmentLikelihood, theta0: np.ndarray, limits, tol: float =
         f, g = sl.value_and_gradient(active, th)
         h = sl.hessian(active, th)
         fmin[active] = f
-        try:
-            step = -np.linalg.solve(h, g[..., None])[..., 0]
-        except np.linalg.LinAlgError:
-            step = np.zeros_like(g)
-            for t in range(len(active)):
-                step[t] = -np.linalg.lstsq(h[t], g[t], rcond=None)[0]
+        step = _newton_steps(h, g)
         dec = -0.5 * np.einsum("ij,ij->i", g, step)
         # a Hessian that is not positive definite: fall back to a scaled gradient step
         bad = ~(dec > 0) | ~np.isfinite(dec)
@@ -143,8 +178,7 @@ def fit_segments(sl: SegmentLikelihood, theta0: np.ndarray, limits, tol: float =
     f, g = sl.value_and_gradient(idx, theta)
     h = sl.hessian(idx, theta)
     fmin[:] = f
-    cov = 2.0 * np.linalg.inv(h)
-    errors = np.sqrt(np.abs(np.einsum("tii->ti", cov)))
+    errors = np.sqrt(np.abs(2.0 * _inverse_diagonal(h)))
     return FitResult(theta, errors, fmin, edm, iters, conv, sl.evaluations)
 
 
