@@ -182,17 +182,35 @@ def fit_segments(sl: SegmentLikelihood, theta0: np.ndarray, limits, tol: float =
     return FitResult(theta, errors, fmin, edm, iters, conv, sl.evaluations)
 
 
+def _log_argument(expr: str):
+    """X when ``expr`` is exactly log(X) (one top-level logarithm), else None."""
+    if not (expr.startswith("log(") and expr.endswith(")")):
+        return None
+    depth = 0
+    for i, ch in enumerate(expr[3:], start=3):
+        depth += ch == "("
+        depth -= ch == ")"
+        if depth == 0:
+            return expr[4:-1] if i == len(expr) - 1 else None
+    return None
+
+
 def density_expression(spec: dict):
     """The model's density as one expression of the raw observables with the
     fitter's parameters: exp of the log-density kernel text (the lh kernel,
     fitter.hh:380-396) with every hoisted event buffer replaced by its own
-    expression. Returns (expression, parameter names, parameter-buffer list)."""
+    expression. A log-density that is one logarithm, log(X), gives X itself:
+    the same density where X > 0, and where X <= 0 both forms reject every
+    proposal (exp(log X) is NaN or 0 there), without a NaN that would send
+    the generator's fast accept test to its exact FP64 path. Returns
+    (expression, parameter names, parameter-buffer list)."""
     k = next(k for k in spec["kernels"] if k["name"] == "lh_kernel")
     expr = k["exprs"][0]
     for name, e in sorted(spec["event_buffers"], key=lambda x: -len(x[0])):
         if name != e:
             expr = re.sub(r"\b" + re.escape(name) + r"\b", "(" + e + ")", expr)
-    return "exp(" + expr + ")", list(k["params"]), spec["lh_buffers"]
+    inner = _log_argument(expr)
+    return (inner if inner is not None else "exp(" + expr + ")"), list(k["params"]), spec["lh_buffers"]
 
 
 def pwave_maxprob(theta: np.ndarray) -> np.ndarray:
