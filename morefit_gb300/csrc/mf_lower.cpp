@@ -2001,39 +2001,51 @@ __device__ __forceinline__ unsigned mf_xoshiro(unsigned* s) {
 
 
 void LoweredKernel::fill_args(const double* params, size_t np, unsigned char* out) const {
-  std::memset(out, 0, args_bytes());
-  double* d = reinterpret_cast<double*>(out);
-  float* f = reinterpret_cast<float*>(out + size_t(nd) * 8);
+  fill_args_many(params, np, 1, out);
+}
+
+void LoweredKernel::fill_args_many(const double* params, size_t np, size_t count, unsigned char* out) const {
   // Straight-line evaluation of the nodes the slots read (both arms of a
   // select are evaluated; their values only feed the select), into a scratch
-  // array of which only those entries are written and read.
-  thread_local std::vector<double> val;
-  if (val.size() < nodes.size()) val.resize(nodes.size());
-  for (int id : eval_order) {
-    const Node& n = nodes[id];
-    double v;
-    switch (n.op) {
-      case Op::Const: v = n.value; break;
-      case Op::Param: v = size_t(n.index) < np ? params[n.index] : 0.0; break;
-      case Op::Input: throw std::runtime_error("input column in a parameter-only value");
-      case Op::Add: case Op::Sub: case Op::Mul: case Op::Div: case Op::Pow: v = apply_binary(n.op, val[n.a], val[n.b]); break;
-      case Op::Cmp: v = apply_cmp(n.cmp, val[n.a], val[n.b]) ? 1.0 : 0.0; break;
-      case Op::Select: v = val[n.a] != 0.0 ? val[n.b] : val[n.c]; break;
-      default: v = apply_unary(n.op, val[n.a]); break;
+  // array of which only those entries are written and read; one scratch for
+  // all rows.
+  std::vector<double> val(nodes.size());
+  const size_t ab = args_bytes();
+  for (size_t r = 0; r < count; r++) {
+    const double* pr = params + r * np;
+    unsigned char* o = out + r * ab;
+    std::memset(o, 0, ab);
+    for (int id : eval_order) {
+      const Node& n = nodes[id];
+      double v;
+      switch (n.op) {
+        case Op::Const: v = n.value; break;
+        case Op::Param: v = size_t(n.index) < np ? pr[n.index] : 0.0; break;
+        case Op::Input: throw std::runtime_error("input column in a parameter-only value");
+        case Op::Add: v = val[n.a] + val[n.b]; break;
+        case Op::Sub: v = val[n.a] - val[n.b]; break;
+        case Op::Mul: v = val[n.a] * val[n.b]; break;
+        case Op::Div: case Op::Pow: v = apply_binary(n.op, val[n.a], val[n.b]); break;
+        case Op::Cmp: v = apply_cmp(n.cmp, val[n.a], val[n.b]) ? 1.0 : 0.0; break;
+        case Op::Select: v = val[n.a] != 0.0 ? val[n.b] : val[n.c]; break;
+        default: v = apply_unary(n.op, val[n.a]); break;
+      }
+      val[id] = v;
     }
-    val[id] = v;
-  }
-  for (const auto& sl : slots) {
-    const double v = val[sl.node];
-    switch (sl.kind) {
-      case UniformSlot::Double: d[sl.offset] = v; break;
-      case UniformSlot::Float: f[sl.offset] = float(v); break;
-      case UniformSlot::Bool: f[sl.offset] = v != 0.0 ? 1.0f : 0.0f; break;
-      case UniformSlot::DwPair: {
-        const float h = float(v);
-        f[sl.offset] = h;
-        f[sl.offset + 1] = float(v - double(h));
-        break;
+    double* d = reinterpret_cast<double*>(o);
+    float* f = reinterpret_cast<float*>(o + size_t(nd) * 8);
+    for (const auto& sl : slots) {
+      const double v = val[sl.node];
+      switch (sl.kind) {
+        case UniformSlot::Double: d[sl.offset] = v; break;
+        case UniformSlot::Float: f[sl.offset] = float(v); break;
+        case UniformSlot::Bool: f[sl.offset] = v != 0.0 ? 1.0f : 0.0f; break;
+        case UniformSlot::DwPair: {
+          const float h = float(v);
+          f[sl.offset] = h;
+          f[sl.offset + 1] = float(v - double(h));
+          break;
+        }
       }
     }
   }

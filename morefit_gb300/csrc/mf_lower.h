@@ -105,6 +105,9 @@ struct LoweredKernel {
   size_t args_bytes() const { return (size_t(nd) * 8 + size_t(nf) * 4 + 7) / 8 * 8; }
   // Fills the argument struct for one parameter vector (params: n_params doubles).
   void fill_args(const double* params, size_t n_params, unsigned char* out) const;
+  // The same for `count` parameter vectors (back to back) into `count`
+  // argument structs (args_bytes() apart).
+  void fill_args_many(const double* params, size_t n_params, size_t count, unsigned char* out) const;
 };
 
 // Rewrite of a REDUCE kernel over prepared columns (mf_fold.cpp). When

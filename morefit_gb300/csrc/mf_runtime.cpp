@@ -1600,8 +1600,7 @@ int mf_kernel_reduce_segments(mf_kernel* k, const mf_buffer* in, uint64_t stride
   std::memcpy(host.data(), seg_begin, bytes_begin);
   std::memcpy(host.data() + bytes_begin, seg_count, size_t(nseg) * 4);
   try {
-    for (uint32_t s = 0; s < nseg; s++)
-      k->lowered.fill_args(params + size_t(s) * n_params, n_params, host.data() + bytes_begin + bytes_count + s * ab);
+    k->lowered.fill_args_many(params, n_params, nseg, host.data() + bytes_begin + bytes_count);
   } catch (const std::exception& e) {
     return fail(MF_ERR_INVALID, std::string("parameter evaluation: ") + e.what());
   }
