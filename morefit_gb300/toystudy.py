@@ -76,13 +76,28 @@ class SegmentLikelihood:
         return -2.0 * s[:, 0], -2.0 * s[:, 1:]
 
     def hessian(self, idx, theta):
-        s = self._submit("lh_hessian_kernel", idx, theta)
+        return _unpack_hessian(self._submit("lh_hessian_kernel", idx, theta), theta.shape[1])
+
+    def value_gradient_hessian(self, idx, theta):
+        """F, gradient and Hessian per segment: one launch of the combined
+        kernel where the model has one, else two."""
+        name = self.like.combined_kernel()
+        if name is None:
+            f, g = self.value_and_gradient(idx, theta)
+            return f, g, self.hessian(idx, theta)
+        s = self._submit(name, idx, theta)
         npar = theta.shape[1]
-        i, j = np.tril_indices(npar)  # row-major lower triangle: the kernel's output order
-        h = np.empty((len(idx), npar, npar))
-        h[:, i, j] = -2.0 * s
-        h[:, j, i] = -2.0 * s
-        return h
+        return -2.0 * s[:, 0], -2.0 * s[:, 1:1 + npar], _unpack_hessian(s[:, 1 + npar:], npar)
+
+
+def _unpack_hessian(s: np.ndarray, npar: int) -> np.ndarray:
+    """-2 x the Hessian kernel's sums (row-major lower triangle per row) as
+    full symmetric matrices (n, npar, npar)."""
+    i, j = np.tril_indices(npar)
+    h = np.empty((len(s), npar, npar))
+    h[:, i, j] = -2.0 * s
+    h[:, j, i] = -2.0 * s
+    return h
 
 
 def _spd_solve(h: np.ndarray, g: np.ndarray | None):
@@ -143,8 +158,7 @@ def fit_segments(sl: SegmentLikelihood, theta0: np.ndarray, limits, tol: float =
         if active.size == 0:
             break
         th = theta[active]
-        f, g = sl.value_and_gradient(active, th)
-        h = sl.hessian(active, th)
+        f, g, h = sl.value_gradient_hessian(active, th)
         fmin[active] = f
         step = _newton_steps(h, g)
         dec = -0.5 * np.einsum("ij,ij->i", g, step)
@@ -175,8 +189,7 @@ def fit_segments(sl: SegmentLikelihood, theta0: np.ndarray, limits, tol: float =
         active = active[~done]
     # errors from the Hessian at the final point
     idx = np.arange(ntoy)
-    f, g = sl.value_and_gradient(idx, theta)
-    h = sl.hessian(idx, theta)
+    f, g, h = sl.value_gradient_hessian(idx, theta)
     fmin[:] = f
     errors = np.sqrt(np.abs(2.0 * _inverse_diagonal(h)))
     return FitResult(theta, errors, fmin, edm, iters, conv, sl.evaluations)
@@ -282,7 +295,8 @@ class ToyStudy:
                  seed: int = DEFAULT_SEED, generator_threads: int = 65536, block: int = 0):
         """``block``: threads per segment of the segment kernels; 0 = tuned on
         the first study of at least TUNE_MIN_TOYS toys (the candidate whose
-        F + gradient launch over that study's toys is fastest on the device),
+        F + gradient + Hessian launch over that study's toys is fastest on
+        the device),
         256 until then."""
         self.backend = backend
         self.spec = spec
@@ -307,10 +321,10 @@ class ToyStudy:
             like = self._likelihood(blk)
             like.set_device_data(cols)
             sl = SegmentLikelihood(like, begins, counts)
-            sl.value_and_gradient(idx, truth)  # makes the prepared copy
+            sl.value_gradient_hessian(idx, truth)  # builds the kernels and the prepared copy
             t0 = time.perf_counter()
             for _ in range(3):
-                sl.value_and_gradient(idx, truth)
+                sl.value_gradient_hessian(idx, truth)
             times[blk] = (time.perf_counter() - t0) / 3
         self.block = min(times, key=times.get)
         self.tuning = {"block": self.block, "launch_s": times, "toys": len(counts)}

@@ -24,6 +24,7 @@ the covariance to -2 H^-1 F H^-1 (fitter.hh:894-943). ``fisher()`` and
 from __future__ import annotations
 
 import json
+import re
 from pathlib import Path
 
 import numpy as np
@@ -75,11 +76,12 @@ class Likelihood:
         # The precompute runs in double-float (FP32 pipe) unless native FP64 is asked for.
         self.pre = CUDABlock(backend, np.float64 if mixed_raw else kernelT, native_f64=native_f64)
         self.blocks = {}
+        self._block_args = dict(native_f64=native_f64, vec=vec, block=block, f32_arith=mixed_raw, pipeline=pipeline,
+                                stages=stages)
         for name in ("lh_kernel", "lh_grad_kernel", "lh_hessian_kernel", "lh_fisher_kernel"):
             if name not in ks:
                 continue
-            b = CUDABlock(backend, kernelT, native_f64=native_f64, vec=vec, block=block, f32_arith=mixed_raw,
-                          pipeline=pipeline, stages=stages)
+            b = CUDABlock(backend, kernelT, **self._block_args)
             if self.has_precompute:
                 b.SetupInputBuffer(self.pre, False)
             else:
@@ -244,6 +246,58 @@ class Likelihood:
     def hessian(self, theta) -> np.ndarray:
         return self._symmetric(self.sums("lh_hessian_kernel", theta))
 
+    COMBINED = "lh_grad_hessian_kernel"
+
+    def combined_kernel(self):
+        """Name of the F + gradient + Hessian kernel (the gradient kernel's
+        outputs followed by the Hessian kernel's, in one launch that shares
+        their common subexpressions; the Hessian's parameter buffers renamed),
+        built on first use. None where the model has no Hessian kernel, the
+        two kernels read different inputs or parameter buffers, or the
+        combined kernel would spill registers."""
+        if "_combined" in self.__dict__:
+            return self._combined
+        self._combined = None
+        ks = self.kspec
+        if "lh_grad_kernel" not in ks or "lh_hessian_kernel" not in ks:
+            return None
+        g, h = ks["lh_grad_kernel"], ks["lh_hessian_kernel"]
+        nth = len(self.params)
+        gbuf, hbuf = self.buffers["lh_grad_kernel"], self.buffers["lh_hessian_kernel"]
+        if g["inputs"] != h["inputs"] or list(g["params"][nth:]) != [n for n, _ in gbuf] \
+                or list(h["params"][nth:]) != [n for n, _ in hbuf] or g["params"][:nth] != h["params"][:nth]:
+            return None
+
+        def ren(e):
+            return re.sub(r"\bmorefit_parambuffer_(\d+)\b", r"mfh_parambuffer_\1", e)
+        hb = [(ren(n), ren(e)) for n, e in hbuf]
+        params = list(g["params"]) + [n for n, _ in hb]
+        exprs = list(g["exprs"]) + [ren(e) for e in h["exprs"]]
+        defs = dict(gbuf)
+        defs.update(dict(hb))
+        b = CUDABlock(self.backend, self.kernelT, **self._block_args)
+        b.SetupInputBuffer(self.pre, not self.has_precompute)
+        b.MakeComputeKernel(self.COMBINED, 0, g["inputs"], [f"r{i}" for i in range(len(exprs))], params, exprs, True,
+                            param_defs=[defs.get(p, "") for p in params])
+        if b.kernel.info()["spill_bytes"] > 0:
+            return None
+        b.SetNevents(self.nevents)
+        self.buffers[self.COMBINED] = list(gbuf) + hb
+        self.blocks[self.COMBINED] = b
+        self._combined = self.COMBINED
+        return self._combined
+
+    def value_gradient_hessian(self, theta):
+        """(-2 ln L, its gradient, its Hessian) at theta: one launch of the
+        combined kernel where it exists, else the two kernels."""
+        name = self.combined_kernel()
+        if name is None:
+            f, g = self.likelihood_and_gradient(theta)
+            return f, g, self.hessian(theta)
+        s = self.sums(name, theta)
+        npar = len(self.params)
+        return -2.0 * float(s[0]), -2.0 * s[1:1 + npar], self._symmetric(s[1 + npar:])
+
     def fisher(self, theta) -> np.ndarray:
         """-2 sum d(w log p)/dtheta_i d(w log p)/dtheta_j (fitter.hh:1328-1370)."""
         if "lh_fisher_kernel" not in self.blocks:
@@ -327,6 +381,12 @@ class _WholeDataset:
     def hessian(self, idx, theta):
         self.evaluations += len(theta)
         return np.array([self.like.hessian(t) for t in theta])
+
+    def value_gradient_hessian(self, idx, theta):
+        self.evaluations += len(theta)
+        fgh = [self.like.value_gradient_hessian(t) for t in theta]
+        return (np.array([f for f, _, _ in fgh]), np.array([g for _, g, _ in fgh]),
+                np.array([h for _, _, h in fgh]))
 
 
 def seed_rows(nrows: int, seed: int = DEFAULT_SEED) -> np.ndarray:

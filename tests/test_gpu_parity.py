@@ -172,6 +172,40 @@ def test_deterministic(backend):
     assert np.array_equal(a, b)
 
 
+@pytest.mark.parametrize("workload", ["pwave", "mass", "cbpoly"])
+def test_combined_gradient_hessian_kernel(backend, workload):
+    """The F + gradient + Hessian kernel (one launch, Hessian parameter buffers
+    renamed) gives the two kernels' values: F and gradient within 1e-12 of
+    the sum of absolute per-event terms, the Hessian within 1e-12 of its
+    largest element. Models whose combined kernel would spill fall back to
+    the two launches, with the same results."""
+    from morefit_gb300.toystudy import SegmentLikelihood
+    from morefit_gb300.workloads import Likelihood
+    g = load_golden(f"{workload}_n1000.json")
+    ev = golden_events(workload, 1000)
+    like = Likelihood(backend, g, np.float64)
+    like.set_data(ev)
+    cols = _cols(g, ev)
+    for pt in g["points"]:
+        f, grad, h = like.value_gradient_hessian(pt["params"])
+        f2, grad2 = like.likelihood_and_gradient(pt["params"])
+        h2 = like.hessian(pt["params"])
+        scale = 2.0 * _abs_scale(g, "lh_grad_kernel", cols, pt["kernel_params"]["lh_grad_kernel"])
+        assert abs(f - f2) <= 1e-12 * scale[0]
+        assert np.all(np.abs(grad - grad2) <= 1e-12 * scale[1:])
+        assert np.all(np.abs(h - h2) <= 1e-12 * np.abs(h2).max())
+    if workload == "pwave":
+        assert like.combined_kernel() is not None
+    # ragged segments through the same kernel: halves of the dataset
+    sl = SegmentLikelihood(like, [0, 500], [500, 500])
+    th = np.array([g["points"][0]["params"]] * 2)
+    fs, gs, hs = sl.value_gradient_hessian(np.arange(2), th)
+    f0, g0 = sl.value_and_gradient(np.arange(2), th)
+    np.testing.assert_allclose(fs, f0, rtol=1e-12)
+    np.testing.assert_allclose(gs, g0, rtol=1e-9, atol=1e-9 * np.abs(g0).max())
+    np.testing.assert_allclose(hs, sl.hessian(np.arange(2), th), rtol=1e-9, atol=1e-12 * np.abs(hs).max())
+
+
 @pytest.mark.parametrize("workload", ["pwave", "mass", "mass_w"])
 def test_sync_evaluation_equals_parameter_vector_path(backend, workload):
     """sums(kernel, theta), whose hoisted parameter buffers are evaluated in
