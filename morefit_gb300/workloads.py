@@ -247,6 +247,7 @@ class Likelihood:
         return self._symmetric(self.sums("lh_hessian_kernel", theta))
 
     COMBINED = "lh_grad_hessian_kernel"
+    COMBINED_MAX_SPILL = 64  # bytes per thread (a few values of call frame)
 
     def combined_kernel(self):
         """Name of the F + gradient + Hessian kernel (the gradient kernel's
@@ -254,7 +255,8 @@ class Likelihood:
         their common subexpressions; the Hessian's parameter buffers renamed),
         built on first use. None where the model has no Hessian kernel, the
         two kernels read different inputs or parameter buffers, or the
-        combined kernel would spill registers."""
+        combined kernel would spill more than COMBINED_MAX_SPILL bytes of
+        registers."""
         if "_combined" in self.__dict__:
             return self._combined
         self._combined = None
@@ -279,7 +281,7 @@ class Likelihood:
         b.SetupInputBuffer(self.pre, not self.has_precompute)
         b.MakeComputeKernel(self.COMBINED, 0, g["inputs"], [f"r{i}" for i in range(len(exprs))], params, exprs, True,
                             param_defs=[defs.get(p, "") for p in params])
-        if b.kernel.info()["spill_bytes"] > 0:
+        if b.kernel.info()["spill_bytes"] > self.COMBINED_MAX_SPILL:
             return None
         b.SetNevents(self.nevents)
         self.buffers[self.COMBINED] = list(gbuf) + hb
