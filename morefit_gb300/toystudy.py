@@ -90,14 +90,21 @@ class SegmentLikelihood:
         return -2.0 * s[:, 0], -2.0 * s[:, 1:1 + npar], _unpack_hessian(s[:, 1 + npar:], npar)
 
 
+_TRIL_FULL = {}  # npar -> for each of the npar * npar positions, its index in the packed lower triangle
+
+
 def _unpack_hessian(s: np.ndarray, npar: int) -> np.ndarray:
     """-2 x the Hessian kernel's sums (row-major lower triangle per row) as
-    full symmetric matrices (n, npar, npar)."""
-    i, j = np.tril_indices(npar)
-    h = np.empty((len(s), npar, npar))
-    h[:, i, j] = -2.0 * s
-    h[:, j, i] = -2.0 * s
-    return h
+    full symmetric matrices (n, npar, npar): one gather through a flat index
+    map (two advanced-index assignments cost several times more)."""
+    flat = _TRIL_FULL.get(npar)
+    if flat is None:
+        i, j = np.tril_indices(npar)
+        m = np.empty((npar, npar), dtype=np.intp)
+        m[i, j] = np.arange(len(i))
+        m[j, i] = np.arange(len(i))
+        flat = _TRIL_FULL[npar] = m.ravel()
+    return (-2.0 * np.asarray(s))[:, flat].reshape(len(s), npar, npar)
 
 
 def _spd_solve(h: np.ndarray, g: np.ndarray | None):
