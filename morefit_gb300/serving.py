@@ -67,25 +67,32 @@ class FitOutcome:
 
 
 def newton_fit(theta0, limits, edm_tol: float = 2e-5, max_iter: int = 100, f_noise: float = 0.0,
-               max_halvings: int = 30):
+               max_halvings: int = 30, combined: bool = False):
     """Coroutine minimiser of F = -2 ln L with the analytic Hessian: damped
     Newton steps inside the parameter limits, halved until F does not rise
     by more than its own precision (``f_noise`` relative: a few 1e-9 for FP32
     per-event arithmetic with compensated sums), until the estimated distance
     to the minimum g^T H^-1 g / 2 is below ``edm_tol``. Yields ("grad", theta)
-    and ("hess", theta), receives (F, gradient) and the Hessian; returns
-    (theta, errors, F, converged, evaluations), errors sqrt(diag(2 H^-1))."""
+    and ("hess", theta), receives (F, gradient) and the Hessian; with
+    ``combined`` it yields ("gh", theta) instead and receives (F, gradient,
+    Hessian) from one evaluation, at the start point and at every step trial,
+    so an accepted step needs no separate Hessian request. Returns (theta,
+    errors, F, converged, evaluations), errors sqrt(diag(2 H^-1))."""
     lo = np.array([a for a, _ in limits])
     hi = np.array([b for _, b in limits])
     x = np.clip(np.array(theta0, dtype=np.float64), lo, hi)
     n_eval = 0
     converged = False
-    f, g = yield ("grad", x)
-    n_eval += 1
     h = None
+    if combined:
+        f, g, h = yield ("gh", x)
+    else:
+        f, g = yield ("grad", x)
+    n_eval += 1
     for _ in range(max_iter):
-        h = yield ("hess", x)
-        n_eval += 1
+        if not combined:
+            h = yield ("hess", x)
+            n_eval += 1
         try:
             p = -np.linalg.solve(h, g)
         except np.linalg.LinAlgError:
@@ -100,7 +107,10 @@ def newton_fit(theta0, limits, edm_tol: float = 2e-5, max_iter: int = 100, f_noi
         lam, accepted = 1.0, False
         for _ in range(max_halvings):
             x1 = np.clip(x + lam * p, lo, hi)
-            f1, g1 = yield ("grad", x1)
+            if combined:
+                f1, g1, h1 = yield ("gh", x1)
+            else:
+                f1, g1 = yield ("grad", x1)
             n_eval += 1
             if np.isfinite(f1) and f1 <= f + f_noise * abs(f):
                 accepted = True
@@ -110,7 +120,9 @@ def newton_fit(theta0, limits, edm_tol: float = 2e-5, max_iter: int = 100, f_noi
             converged = bool(edm < 10.0 * edm_tol)
             break
         x, f, g = x1, f1, g1
-    if h is None or not converged:
+        if combined:
+            h = h1
+    if h is None or (not converged and not combined):
         h = yield ("hess", x)
         n_eval += 1
     try:
@@ -129,6 +141,8 @@ class ModelRuntime:
         self.model = model
         self.spec = load_spec(model)
         self.template = Likelihood(backend, self.spec, kernelT)
+        # F + gradient + Hessian in one launch where the model's combined kernel compiles
+        self.combined = self.template.combined_kernel()
         self.kernels = {k: b.kernel for k, b in self.template.blocks.items()}
         self.npar = len(self.spec["parameters"])
         self.limits = MODEL_LIMITS[model]
@@ -269,7 +283,7 @@ class FitServer:
                 waiting.pop(0)
                 data = rt.dataset(r.nevents, r.seed)
                 start = r.start if r.start is not None else np.array(rt.spec["truth"], dtype=np.float64)
-                co = newton_fit(start, rt.limits, f_noise=self.f_noise)
+                co = newton_fit(start, rt.limits, f_noise=self.f_noise, combined=rt.combined is not None)
                 a = _Active(r, data, need, co, co.send(None), time.perf_counter() - t0)
                 active.append(a)
                 used += need
@@ -283,7 +297,8 @@ class FitServer:
             groups: dict = {}
             for a in active:
                 kind, theta = a.pending
-                kern = "lh_hessian_kernel" if kind == "hess" else "lh_grad_kernel"
+                kern = {"hess": "lh_hessian_kernel", "grad": "lh_grad_kernel"}.get(kind) or \
+                    self.models[a.req.model].combined
                 groups.setdefault((a.req.model, kern), []).append((a, theta))
             for (model, kern), items in groups.items():
                 rt = self.models[model]
@@ -291,8 +306,14 @@ class FitServer:
                                    [th for _, th in items])
                 stats.batched_calls += 1
                 stats.evaluations += len(items)
+                npar = rt.npar
                 for (a, _), s in zip(items, sums):
-                    reply = self._hess(rt, s) if kern == "lh_hessian_kernel" else (-2.0 * s[0], -2.0 * s[1:])
+                    if kern == "lh_hessian_kernel":
+                        reply = self._hess(rt, s)
+                    elif kern == "lh_grad_kernel":
+                        reply = (-2.0 * s[0], -2.0 * s[1:])
+                    else:  # combined: F, gradient, then the Hessian's lower triangle
+                        reply = (-2.0 * s[0], -2.0 * s[1:1 + npar], self._hess(rt, s[1 + npar:]))
                     try:
                         a.pending = a.co.send(reply)
                     except StopIteration as stop:
