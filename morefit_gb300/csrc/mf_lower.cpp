@@ -1040,6 +1040,10 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
       // their accumulators stay in registers
       out.vec = (!out.pipelined && exprs.size() <= 16) ? 2 : 1;
     }
+    // FP32 Hessian-sized kernels: one event per thread as well (measured on
+    // GB300: K*mumu P-wave Hessian 12.1 vs 13.4 us at four events per thread,
+    // S+P-wave Hessian, 105 outputs, 58.7 vs 70.6 us per 1M events)
+    if (st32 && !out.pipelined && exprs.size() > 16) out.vec = 1;
     if (vec_req == 1 || vec_req == 2 || (vec_req == 4 && st32)) out.vec = vec_req;
     if (block_req >= 64 && block_req <= 1024 && block_req % 32 == 0) out.block = block_req;
     // bulk-copy pipeline: shared-memory stages; direct loads: loop unroll
