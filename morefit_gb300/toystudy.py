@@ -66,7 +66,10 @@ class SegmentLikelihood:
 
     def _submit(self, kernel: str, idx: np.ndarray, theta: np.ndarray) -> np.ndarray:
         self.evaluations += 1
-        return self.like.blocks[kernel].SubmitSegments(self.begins[idx], self.counts[idx], self._rows(kernel, theta))
+        parts = self.like.kernel_parts(kernel)
+        rows = self._rows(kernel, theta)
+        return np.concatenate([self.like.blocks[p].SubmitSegments(self.begins[idx], self.counts[idx], rows)
+                               for p in parts], axis=1)
 
     def value(self, idx, theta):
         return -2.0 * self._submit("lh_kernel", idx, theta)[:, 0]

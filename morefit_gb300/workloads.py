@@ -188,7 +188,48 @@ class Likelihood:
             return th.copy()
         return np.concatenate([th, self._exprs(kernel).eval(th)], axis=1)
 
+    HESSIAN_PART_OUTPUTS = 36  # the K*mumu P-wave Hessian's size, which keeps its accumulators in registers
+
+    def kernel_parts(self, kernel: str) -> list:
+        """Kernels whose outputs, concatenated, are ``kernel``'s: the kernel
+        itself, or for a Hessian kernel that spills more than
+        COMBINED_MAX_SPILL bytes of registers (the S+P wave's 105 outputs),
+        equal slices of its outputs of at most HESSIAN_PART_OUTPUTS each, one
+        kernel per slice, built on first use (each part repeats the per-event
+        work the slice needs but keeps its accumulators in registers, and
+        reads its own prepared copy of the dataset: worth it for a dataset
+        evaluated many times, not for the serving loop's one-fit datasets,
+        which keep the single kernel)."""
+        parts = self.__dict__.setdefault("_parts", {})
+        if kernel in parts:
+            return parts[kernel]
+        res = [kernel]
+        k, b = self.kspec.get(kernel), self.blocks.get(kernel)
+        if kernel == "lh_hessian_kernel" and b is not None and len(k["exprs"]) > self.HESSIAN_PART_OUTPUTS \
+                and b.kernel.info()["spill_bytes"] > self.COMBINED_MAX_SPILL:
+            exprs = k["exprs"]
+            m = -(-len(exprs) // self.HESSIAN_PART_OUTPUTS)
+            size = -(-len(exprs) // m)
+            defs = dict(self.buffers[kernel])
+            res = []
+            for i in range(m):
+                name = f"{kernel}_part{i}"
+                sub = exprs[i * size:(i + 1) * size]
+                nb = CUDABlock(self.backend, self.kernelT, **self._block_args)
+                nb.SetupInputBuffer(self.pre, not self.has_precompute)
+                nb.MakeComputeKernel(name, 0, k["inputs"], [f"r{j}" for j in range(len(sub))], k["params"], sub, True,
+                                     param_defs=[defs.get(p, "") for p in k["params"]])
+                nb.SetNevents(self.nevents)
+                self.buffers[name] = self.buffers[kernel]
+                self.blocks[name] = nb
+                res.append(name)
+        parts[kernel] = res
+        return res
+
     def sums(self, kernel: str, theta=None, param_vector=None) -> np.ndarray:
+        parts = self.kernel_parts(kernel)
+        if parts != [kernel]:
+            return np.concatenate([self.sums(p, theta, param_vector) for p in parts])
         if param_vector is None:
             calls = self.__dict__.setdefault("_sync_calls", {})
             call = calls.get(kernel)
@@ -206,6 +247,9 @@ class Likelihood:
         batched call (mf_kernel_reduce_many: consecutive evaluations overlap,
         one combine per chunk); each row equals ``sums(kernel, theta)`` bit
         for bit. Returns (npoints, noutputs)."""
+        parts = self.kernel_parts(kernel)
+        if parts != [kernel]:
+            return np.concatenate([self.sums_many(p, thetas) for p in parts], axis=1)
         b = self.blocks[kernel]
         k = b.kernel
         rows = np.ascontiguousarray(self.param_rows(kernel, thetas))

@@ -206,6 +206,35 @@ def test_combined_gradient_hessian_kernel(backend, workload):
     np.testing.assert_allclose(hs, sl.hessian(np.arange(2), th), rtol=1e-9, atol=1e-12 * np.abs(hs).max())
 
 
+@pytest.mark.parametrize("kernelT", [np.float64, np.float32])
+def test_hessian_split_in_parts(backend, kernelT):
+    """A Hessian kernel that spills (the S+P wave's 105 outputs) is evaluated
+    as parts of at most 36 outputs that do not spill; the concatenated sums
+    equal the single kernel's to 1e-12 (FP64) / 1e-6 (FP32) of the largest
+    element, single and batched, and the P-wave Hessian stays one kernel."""
+    from morefit_gb300.workloads import Likelihood
+    g = load_golden("spwave_n2000.json")
+    like = Likelihood(backend, g, kernelT)
+    like.set_data(golden_events("spwave", 2000))
+    parts = like.kernel_parts("lh_hessian_kernel")
+    assert len(parts) == 3
+    assert all(like.blocks[p].kernel.info()["spill_bytes"] == 0 for p in parts)
+    tol = 1e-12 if kernelT == np.float64 else 1e-6
+    b = like.blocks["lh_hessian_kernel"]
+    for pt in g["points"]:
+        pv = like.param_vector("lh_hessian_kernel", pt["params"])
+        b.CopyToParameterBuffer(pv)
+        b.SubmitKernel()
+        whole = b.CopyFromKahanBuffer()
+        split = like.sums("lh_hessian_kernel", pt["params"])
+        assert split.shape == whole.shape
+        assert np.all(np.abs(split - whole) <= tol * np.abs(whole).max())
+        many = like.sums_many("lh_hessian_kernel", np.array([pt["params"]] * 2))
+        assert np.array_equal(many[0], split) and np.array_equal(many[1], split)
+    pw = Likelihood(backend, load_golden("pwave_n1000.json"), kernelT)
+    assert pw.kernel_parts("lh_hessian_kernel") == ["lh_hessian_kernel"]
+
+
 @pytest.mark.parametrize("workload", ["pwave", "mass", "mass_w"])
 def test_sync_evaluation_equals_parameter_vector_path(backend, workload):
     """sums(kernel, theta), whose hoisted parameter buffers are evaluated in
