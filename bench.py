@@ -27,6 +27,7 @@ import datetime
 import json
 import math
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -160,46 +161,97 @@ def replica_value(ms: float, steps: int):
     return ms, world * steps / (ms / 1e3)
 
 
+def bench_config(n: int) -> dict:
+    """The workload both arms name (identical dicts): the K*mumu P-wave events
+    of dataset 0 (seed 229387429, the reference's accelerator partition of
+    8192 generator streams) and the GPU arm's L2 policy."""
+    nsets = rotation_sets(n)
+    return {"workload": "K*mumu P-wave angular fit, 8 free parameters, 1M events, FP64",
+            "nevents": n, "events": "seeded accept-reject, seed 229387429, accelerator partition (8192 streams)",
+            "l2": f"GPU arm: {nsets} datasets x {n * 72 / 1e6:.0f} MB read in rotation (> 2x L2), no flush",
+            "parallelism": "single device"}
+
+
+def rotation_sets(n: int) -> int:
+    """Independent 1M-event datasets the device arm rotates over so that the
+    bytes read between two reads of one set exceed twice the L2."""
+    return max(2, math.ceil(2 * L2_BYTES / (n * 11 * 8)) + 1)
+
+
+def _refkit():
+    p = ROOT / "oracle" / "_ref" / platform.machine() / "refkit"
+    return p if p.exists() else None
+
+
+def cpu_reference_rate(events: np.ndarray, nthreads: int, max_evals: int, seconds: float) -> dict:
+    """NLL + gradient evaluations per second of the reference's CPU path over
+    `events` (3 x n P-wave events) at the truth, on `nthreads` host threads:
+    the reference's own fitter::likelihood_and_gradient over its CPU backend's
+    loop (oracle/_ref/<arch>/refkit benchevents: the reference compiled from
+    its sources, its kernel text compiled by gcc), "kind": "reference"; where
+    the kit is not built, the reference's lh_grad kernel text in the oracle's
+    restatement of that loop (oracle/spec_kernel.py), "kind": "port".
+    At most max_evals evaluations or `seconds` of them, after 3 untimed ones."""
+    import tempfile
+    kit = _refkit()
+    if kit is not None:
+        with tempfile.TemporaryDirectory() as td:
+            path = Path(td) / "events.f64"
+            np.ascontiguousarray(events, dtype=np.float64).tofile(path)
+            r = subprocess.run([str(kit), "benchevents", "pwave", str(path), str(nthreads), str(max_evals),
+                                str(seconds)], capture_output=True, text=True, check=True)
+        d = json.loads(r.stdout.strip().splitlines()[-1])
+        return {"value": d["evals_per_s"], "nthreads": nthreads, "nevals": d["nevals"], "seconds": d["seconds"],
+                "nll": d["nll"], "kind": "reference",
+                "how": "the reference's fitter::likelihood_and_gradient over its CPU backend loop (kernel text "
+                       "compiled by gcc -O3), oracle/_ref refkit benchevents"}
+    from oracle.spec_kernel import SpecKernel
+    g = json.loads((ROOT / "tests" / "golden" / "pwave_n1000000.json").read_text())
+    ks = {k["name"]: k for k in g["kernels"]}
+    cols = SpecKernel(ks["precompute_kernel"]).store(events, [])
+    grad = SpecKernel(ks["lh_grad_kernel"])
+    pv = np.array(g["points"][0]["kernel_params"]["lh_grad_kernel"])  # the truth
+    for _ in range(3):
+        grad.reduce(cols, pv, nthreads)
+    t0 = time.perf_counter()
+    done = 0
+    while done < max_evals and (done == 0 or time.perf_counter() - t0 < seconds):
+        s = grad.reduce(cols, pv, nthreads)
+        done += 1
+    dt = time.perf_counter() - t0
+    return {"value": done / dt, "nthreads": nthreads, "nevals": done, "seconds": dt, "nll": float(-2.0 * s[0]),
+            "kind": "port", "how": "the reference's lh_grad kernel text compiled by gcc -O3 in the oracle's "
+                                   "restatement of its CPU backend loop (oracle/spec_kernel.py)"}
+
+
 def reference_arm(args):
-    """The reference's CPU path: its kernel text through the CPU backend's loop, all host threads."""
+    """The reference's CPU path on the events of the device arm's dataset 0,
+    all host threads (the line's value) and one thread (every reference
+    driver's setting, benchmarking/morefit_kstarmumu.cc:27) beside it."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
     from oracle import mforacle
-    from oracle.spec_kernel import SpecKernel
-    from morefit_gb300.workloads import load_spec
-    spec = load_spec("pwave")
-    ks = {k["name"]: k for k in spec["kernels"]}
     n = args.nevents
-    ev = mforacle.generate("pwave", n)
-    cols = SpecKernel(ks["precompute_kernel"]).store(ev, [])
-    grad = SpecKernel(ks["lh_grad_kernel"])
-    from morefit_gb300.backend import eval_expressions
-    truth = np.array(spec["truth"])
-    pv = np.concatenate([truth, eval_expressions(spec["parameters"], truth, [e for _, e in spec["grad_buffers"]])])
-    nthreads = os.cpu_count() or 1
-    for _ in range(min(args.warmup, 3)):
-        grad.reduce(cols, pv, nthreads)
-    # Bounded sample: K evaluations or --cpu-seconds of them, whichever ends first.
-    t0 = time.perf_counter()
-    done = 0
-    while done < args.steps and (done == 0 or time.perf_counter() - t0 < args.cpu_seconds):
-        s = grad.reduce(cols, pv, nthreads)
-        done += 1
-    dt = time.perf_counter() - t0
-    v = done / dt
+    nper, nseeds = mforacle.accelerator_partition(n)
+    ev = mforacle.generate_partitioned("pwave", n, nper, nseeds)
+    h = mforacle.fnv1a(ev)
+    cores = os.cpu_count() or 1
+    allc = cpu_reference_rate(ev, cores, args.steps, args.cpu_seconds)
+    one = cpu_reference_rate(ev, 1, args.steps, args.cpu_seconds)
+    v = allc["value"]
     line = {"metric": METRIC, "value": v, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
-            "steps_timed": done, "warmup": args.warmup, "ms_per_step": 1e3 * dt / done, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded accept-reject)",
-            "impl": "reference",
-            "config": {"workload": "K*mumu P-wave angular fit, 8 parameters, 1M events, FP64",
-                       "nevents": n, "inputs": "host memory"},
-            "cpu_baseline": {"value": v, "unit": "evals/s", "cores": nthreads, "kind": "port",
-                             "sample": f"{done} NLL+grad evaluations over all {n} events (at most K or "
-                                       f"{args.cpu_seconds:.0f} s); the reference's "
-                                       "lh_grad kernel text compiled by gcc -O3, Kahan-summed per thread chunk"},
-            "e2e": {"value": v, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "nll_check": float(-2.0 * s[0])}
+            "steps_timed": allc["nevals"], "warmup": args.warmup, "ms_per_step": 1e3 / v,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic: seeded accept-reject K*mumu P-wave events (the device arm's dataset 0)",
+            "impl": "reference", "config": bench_config(n),
+            "cpu_baseline": {"value": v, "unit": "evals/s", "cores": cores, "kind": allc["kind"],
+                             "sample": f"{allc['nevals']} NLL+grad evaluations over all {n} events (at most K or "
+                                       f"{args.cpu_seconds:g} s); {allc['how']}"},
+            "nthreads_1": {"value": one["value"], "unit": "evals/s", "cores": 1, "nevals": one["nevals"],
+                           "nll": one["nll"]},
+            "events_fnv1a": h, "nll": allc["nll"],
+            "e2e": {"value": v, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
@@ -220,15 +272,13 @@ def ours(args):
     truth = np.array(spec["truth"])
     n = args.nevents
     ks = {k["name"]: k for k in spec["kernels"]}
-    ncols_read = 11  # morefit_eventbuffer_3..13, the source columns of the lh_grad kernel (sizes the rotation)
 
     def make_sets(kernelT, native=False):
-        """Rotating datasets totalling more than 2x L2 of what the NLL+grad kernel reads.
-        Returns the sets, the kernel's algorithmic bytes per launch (columns it reads x
-        n x element bytes) and the number of sets."""
-        itemsize = np.dtype(kernelT).itemsize
-        per_set = n * ncols_read * itemsize
-        nsets = max(2, math.ceil(2 * L2_BYTES / per_set) + 1)
+        """Rotating datasets totalling more than 2x L2 of what the NLL+grad kernel reads
+        (dataset r: seed 229387429 + 1000 rank + r). Returns the sets, the kernel's
+        algorithmic bytes per launch (columns it reads x n x element bytes) and the
+        number of sets."""
+        nsets = rotation_sets(n) if kernelT == np.float64 else max(2, math.ceil(2 * L2_BYTES / (n * 11 * 4)) + 1)
         sets = []
         for r in range(nsets):
             like = Likelihood(backend, spec, kernelT, native_f64=native)
@@ -242,27 +292,37 @@ def ours(args):
     ext = torch.cuda.ExternalStream(stream_ptr, device=torch.device("cuda", local))
 
     def timed_device(sets, K, W, clk=None):
-        """K NLL+grad launches rotating over the datasets, enqueued back to back; CUDA events on the stream."""
+        """K NLL+grad evaluations rotating over the datasets through one
+        mf_kernel_reduce_many call (the batched entry: parameter-only values
+        evaluated per evaluation, launches enqueued back to back), bracketed by
+        CUDA events on the library's stream. The call's argument arrays (input
+        handles, strides, sizes, one parameter row per evaluation) are built
+        before the first event; everything the library does is inside."""
         import ctypes as C
         pv = sets[0].param_vector("lh_grad_kernel", truth)
         kern = sets[0].blocks["lh_grad_kernel"].kernel
         out_buf = L.c_buf()
         L.check(L.lib.mf_buffer_alloc(backend.handle, max(K, W, len(sets), 1) * kern.nout * 8, C.byref(out_buf)))
+        u64p = C.POINTER(C.c_uint64)
 
-        def enqueue(count):
+        def request(count):
             ins = (L.c_buf * count)(*[sets[i % len(sets)].blocks["lh_grad_kernel"].input.buf for i in range(count)])
             strides = np.array([sets[i % len(sets)].blocks["lh_grad_kernel"].input.stride for i in range(count)],
                                dtype=np.uint64)
             ns = np.full(count, n, dtype=np.uint64)
             rows = np.ascontiguousarray(np.tile(pv, (count, 1)))
-            u64p = C.POINTER(C.c_uint64)
+            return (count, ins, strides, ns, rows)
+
+        def enqueue(req):
+            count, ins, strides, ns, rows = req
             L.check(L.lib.mf_kernel_reduce_many(kern.handle, count, ins, strides.ctypes.data_as(u64p),
                                                 ns.ctypes.data_as(u64p), L.dptr(rows), len(pv), out_buf))
 
         # one untimed launch per dataset first: each makes the dataset's
         # prepared columns (folded, pre-split) that the kernel reads
-        enqueue(len(sets))
-        enqueue(W)
+        enqueue(request(len(sets)))
+        enqueue(request(W))
+        timed = request(K)
         backend.synchronize()
         if world > 1:
             torch.distributed.barrier()
@@ -272,7 +332,7 @@ def ours(args):
         if clk is not None:
             clk.mark_start()
         e0.record(ext)
-        enqueue(K)
+        enqueue(timed)
         e1.record(ext)
         e1.synchronize()
         if clk is not None:
@@ -504,18 +564,11 @@ def ours(args):
     # ---------------- CPU baseline (rank 0, N=1 only) ----------------
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
+        from oracle import mforacle
         from oracle.spec_kernel import SpecKernel
-        cols = SpecKernel(ks["precompute_kernel"]).store(host, [])
-        gk = SpecKernel(ks["lh_grad_kernel"])
-        pvh = sets64[0].param_vector("lh_grad_kernel", truth)
         nthreads = os.cpu_count() or 1
-        gk.reduce(cols, pvh, nthreads)
-        t0 = time.perf_counter()
-        nev = 0
-        while time.perf_counter() - t0 < args.cpu_seconds:
-            s_cpu = gk.reduce(cols, pvh, nthreads)
-            nev += 1
-        cpu_s = (time.perf_counter() - t0) / nev
+        allc = cpu_reference_rate(host, nthreads, 1 << 30, args.cpu_seconds)
+        one = cpu_reference_rate(host, 1, 1 << 30, args.cpu_seconds / 2)
         # configuration C1: the reference's mass lh_grad kernel text on 100k events, all host threads
         mspec = load_spec("mass")
         mk = {k["name"]: k for k in mspec["kernels"]}
@@ -529,53 +582,67 @@ def ours(args):
         while time.perf_counter() - t0 < 3.0:
             mgk.reduce(mev, mpv, nthreads)
             mdone += 1
-        c1_cpu = {"value": mdone / (time.perf_counter() - t0), "unit": "evals/s", "cores": nthreads,
+        c1_cpu = {"value": mdone / (time.perf_counter() - t0), "unit": "evals/s", "cores": nthreads, "kind": "port",
                   "sample": f"{mdone} NLL+grad evaluations of the mass model over 100k events (~3 s)"}
-        cpu = {"value": 1.0 / cpu_s, "unit": "evals/s", "cores": nthreads, "kind": "port", "c1_mass_100k": c1_cpu,
-               "sample": f"{nev} NLL+grad evaluations over all {n} events of dataset 0 "
-                         f"(~{args.cpu_seconds:.0f} s); the reference's lh_grad kernel text compiled by gcc -O3",
-               "nll_rel_diff_vs_gpu": abs(s_cpu[0] - float(like.sums('lh_grad_kernel', truth)[0])) / abs(s_cpu[0])}
+        nll_gpu = -2.0 * float(like.sums("lh_grad_kernel", truth)[0])
+        cpu = {"value": allc["value"], "unit": "evals/s", "cores": nthreads, "kind": allc["kind"],
+               "sample": f"{allc['nevals']} NLL+grad evaluations over all {n} events of dataset 0 "
+                         f"(~{args.cpu_seconds:g} s); {allc['how']}",
+               "nthreads_1": {"value": one["value"], "unit": "evals/s", "cores": 1, "nevals": one["nevals"]},
+               "events_fnv1a": mforacle.fnv1a(host),
+               "nll_rel_diff_vs_gpu": abs(allc["nll"] - nll_gpu) / abs(nll_gpu), "c1_mass_100k": c1_cpu}
 
     if rank == 0:
+        r3 = lambda x: None if x is None else float(f"{x:.4g}")
+        # the targets' figures, last in the line so that a tail of the output shows them
+        headline = {
+            "fp64_evals_per_s": r3(value), "fp64_hbm_frac": r3(achieved / hbm_peak),
+            "fp64_us_per_eval": r3(1e3 * ms64 / args.steps),
+            "mixed_evals_per_s": r3(mixed["value"]) if mixed else None,
+            "mixed_over_fp64": r3(mixed["speedup_vs_f64"]) if mixed else None,
+            "mixed_nll_rel_diff": r3(mixed["nll_rel_diff_vs_f64"]) if mixed else None,
+            "native_fp64_evals_per_s": r3(native["value"]) if native else None,
+            "spwave_10M_mixed_evals_per_s": r3(spw["value"]) if spw else None,
+            "spwave_10M_mixed_over_fp64": r3(spw["speedup_vs_f64"]) if spw else None,
+            "spwave_10M_shift_sigma": r3(spw["max_param_shift_sigma_vs_f64"]) if spw else None,
+            "toys_fits_per_s": r3(toys["value"]) if toys else None,
+            "toys_fit_only_over_serial": r3(toys["batched_over_serial"]) if toys else None,
+            "serving_fits_per_s": r3(serving["value"]) if serving else None,
+            "serving_p50_ms": r3(serving["p50_ms"]) if serving else None,
+            "serving_p99_ms": r3(serving["p99_ms"]) if serving else None,
+            "serving_capacity_over_serial": r3(serving["capacity_over_serial"]) if serving else None,
+            "e2e_evals_per_s": r3(world / e2e_s), "fit_loop_evals_per_s": r3(world / fit_loop_s),
+            "cpu_reference_evals_per_s": r3(cpu["value"]) if cpu else None,
+            "cpu_reference_1thread_evals_per_s": r3(cpu["nthreads_1"]["value"]) if cpu else None}
         line = {"metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms64 / args.steps, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-                "arithmetic": "FP64 storage and sums; per-event math in double-float (FP32 pairs, ~48-bit) -- "
-                              "NLL within 1e-10 rel of native FP64; native FP64 timed in native_fp64",
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64 (double-float arithmetic, 48-bit)",
                 "data": "synthetic: seeded accept-reject K*mumu P-wave events generated on the GPU",
-                "config": {"workload": "K*mumu P-wave angular fit, 8 free parameters, 1M events, FP64 (configs[1])",
-                           "nevents": n, "datasets_rotated": nsets64,
-                           "l2": f"{nsets64} x {bytes64 / 1e6:.0f} MB read in rotation (> 2x L2), no flush",
-                           "parallelism": "replicas" if world > 1 else "single GPU"},
+                "config": bench_config(n),
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                              "frac": achieved / hbm_peak, "traffic": NCU_TRAFFIC_F64,
-                             "traffic_source": NCU_TRAFFIC_SOURCE,
-                             "peak_source": peak_kind,
+                             "traffic_source": NCU_TRAFFIC_SOURCE, "peak_source": peak_kind,
                              "algorithmic_bytes_per_launch": bytes64},
                 "e2e": {"value": world / e2e_s, "unit": "evals/s",
                         "h2d_bytes_per_step": int(host.nbytes), "d2h_bytes_per_step": nout * 8,
-                        "what": "per step: upload raw events from page-locked host memory, precompute, prepare, "
-                                f"NLL+grad, read sums to host; steps pipelined over {E2E_LANES} contexts (the "
-                                "24 MB upload at 207 GB/s bounds a step at ~116 us)",
+                        "what": "per step: raw events uploaded from page-locked host memory, precompute, prepare, "
+                                f"NLL+grad, sums read to host; steps pipelined over {E2E_LANES} contexts",
                         "nll_rel_diff_vs_device": e2e_rel},
-                "e2e_mapped": {"value": world / e2e_mapped_s, "unit": "evals/s",
-                               "h2d_bytes_per_step": int(host.nbytes), "d2h_bytes_per_step": nout * 8,
-                               "what": "the same steps, the precompute kernel reading the raw events in place from "
-                                       "page-locked host memory (mf_buffer_wrap_host) instead of a copy to HBM",
-                               "nll_rel_diff_vs_device": e2e_mapped_rel},
-                "e2e_sequential": {"value": world / seq_s, "unit": "evals/s",
-                                   "h2d_bytes_per_step": int(host.nbytes), "d2h_bytes_per_step": nout * 8,
-                                   "what": "the same step, one at a time, each waiting for its result"},
-                "e2e_fit_loop": {"value": world / fit_loop_s, "unit": "evals/s", "h2d_bytes_per_step": 0,
-                                 "d2h_bytes_per_step": nout * 8,
-                                 "what": "events resident; parameters in, sums out (the fitter's per-evaluation path)"},
-                "native_fp64": native, "mixed": mixed, "spwave_10M": spw, "toys": toys, "serving": serving,
-                "extras": extras,
                 "cpu_baseline": cpu,
                 "clocks": clk.summary(),
                 # K per-evaluation launches plus one combine per COMBINE_CHUNK
                 "gpu_launches": args.steps + math.ceil(args.steps / COMBINE_CHUNK),
-                "nll_truth": float(-2.0 * res64[0])}
+                "nll_truth": float(-2.0 * res64[0]),
+                "e2e_mapped": {"value": world / e2e_mapped_s, "unit": "evals/s",
+                               "h2d_bytes_per_step": int(host.nbytes), "d2h_bytes_per_step": nout * 8,
+                               "nll_rel_diff_vs_device": e2e_mapped_rel},
+                "e2e_sequential": {"value": world / seq_s, "unit": "evals/s",
+                                   "h2d_bytes_per_step": int(host.nbytes), "d2h_bytes_per_step": nout * 8},
+                "e2e_fit_loop": {"value": world / fit_loop_s, "unit": "evals/s", "h2d_bytes_per_step": 0,
+                                 "d2h_bytes_per_step": nout * 8},
+                "native_fp64": native, "mixed": mixed, "spwave_10M": spw, "toys": toys, "serving": serving,
+                "extras": extras,
+                "headline": headline}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

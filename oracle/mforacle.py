@@ -82,6 +82,18 @@ def generate(workload: str, n: int, truth=None, seed: int = SEED, nthreads: int 
     return out
 
 
+def accelerator_partition(n: int, max_workitems: int = 8192):
+    """(events per generator thread, generator threads) of the reference's
+    accelerator generator for n events and compute_options::
+    opencl_max_generator_workitems = max_workitems (compute_opencl.hh:437-445:
+    nper = n / max + 1 when n exceeds max, else 1; thread t owns events
+    [t * nper, (t + 1) * nper), so n / nper + 1 threads cover them)."""
+    if max_workitems > 0 and n > max_workitems:
+        nper = n // max_workitems + 1
+        return nper, n // nper + 1
+    return 1, max(n, 1)
+
+
 def generate_partitioned(workload: str, n: int, nper: int, nseeds: int, truth=None, seed: int = SEED) -> np.ndarray:
     """Events with the accelerator partition: seed row t owns [t*nper, (t+1)*nper)."""
     w = 0 if workload == "mass" else 1

@@ -1,5 +1,8 @@
 """Shared fixtures. GPU tests carry @pytest.mark.gpu; everything else runs on CPU."""
 import json
+import os
+import platform
+import subprocess
 import sys
 from pathlib import Path
 
@@ -11,6 +14,28 @@ if str(ROOT) not in sys.path:
     sys.path.insert(0, str(ROOT))
 
 GOLDEN = ROOT / "tests" / "golden"
+ARCH = platform.machine()
+
+
+def reference_sources():
+    """The reference sources the C++ drop-in compiles against: the tree named by
+    MOREFIT_REFERENCE, else the copy staged by `make -C oracle stage` (which
+    travels with the working tree to hosts that have no reference tree), else None."""
+    env = os.environ.get("MOREFIT_REFERENCE")
+    if env and (Path(env) / "include" / "fitter.hh").exists():
+        return Path(env)
+    staged = ROOT / "oracle" / "_ref" / "src"
+    return staged if (staged / "include" / "fitter.hh").exists() else None
+
+
+def build_dropin() -> Path:
+    """Builds Minuit2, the oracle kit and tests/cpp/_build/<arch>/dropin from the reference sources."""
+    from morefit_gb300.build import build_library
+    build_library()
+    jobs = f"-j{os.cpu_count() or 4}"
+    subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), "ref", jobs], check=True)
+    subprocess.run(["make", "-s", "-C", str(ROOT / "tests" / "cpp"), jobs], check=True)
+    return ROOT / "tests" / "cpp" / "_build" / ARCH / "dropin"
 
 
 def pytest_configure(config):

@@ -1,22 +1,38 @@
 // Drop-in check of include/compute_cuda.hh against the reference's unchanged
-// fitter, generator and toystudy (compiled with the reference headers where
-// they lie; built by tests/cpp/Makefile).
+// fitter, generator and Minuit2 (compiled from the reference sources by
+// tests/cpp/Makefile; workloads from oracle/refkit/workloads.hh, the same
+// models, parameters and fitter options as the golden vectors).
 //
-//   dropin lower <mass|pwave>   print the CUDA C the backend generates for every
-//                               kernel the reference's fitter requests (works
-//                               without a GPU: print_kernel output of the blocks)
-//   dropin fit <mass|pwave> <n> generate n events on the GPU with the reference's
-//                               generator and fit them with its fitter + Minuit2
-//                               (needs a GB300)
+//   dropin lower <workload>                print the CUDA C the backend generates
+//                                          for every kernel the reference's
+//                                          fitter requests (no GPU needed)
+//   dropin fit <workload> <events.f64> [f32]
+//                                          fit the events of a raw SoA file
+//                                          (ndims x n doubles) with the
+//                                          reference's fitter + Minuit2 MIGRAD
+//                                          and HESSE over CUDABlock<double> (or
+//                                          CUDABlock<float> with f32); prints
+//                                          one JSON line
+//   dropin genfit <workload> <n> [f32]     generate n events on the GPU with the
+//                                          reference's generator (accelerator
+//                                          partition, seed 229387429), then fit
+//   dropin threads <workload> <nthreads> <events.f64> [f32]
+//                                          nthreads host threads, each with its
+//                                          own fitter and CUDABlocks fitting its
+//                                          own copy of the events, at once
 #define MOREFIT_H 1
+#include <atomic>
 #include <cassert>
 #include <chrono>
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <functional>
 #include <iostream>
 #include <sstream>
 #include <string>
+#include <thread>
+#include <vector>
 
 #include "graph.hh"
 #include "eventvector.hh"
@@ -36,86 +52,255 @@ class LLVMBackend : public ComputeBackend {
 };
 }  // namespace morefit
 #include "generator.hh"
-#include "toystudy.hh"
+#include "workloads.hh"
 
 using namespace morefit;
 
+static uint64_t fnv1a(const void* p, size_t n) {
+  const unsigned char* b = (const unsigned char*)p;
+  uint64_t h = 1469598103934665603ULL;
+  for (size_t i = 0; i < n; i++) {
+    h ^= b[i];
+    h *= 1099511628211ULL;
+  }
+  return h;
+}
+
+static std::vector<double> read_events(const std::string& path, size_t ndims, unsigned& n) {
+  FILE* f = std::fopen(path.c_str(), "rb");
+  if (!f) {
+    std::fprintf(stderr, "cannot open %s\n", path.c_str());
+    std::exit(2);
+  }
+  std::fseek(f, 0, SEEK_END);
+  const long bytes = std::ftell(f);
+  std::fseek(f, 0, SEEK_SET);
+  n = unsigned(size_t(bytes) / (8 * ndims));
+  std::vector<double> v(ndims * size_t(n));
+  if (std::fread(v.data(), 8, v.size(), f) != v.size()) {
+    std::fprintf(stderr, "short read of %s\n", path.c_str());
+    std::exit(2);
+  }
+  std::fclose(f);
+  return v;
+}
+
+static std::string jvec(const std::vector<double>& v) {
+  std::string o = "[";
+  char b[64];
+  for (size_t i = 0; i < v.size(); i++) {
+    std::snprintf(b, sizeof b, "%s%.17g", i ? "," : "", v[i]);
+    o += b;
+  }
+  return o + "]";
+}
+
+// "Hesse returns <status>" is the fitter's report of Minuit2's covariance status (fitter.hh:819-823).
+static int cov_status_of(const std::string& log) {
+  const std::string key = "Hesse returns ";
+  size_t p = log.rfind(key);
+  return p == std::string::npos ? -1 : std::atoi(log.c_str() + p + key.size());
+}
+
+struct FitResult {
+  std::vector<double> values, errors;
+  double first_ms = 0, warm_ms = 0;
+  int cov_status = -1;
+  bool ok = false;
+};
+
+// Discards what is written to it; no state, so several threads may write at once.
+struct NullBuf : std::streambuf {
+  int overflow(int c) override { return c; }
+};
+
+// One fit of `ev` (ndims x n doubles) with the reference's fitter over
+// CUDABlock<kT>: first from the start values (this builds the kernels), then
+// once more from the same start values with the kernels kept (refit), timed.
+// With capture, the fitter's std::cout output is read for Minuit2's
+// covariance status (one thread only; threads mode discards the output).
 template <typename kT>
-static int run(const std::string& mode, const std::string& which, unsigned n) {
+static FitResult fit_events(CUDABackend& backend, const std::string& which, const std::vector<double>& ev, unsigned n,
+                            bool capture = true) {
+  typedef double eT;
+  Workload<kT, eT> w = make_workload<kT, eT>(which);
+  const size_t nd = w.dims.size();
+  EventVector<kT, eT> data(w.dims, n);
+  for (size_t d = 0; d < nd; d++)
+    for (unsigned i = 0; i < n; i++) data(i, d) = kT(ev[d * n + i]);
+  std::vector<double> start;
+  for (auto* p : w.params) start.push_back(p->get_value());
+  fitter_options fo = make_fit_opts(w);
+  fitter<kT, eT, CUDABackend, CUDABlock<kT, eT>> fit(&fo, &backend);
+  FitResult r;
+  std::ostringstream log;
+  std::streambuf* old = capture ? std::cout.rdbuf(log.rdbuf()) : nullptr;
+  auto t0 = std::chrono::steady_clock::now();
+  r.ok = fit.fit(w.pdf, w.params, &data);
+  auto t1 = std::chrono::steady_clock::now();
+  if (capture) r.cov_status = cov_status_of(log.str());
+  for (auto* p : w.params) {
+    r.values.push_back(p->get_value());
+    r.errors.push_back(p->get_error());
+  }
+  for (size_t i = 0; i < start.size(); i++) {
+    w.params[i]->set_value(start[i]);
+    w.params[i]->set_start_value(start[i]);
+  }
+  auto t2 = std::chrono::steady_clock::now();
+  fit.fit(w.pdf, w.params, &data, true);
+  auto t3 = std::chrono::steady_clock::now();
+  if (capture) std::cout.rdbuf(old);
+  r.first_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+  r.warm_ms = std::chrono::duration<double, std::milli>(t3 - t2).count();
+  return r;
+}
+
+static void print_fit(const std::string& which, unsigned n, const char* prec, uint64_t hash, const FitResult& r,
+                      const char* extra = "") {
+  std::printf("{\"workload\":\"%s\",\"n\":%u,\"kernelT\":\"%s\",\"events_fnv1a\":\"%016llx\",\"ok\":%s,"
+              "\"cov_status\":%d,\"first_fit_ms\":%.3f,\"fit_ms\":%.3f,\"values\":%s,\"errors\":%s%s}\n",
+              which.c_str(), n, prec, (unsigned long long)hash, r.ok ? "true" : "false", r.cov_status, r.first_ms,
+              r.warm_ms, jvec(r.values).c_str(), jvec(r.errors).c_str(), extra);
+}
+
+template <typename kT>
+static int cmd_lower(const std::string& which) {
   typedef double eT;
   compute_options copts;
-  copts.print_kernel = (mode == "lower");
+  copts.print_kernel = true;
   cuda_options cu;
-  cu.quiet = (mode == "lower");
+  cu.quiet = true;
   CUDABackend backend(&copts, cu);
-  std::vector<dimension<eT>*> dims;
-  std::vector<parameter<eT>*> params;
-  PDF<kT, eT>* pdf = nullptr;
-  fitter_options fo;
-  fo.minuit_printlevel = 0;
-  fo.print_level = 0;
-  if (which == "mass") {
-    auto* m = new dimension<eT>("m", "m", 5000.0, 5600.0, false);
-    auto* mb = new parameter<eT>("mb", "mb", 5280.0, 5200.0, 5400.0, 1.0, false);
-    auto* sigma = new parameter<eT>("sigma", "sigma", 20.0, 5.0, 50.0, 0.5, false);
-    auto* fsig = new parameter<eT>("fsig", "fsig", 0.3, 0.0, 1.0, 0.01, false);
-    auto* alpha = new parameter<eT>("alpha", "alpha", -0.002, -0.01, 0.01, 0.0001, false);
-    pdf = new SumPDF<kT, eT>(new GaussianPDF<kT, eT>(m, mb, sigma), new ExponentialPDF<kT, eT>(m, alpha), fsig);
-    dims = {m};
-    params = {mb, sigma, fsig, alpha};
-    fo.optimize_dimensions = false;
-  } else {
-    auto* ctl = new dimension<eT>("ctl", "ctl", -1.0, 1.0, false);
-    auto* ctk = new dimension<eT>("ctk", "ctk", -1.0, 1.0, false);
-    auto* phi = new dimension<eT>("phi", "phi", -M_PI, +M_PI, false);
-    const char* names[8] = {"Fl", "S3", "S4", "S5", "Afb", "S7", "S8", "S9"};
-    const double truth[8] = {0.70, -0.01, -0.15, -0.20, -0.10, 0.0, 0.0, 0.0};
-    for (int i = 0; i < 8; i++)
-      params.push_back(new parameter<eT>(names[i], names[i], truth[i], i == 0 ? 0.0 : -1.0, 1.0, 0.01, false));
-    pdf = new KstarmumuAngularPDF<kT, eT>(ctl, ctk, phi, params[0], params[1], params[2], params[3], params[4],
-                                           params[5], params[6], params[7]);
-    dims = {ctl, ctk, phi};
-    fo.optimize_dimensions = true;
-  }
-  if (mode == "lower") {
-    // make_kernels only reads the dimensions and event count of the data.
-    EventVector<kT, eT> data(dims, 16);
-    for (unsigned i = 0; i < 16 * dims.size(); i++) data.get_data()[i] = 0.5;
-    fitter<kT, eT, CUDABackend, CUDABlock<kT, eT>> fit(&fo, &backend);
-    fit.make_kernels(pdf, params, &data);
-    return 0;
-  }
-  if (!backend.ok()) {
-    std::printf("{\"skipped\":\"%s\"}\n", backend.error().c_str());
-    return 0;
-  }
-  Xoshiro128pp rnd;
-  rnd.setSeed(int64_t(229387429));
-  generator_options go;
-  go.print_level = 0;
-  generator<kT, eT, CUDABackend, CUDABlock<kT, eT>> gen(&go, &backend, &rnd);
-  EventVector<kT, eT> data(dims);
-  gen.generate(n, pdf, params, data);
+  Workload<kT, eT> w = make_workload<kT, eT>(which);
+  // make_kernels only reads the dimensions and event count of the data.
+  EventVector<kT, eT> data(w.dims, 16);
+  for (unsigned i = 0; i < 16 * w.dims.size(); i++) data.get_data()[i] = 0.5;
+  fitter_options fo = make_fit_opts(w);
   fitter<kT, eT, CUDABackend, CUDABlock<kT, eT>> fit(&fo, &backend);
-  auto t0 = std::chrono::steady_clock::now();
-  fit.fit(pdf, params, &data);
-  auto t1 = std::chrono::steady_clock::now();
-  std::printf("{\"workload\":\"%s\",\"n\":%u,\"fit_ms\":%.3f,\"values\":[", which.c_str(), n,
-              std::chrono::duration<double, std::milli>(t1 - t0).count());
-  for (size_t i = 0; i < params.size(); i++) std::printf("%s%.17g", i ? "," : "", params[i]->get_value());
-  std::printf("],\"errors\":[");
-  for (size_t i = 0; i < params.size(); i++) std::printf("%s%.17g", i ? "," : "", params[i]->get_error());
-  std::printf("]}\n");
+  fit.make_kernels(w.pdf, w.params, &data);
   return 0;
 }
 
+template <typename kT>
+static int cmd_fit(const std::string& which, const std::string& path, const char* prec) {
+  compute_options copts;
+  CUDABackend backend(&copts);
+  if (!backend.ok()) {
+    std::printf("{\"skipped\":\"%s\"}\n", backend.error().c_str());
+    return 3;
+  }
+  Workload<double, double> w0 = make_workload<double, double>(which);
+  unsigned n = 0;
+  std::vector<double> ev = read_events(path, w0.dims.size(), n);
+  const uint64_t h = fnv1a(ev.data(), ev.size() * sizeof(double));
+  FitResult r = fit_events<kT>(backend, which, ev, n);
+  print_fit(which, n, prec, h, r);
+  return r.ok ? 0 : 1;
+}
+
+template <typename kT>
+static int cmd_genfit(const std::string& which, unsigned n, const char* prec) {
+  typedef double eT;
+  compute_options copts;
+  CUDABackend backend(&copts);
+  if (!backend.ok()) {
+    std::printf("{\"skipped\":\"%s\"}\n", backend.error().c_str());
+    return 3;
+  }
+  // the reference's generator over CUDABlock: accelerator partition over
+  // compute_options::opencl_max_generator_workitems threads (generator.hh:102-175)
+  Workload<kT, eT> w = make_workload<kT, eT>(which);
+  Xoshiro128pp rnd;
+  rnd.setSeed(int64_t(229387429));
+  generator_options go;
+  go.rndtype = generator_options::randomization_type::on_accelerator;
+  go.print_level = 0;
+  EventVector<kT, eT> data(w.dims);
+  auto t0 = std::chrono::steady_clock::now();
+  {
+    generator<kT, eT, CUDABackend, CUDABlock<kT, eT>> gen(&go, &backend, &rnd);
+    std::ostringstream log;
+    auto* old = std::cout.rdbuf(log.rdbuf());
+    gen.generate(n, w.pdf, w.params, data);
+    std::cout.rdbuf(old);
+  }
+  auto t1 = std::chrono::steady_clock::now();
+  const size_t nd = w.dims.size();
+  n = data.nevents();
+  std::vector<double> ev(nd * size_t(n));
+  for (size_t d = 0; d < nd; d++)
+    for (unsigned i = 0; i < n; i++) ev[d * n + i] = double(data(i, d));
+  const uint64_t h = fnv1a(ev.data(), ev.size() * sizeof(double));
+  FitResult r = fit_events<kT>(backend, which, ev, n);
+  char extra[96];
+  std::snprintf(extra, sizeof extra, ",\"generate_ms\":%.3f",
+                std::chrono::duration<double, std::milli>(t1 - t0).count());
+  print_fit(which, n, prec, h, r, extra);
+  return r.ok ? 0 : 1;
+}
+
+// Several host threads, each with its own fitter and CUDABlocks (one fitter
+// per host thread, the reference's threading model) over one backend.
+template <typename kT>
+static int cmd_threads(const std::string& which, unsigned nthreads, const std::string& path, const char* prec) {
+  compute_options copts;
+  CUDABackend backend(&copts);
+  if (!backend.ok()) {
+    std::printf("{\"skipped\":\"%s\"}\n", backend.error().c_str());
+    return 3;
+  }
+  Workload<double, double> w0 = make_workload<double, double>(which);
+  unsigned n = 0;
+  std::vector<double> ev = read_events(path, w0.dims.size(), n);
+  std::vector<FitResult> res(nthreads);
+  std::vector<std::thread> th;
+  NullBuf null;
+  auto* old = std::cout.rdbuf(&null);
+  auto t0 = std::chrono::steady_clock::now();
+  for (unsigned t = 0; t < nthreads; t++)
+    th.emplace_back([&, t]() { res[t] = fit_events<kT>(backend, which, ev, n, false); });
+  for (auto& x : th) x.join();
+  auto t1 = std::chrono::steady_clock::now();
+  std::cout.rdbuf(old);
+  const uint64_t h = fnv1a(ev.data(), ev.size() * sizeof(double));
+  std::printf("{\"workload\":\"%s\",\"n\":%u,\"kernelT\":\"%s\",\"nthreads\":%u,\"events_fnv1a\":\"%016llx\","
+              "\"wall_ms\":%.3f,\"fits\":[",
+              which.c_str(), n, prec, nthreads, (unsigned long long)h,
+              std::chrono::duration<double, std::milli>(t1 - t0).count());
+  bool ok = true;
+  for (unsigned t = 0; t < nthreads; t++) {
+    ok = ok && res[t].ok;
+    std::printf("%s{\"ok\":%s,\"cov_status\":%d,\"fit_ms\":%.3f,\"values\":%s,\"errors\":%s}", t ? "," : "",
+                res[t].ok ? "true" : "false", res[t].cov_status, res[t].warm_ms, jvec(res[t].values).c_str(),
+                jvec(res[t].errors).c_str());
+  }
+  std::printf("]}\n");
+  return ok ? 0 : 1;
+}
+
 int main(int argc, char** argv) {
+  const std::string usage =
+      "usage: dropin lower <workload> | dropin fit <workload> <events.f64> [f32] | "
+      "dropin genfit <workload> <n> [f32] | dropin threads <workload> <nthreads> <events.f64> [f32]\n";
   if (argc < 3) {
-    std::fprintf(stderr, "usage: dropin lower <mass|pwave> | dropin fit <mass|pwave> <n> [f32]\n");
+    std::fprintf(stderr, "%s", usage.c_str());
     return 2;
   }
-  std::string mode = argv[1], which = argv[2];
-  unsigned n = argc > 3 ? unsigned(std::stoul(argv[3])) : 1000;
-  bool f32 = argc > 4 && std::string(argv[4]) == "f32";
-  return f32 ? run<float>(mode, which, n) : run<double>(mode, which, n);
+  const std::string mode = argv[1], which = argv[2];
+  auto is_f32 = [&](int i) { return argc > i && std::string(argv[i]) == "f32"; };
+  if (mode == "lower") return is_f32(3) ? cmd_lower<float>(which) : cmd_lower<double>(which);
+  if (mode == "fit" && argc >= 4)
+    return is_f32(4) ? cmd_fit<float>(which, argv[3], "float") : cmd_fit<double>(which, argv[3], "double");
+  if (mode == "genfit" && argc >= 4) {
+    const unsigned n = unsigned(std::stoul(argv[3]));
+    return is_f32(4) ? cmd_genfit<float>(which, n, "float") : cmd_genfit<double>(which, n, "double");
+  }
+  if (mode == "threads" && argc >= 5) {
+    const unsigned t = unsigned(std::stoul(argv[3]));
+    return is_f32(5) ? cmd_threads<float>(which, t, argv[4], "float")
+                     : cmd_threads<double>(which, t, argv[4], "double");
+  }
+  std::fprintf(stderr, "%s", usage.c_str());
+  return 2;
 }

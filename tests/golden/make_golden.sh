@@ -1,13 +1,14 @@
 #!/usr/bin/env bash
 # Regenerates the golden vectors under tests/golden/ from the reference's own
 # generator, fitter and Minuit2 (oracle/refkit, built from the reference
-# sources by `make -C oracle ref`). Needs the reference tree (REF, default
-# /root/reference); the GPU host only reads the committed outputs.
+# sources by `make -C oracle ref`). Needs the reference sources
+# (MOREFIT_REFERENCE=<reference tree>, or a copy staged by `make -C oracle
+# stage`); the GPU host only reads the committed outputs.
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
 ROOT="$(cd "$HERE/../.." && pwd)"
 make -C "$ROOT/oracle" ref -j"$(nproc)" >/dev/null
-K="$ROOT/oracle/_ref/refkit"
+K="$ROOT/oracle/_ref/$(uname -m)/refkit"
 "$K" golden pwave 1000 "$HERE/pwave_n1000.json" "$HERE/pwave_n1000_events.f64"
 "$K" golden mass 1000 "$HERE/mass_n1000.json" "$HERE/mass_n1000_events.f64"
 "$K" golden mass 100000 "$HERE/mass_n100000.json"

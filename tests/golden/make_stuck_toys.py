@@ -3,9 +3,10 @@ toy datasets (Poisson(2000) events at truths jittered by +-10%, generated by
 the oracle's restatement of the reference generator) on which the
 reference's fitter (MIGRAD + HESSE via oracle/refkit fitfile, started at the
 truth) returns the start point unmoved while the gradient there is far from
-zero. Test infrastructure: needs oracle/_ref/refkit (built from the
+zero. Test infrastructure: needs oracle/_ref/<arch>/refkit (built from the
 reference sources by `make -C oracle ref`)."""
 import json
+import platform
 import struct
 import subprocess
 import sys
@@ -36,7 +37,7 @@ def main(ntry=120, keep=3):
                 f.write(struct.pack("<I", ev.shape[1]))
                 f.write(truth.astype(np.float64).tobytes())
                 f.write(np.ascontiguousarray(ev, dtype=np.float64).tobytes())
-        subprocess.run([str(ROOT / "oracle" / "_ref" / "refkit"), "fitfile", "pwave", str(inp), str(out)], check=True)
+        subprocess.run([str(ROOT / "oracle" / "_ref" / platform.machine() / "refkit"), "fitfile", "pwave", str(inp), str(out)], check=True)
         res = json.loads(out.read_text())
     stuck = [i for i, v in enumerate(res["values"]) if np.array_equal(np.array(v), sets[i][0])][:keep]
     events = np.concatenate([sets[i][1] for i in stuck], axis=1)

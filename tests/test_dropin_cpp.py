@@ -1,7 +1,8 @@
 """include/compute_cuda.hh under the reference's unchanged fitter (CPU only).
 
 The drop-in C++ backend is compiled against the reference's own headers and
-vendored Minuit2 (tests/cpp/Makefile; only where the reference tree exists).
+vendored Minuit2 (tests/cpp/Makefile; only where the reference sources are
+present: MOREFIT_REFERENCE or the copy staged under oracle/_ref/src).
 Without a GPU the reference fitter's make_kernels still drives every
 MakeComputeKernel call, and the backend prints the CUDA source it lowers
 (print_kernel). That source must be byte-identical to what the C ABI lowers
@@ -9,21 +10,17 @@ from the frozen kernel specs, which are the kernels the GPU tests run: the
 C++ drop-in and the GPU-tested path build the same kernels.
 """
 import subprocess
-from pathlib import Path
 
 import pytest
 
-from conftest import ROOT, kernel_spec, load_golden
+from conftest import build_dropin, kernel_spec, load_golden, reference_sources
 
-REF = Path("/root/reference/include/fitter.hh")
-pytestmark = pytest.mark.skipif(not REF.exists(), reason="reference headers not present")
+pytestmark = pytest.mark.skipif(reference_sources() is None, reason="reference sources not present")
 
 
 @pytest.fixture(scope="module")
 def dropin():
-    subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), "ref", "-j8"], check=True)
-    subprocess.run(["make", "-s", "-C", str(ROOT / "tests" / "cpp")], check=True)
-    return ROOT / "tests" / "cpp" / "_build" / "dropin"
+    return build_dropin()
 
 
 def _sources(text):
