@@ -732,11 +732,30 @@ def variants(args):
             ref = res
         info = kern.info()
         bpe = kern.read_layout()["bytes_per_event"]
-        print(json.dumps({"variant": name, "us_per_eval": ms * 1e3, "evals_per_s": 1e3 / ms,
-                          "GBs": n * bpe / (ms * 1e-3) / 1e9, "bytes_per_event": bpe, "registers": info["registers"],
-                          "vec": info["vec"], "block": info["block"],
-                          "rel_diff_vs_first": (np.abs(res - ref) / np.maximum(np.abs(ref), 1.0)).max().item()}),
-              flush=True)
+        row = {"variant": name, "us_per_eval": ms * 1e3, "evals_per_s": 1e3 / ms,
+               "GBs": n * bpe / (ms * 1e-3) / 1e9, "bytes_per_event": bpe, "registers": info["registers"],
+               "vec": info["vec"], "block": info["block"],
+               "rel_diff_vs_first": (np.abs(res - ref) / np.maximum(np.abs(ref), 1.0)).max().item()}
+        if args.lone:
+            # synchronous single evaluations (the fitter's call): host time per
+            # call, and the GPU time of each lone launch from events around it
+            lk = sets[0]
+            for _ in range(20):
+                lk.sums("lh_grad_kernel", truth)
+            gpu_us, host_us = [], []
+            for i in range(max(50, K)):
+                li = sets[i % nsets]
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                t0 = time.perf_counter()
+                a.record(ext)
+                li.sums("lh_grad_kernel", truth)
+                b.record(ext)
+                host_us.append((time.perf_counter() - t0) * 1e6)
+                b.synchronize()
+                gpu_us.append(a.elapsed_time(b) * 1e3)
+            row["lone_gpu_us_median"] = statistics.median(gpu_us)
+            row["lone_call_us_median"] = statistics.median(host_us)
+        print(json.dumps(row), flush=True)
         del sets
 
 
@@ -890,6 +909,7 @@ def main():
     ap.add_argument("--variants", action="store_true", help="time every kernel variant instead")
     ap.add_argument("--variant-list", default="")
     ap.add_argument("--sets", type=int, default=5)
+    ap.add_argument("--lone", action="store_true", help="with --variants: also time synchronous single evaluations")
     args = ap.parse_args()
     if args.warmup < 3 and not args.variants:
         args.warmup = 3

@@ -305,9 +305,12 @@ int mf_columns_sum(const mf_buffer* buf, int elem_type, uint32_t ncols, uint64_t
  * overlaps on the same GPU (two streams, two host threads) race and give
  * wrong sums: serialize them. Each GPU has its own copy. The first
  * call on a device looks up the array's device address on that device (a
- * one-time set-up); make that first call before any stream capture. The
- * call allocates nothing (no cudaMalloc/cudaFree, no allocating library
- * routine); it clears its completion counter with cudaMemsetAsync. */
+ * one-time set-up); make that first call before any stream capture. That
+ * address belongs to the device's primary context (the CUDA runtime's): do
+ * not call the entry point from another driver context on the device, nor
+ * after a cudaDeviceReset in the same process. The call allocates nothing
+ * (no cudaMalloc/cudaFree, no allocating library routine); it clears its
+ * completion counter with cudaMemsetAsync. */
 int mf_columns_sum_noalloc(const void* data, int elem_type, uint32_t ncols, uint64_t n, uint64_t stride,
                            double* sums, void* stream);
 

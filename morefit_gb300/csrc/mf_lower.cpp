@@ -595,6 +595,21 @@ __device__ __forceinline__ void mf_dw_acc_mul(mf_dw& a, mf_dw x, mf_dw y) {
   a.h = s.h;
   a.l = __fadd_rn(a.l, __fadd_rn(s.l, e));
 }
+// a += x * y for FP32 operands: the product is exact as p + e (FMA), so a
+// dot product of FP32 values accumulated this way is as accurate as one
+// computed in double-float (the compensated dot product of Ogita, Rump and
+// Oishi, SIAM J. Sci. Comput. 26, 2005, with a lazily renormalised sum).
+__device__ __forceinline__ mf_dw mf_dw_prodf(float x, float y) {
+  const float p = __fmul_rn(x, y);
+  return mf_dw_make(p, __fmaf_rn(x, y, -p));
+}
+__device__ __forceinline__ void mf_dw_acc_mulf(mf_dw& a, float x, float y) {
+  const float p = __fmul_rn(x, y);
+  const float e = __fmaf_rn(x, y, -p);
+  const mf_dw s = mf_two_sum(a.h, p);
+  a.h = s.h;
+  a.l = __fadd_rn(a.l, __fadd_rn(s.l, e));
+}
 __device__ __forceinline__ mf_dw mf_dw_renorm(mf_dw a) { return mf_two_sum(a.h, a.l); }
 // Round-to-nearest split with integer operations only: h = x rounded to 24
 // bits, l = x - h rounded to 24 bits, |x - h - l| <= 2^-48 |x| for |x| from
@@ -1212,7 +1227,19 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
     std::map<int, std::vector<std::pair<int, int>>> chains;  // chain root -> its terms (a, b)
     std::vector<std::pair<int, int>> fused(roots.size(), {-1, -1});
     std::vector<int> logprod(roots.size(), -1);  // output j = log(node) summed as a running product
-    if (ar == Ar::DW && kind == Kind::Reduce) {
+    // FP32 REDUCE bodies (mixed precision) whose only output is the logarithm
+    // of a dot product of per-event values with parameter-only factors (the
+    // fitter's NLL kernel for a density linear in its prepared columns): that
+    // dot product is kept as a compensated double-float value and its
+    // logarithm summed as a double-float running product, so the NLL carries
+    // no per-event FP32 rounding. Minuit2 takes function values from this
+    // kernel (minuit2_grad_fcn::DoEval, fitter.hh:131-136) and compares them
+    // in its line searches, which FP32 rounding noise of ~1e-7 per event
+    // (1e-4 in the NLL of 1M events) would disturb. Kernels with gradient
+    // outputs keep plain FP32 arithmetic: Minuit2 discards their NLL value
+    // (fitter.hh:138-144), and their cost per event stays at the FP32 rate.
+    std::set<int> f32_dw_chain;  // chain roots evaluated in double-float under F32
+    if ((ar == Ar::DW || ar == Ar::F32) && kind == Kind::Reduce) {
       for (size_t i = 0; i < ns.size(); i++) {
         if (!live[i] || ns[i].uniform || ns[i].op == Op::Input) continue;
         for (int c : {ns[i].a, ns[i].b, ns[i].c})
@@ -1244,6 +1271,22 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
           terms.push_back({ns[k].a, ns[k].b});
         }
       };
+      if (ar == Ar::F32) {
+        // only the chain that is the argument of the single output's logarithm
+        std::set<int> wanted;
+        for (int r : roots)
+          if (M == 1 && ns[r].op == Op::Log && !ns[r].uniform && uses[r] == 1 && chain[ns[r].a])
+            wanted.insert(ns[r].a);
+        for (size_t i = 0; i < ns.size(); i++)
+          if (chain[i] && !wanted.count(int(i))) {
+            // keep chain marks only below a wanted root
+            bool below = false;
+            for (int c = consumer[i]; c >= 0 && !below; c = (uses[c] == 1 && chain[c]) ? consumer[c] : -1)
+              below = wanted.count(c) > 0;
+            if (!below) chain[i] = 0;
+          }
+        f32_dw_chain = wanted;
+      }
       for (size_t i = 0; i < ns.size(); i++) {
         if (!chain[i]) continue;
         const bool absorbed = uses[i] == 1 && consumer[i] >= 0 && chain[consumer[i]];
@@ -1264,6 +1307,13 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
       for (size_t j = 0; j < roots.size(); j++) {
         const int r = roots[j];
         const Node& n = ns[r];
+        if (ar == Ar::F32) {
+          if (n.op == Op::Log && !n.uniform && uses[r] == 1 && !skip[r] && f32_dw_chain.count(n.a)) {
+            logprod[j] = n.a;
+            skip[r] = 1;
+          }
+          continue;
+        }
         if (n.op == Op::Mul && !n.uniform && uses[r] == 1 && !chains.count(r) && !skip[r]) {
           fused[j] = {n.a, n.b};
           skip[r] = 1;
@@ -1284,6 +1334,16 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
       const std::string T = ar == Ar::F32 || ar == Ar::F32S ? "float" : ar == Ar::F64 ? "double" : "mf_dw";
       const std::string lhs = "const " + std::string(n.op == Op::Cmp ? "bool" : T) + " e" + std::to_string(id) + " = ";
       const std::string A = n.a >= 0 ? eref(n.a) : "", B = n.b >= 0 ? eref(n.b) : "", Cc = n.c >= 0 ? eref(n.c) : "";
+      if (ar == Ar::F32 && skip[id]) return "";
+      if (ar == Ar::F32 && chains.count(id)) {
+        const std::string e = "e" + std::to_string(id);
+        const auto& terms = chains.at(id);
+        std::string c = "mf_dw w" + e + "; { mf_dw t_ = mf_dw_prodf(" + eref(terms[0].first) + ", " +
+                        eref(terms[0].second) + ");";
+        for (size_t q = 1; q < terms.size(); q++)
+          c += " mf_dw_acc_mulf(t_, " + eref(terms[q].first) + ", " + eref(terms[q].second) + ");";
+        return c + " w" + e + " = mf_dw_renorm(t_); } const float " + e + " = w" + e + ".h;";
+      }
       if (ar != Ar::DW) {
         const bool f = ar == Ar::F32 || ar == Ar::F32S;
         switch (n.op) {
@@ -1494,12 +1554,21 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
     };
     // Per-thread partials of the log-product outputs, before the block reduction.
     auto acc_finish = [&](std::ostringstream& o) {
-      for (int j = 0; j < M; j++)
-        if (logprod[j] >= 0)
+      for (int j = 0; j < M; j++) {
+        if (logprod[j] < 0) continue;
+        if (ar == Ar::F32)  // as a compensated FP32 partial: (acc, -cmp) = (h, l)
+          o << "  { const mf_dw q_ = mf_dw_logprod_log(lpm" << j << ", lpe" << j << ", mf_logtab); acc[" << j
+            << "] = q_.h; cmp[" << j << "] = -q_.l; }\n";
+        else
           o << "  acc[" << j << "] = mf_dw_logprod_log(lpm" << j << ", lpe" << j << ", mf_logtab);\n";
+      }
     };
     auto acc_add = [&](std::ostringstream& o, const std::string& ind) {
       for (int j = 0; j < M; j++) {
+        if (ar == Ar::F32 && logprod[j] >= 0) {
+          o << ind << "mf_dw_logprod(lpm" << j << ", lpe" << j << ", we" << logprod[j] << ");\n";
+          continue;
+        }
         const std::string r = eref(roots[j]);
         if (ar == Ar::F32 || ar == Ar::F32S)
           o << ind << "mf_kahan_f32(acc[" << j << "], cmp[" << j << "], " << r << ");\n";
@@ -1541,7 +1610,15 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
         << "      if (lane == 0) mf_blk[j0 + warp] = make_float2(a.h, a.l);\n    }\n"
         << "    __syncthreads();\n  }\n";
     };
+    bool f32_logprod = false;
+    for (int j = 0; j < M; j++) f32_logprod = f32_logprod || (ar == Ar::F32 && logprod[j] >= 0);
     auto load_table = [&](std::ostringstream& o) {
+      if (f32_logprod) {
+        o << "  __shared__ float4 mf_logtab[128];\n"
+          << "  for (int q = threadIdx.x; q < 128; q += MF_BLOCK) mf_logtab[q] = mf_dw_logtab_g[q];\n"
+          << "  __syncthreads();\n";
+        return;
+      }
       if (ar != Ar::DW || (!has_log && !has_exp)) return;
       if (has_log)
         o << "  __shared__ float4 mf_logtab[128];\n"

@@ -1361,8 +1361,12 @@ int launch_batched(mf_kernel* k, uint32_t count, const void* const* data, const 
     }
     c->ring = nullptr;
     c->ring_cap = 0;
-    MF_CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&c->ring), size_t(chunk * pstride) * sizeof(float2)));
-    c->ring_cap = size_t(chunk * pstride);
+    // sized for a full chunk of this kernel's evaluations at the largest grid
+    // the device runs, so that later batches (of any count) allocate nothing
+    const uint64_t full = uint64_t(kChunk) * uint64_t(c->num_sms) * uint64_t(k->blocks_per_sm) * k->n_outputs;
+    const uint64_t cap = std::max<uint64_t>(chunk * pstride, full);
+    MF_CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&c->ring), size_t(cap) * sizeof(float2)));
+    c->ring_cap = size_t(cap);
   }
   if (c->ring_grids_cap < kChunk) {
     MF_CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&c->ring_grids), kChunk * sizeof(unsigned)));

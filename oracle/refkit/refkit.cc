@@ -51,6 +51,7 @@
 #include "compute.hh"
 #include "gcc_block.hh"
 #include "fitter.hh"
+#include "Math/MinimizerOptions.h"
 #include "generator.hh"
 #include "plotter.hh"
 #include "random.hh"
@@ -655,6 +656,10 @@ static int cmd_benchevents(const std::string& which, const std::string& path, un
 }
 
 int main(int argc, char** argv) {
+  // MOREFIT_MINUIT_TOLERANCE: Minuit2's default tolerance for every fitter
+  // this process makes (MIGRAD stops at EDM < 0.002 x tolerance); unset, the
+  // Minuit2 default (0.01), as the reference's drivers run.
+  if (const char* t = std::getenv("MOREFIT_MINUIT_TOLERANCE")) ROOT::Math::MinimizerOptions::SetDefaultTolerance(std::atof(t));
   install_capture();
   if (argc >= 5 && std::string(argv[1]) == "fitfile") return cmd_fitfile(argv[2], argv[3], argv[4]);
   if (argc >= 5 && std::string(argv[1]) == "fitevents")

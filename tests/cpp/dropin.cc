@@ -42,6 +42,7 @@
 #include "compute.hh"
 #include "compute_cuda.hh"
 #include "fitter.hh"
+#include "Math/MinimizerOptions.h"
 #include "random.hh"
 // generator.hh selects its seeding by dynamic_cast<LLVMBackend*>; the CUDA
 // backend takes the accelerator branch, so an empty LLVMBackend type suffices.
@@ -280,6 +281,10 @@ static int cmd_threads(const std::string& which, unsigned nthreads, const std::s
 }
 
 int main(int argc, char** argv) {
+  // MOREFIT_MINUIT_TOLERANCE: Minuit2's default tolerance for every fitter
+  // this process makes (MIGRAD stops at EDM < 0.002 x tolerance); unset, the
+  // Minuit2 default (0.01), as the reference's drivers run.
+  if (const char* t = std::getenv("MOREFIT_MINUIT_TOLERANCE")) ROOT::Math::MinimizerOptions::SetDefaultTolerance(std::atof(t));
   const std::string usage =
       "usage: dropin lower <workload> | dropin fit <workload> <events.f64> [f32] | "
       "dropin genfit <workload> <n> [f32] | dropin threads <workload> <nthreads> <events.f64> [f32]\n";
