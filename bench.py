@@ -657,6 +657,8 @@ VARIANTS = {
     "f64_dw_v2": (np.float64, False, 2, 256, False, 0),
     "f64_dw_u2": (np.float64, False, 2, 256, False, 2),
     "f64_dw_v1_u2": (np.float64, False, 1, 256, False, 2),
+    "f64_dw_v2_u1": (np.float64, False, 2, 256, False, 1),
+    "f64_dw_v1_u1": (np.float64, False, 1, 256, False, 1),
     "f32_u2": (np.float32, False, 4, 256, False, 2),
     "f32_v2_u2": (np.float32, False, 2, 256, False, 2),
     "f32_b512": (np.float32, False, 4, 512, False, 0),
@@ -755,6 +757,25 @@ def variants(args):
                 gpu_us.append(a.elapsed_time(b) * 1e3)
             row["lone_gpu_us_median"] = statistics.median(gpu_us)
             row["lone_call_us_median"] = statistics.median(host_us)
+            # the lone launch itself: a spin kernel keeps the stream busy while
+            # the host enqueues event, evaluation and event, so the events
+            # bracket the kernel (and one launch gap) without host latency
+            ob = L.c_buf()
+            L.check(L.lib.mf_buffer_alloc(backend.handle, kern.nout * 8, C.byref(ob)))
+            kus = []
+            with torch.cuda.stream(ext):
+                for i in range(max(50, K)):
+                    li = sets[i % nsets]
+                    torch.cuda._sleep(100000)
+                    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    a.record(ext)
+                    li.sums_async("lh_grad_kernel", truth, ob, 0)
+                    b.record(ext)
+                    b.synchronize()
+                    kus.append(a.elapsed_time(b) * 1e3)
+            L.lib.mf_buffer_free(ob)
+            row["lone_kernel_us_median"] = statistics.median(kus)
+            row["lone_kernel_us_min"] = min(kus)
         print(json.dumps(row), flush=True)
         del sets
 

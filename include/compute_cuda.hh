@@ -12,8 +12,16 @@
  *                   morefit::CUDABlock<double, double>> fit(&fit_opts, &backend);
  *
  * kernelT = double gives the plain FP64 path; kernelT = float gives the
- * mixed-precision path (FP32 event columns and per-event arithmetic, FP64
- * sums; evalT stays double).
+ * reference's mixed-precision interface (FP32 event columns and per-event
+ * arithmetic, FP64 sums; evalT stays double). With kernelT = float the
+ * reference's fitter hands every parameter and hoisted parameter buffer to
+ * the block rounded to FP32 (fitter.hh:1059-1073), each rounded on its own,
+ * so the likelihood it minimises jumps by about N * 6e-8 whenever one of
+ * them crosses an FP32 boundary (~0.03 at 1M events): more than MIGRAD's
+ * convergence test tolerates. cuda_options::mixed_precision keeps kernelT =
+ * double at the interface (FP64 parameters) and stores and computes the
+ * events in FP32 inside the block: the function stays smooth in the
+ * parameters and fits agree with FP64 ones to ~1e-5 sigma.
  *
  * Mapping of the interface (reference line -> this class):
  *  - MakeComputeKernel (compute.hh:143) hands the ComputeGraphNode
@@ -56,6 +64,13 @@ struct cuda_options {
   int device = 0;
   uint64_t hbm_budget_bytes = 0;  // 0 = no cap
   bool quiet = false;             // do not print failures to std::cerr
+  // CUDABlock<double>: FP32 event columns and per-event arithmetic behind the
+  // FP64 interface (FP64 parameters, sums and Minuit2 covariance)
+  bool mixed_precision = false;
+  // Route every synchronous evaluation of this backend's blocks through a
+  // coalescer shared with other threads' backends (mf_coalescer_create);
+  // not owned, must outlive the backend.
+  mf_coalescer* coalescer = nullptr;
 };
 
 class CUDABackend : public ComputeBackend {
@@ -65,10 +80,19 @@ class CUDABackend : public ComputeBackend {
       error_ = mf_last_error();
       ctx_ = nullptr;
       if (!copts_.quiet) std::cerr << "CUDABackend: " << error_ << std::endl;
+      return;
+    }
+    if (copts_.coalescer && mf_context_set_coalescer(ctx_, copts_.coalescer) != MF_OK) {
+      error_ = mf_last_error();
+      mf_context_destroy(ctx_);
+      ctx_ = nullptr;
+      if (!copts_.quiet) std::cerr << "CUDABackend: " << error_ << std::endl;
     }
   }
   ~CUDABackend() {
-    if (ctx_) mf_context_destroy(ctx_);
+    if (!ctx_) return;
+    if (copts_.coalescer) mf_context_set_coalescer(ctx_, nullptr);
+    mf_context_destroy(ctx_);
   }
   CUDABackend(const CUDABackend&) = delete;
   CUDABackend& operator=(const CUDABackend&) = delete;
@@ -121,11 +145,12 @@ class CUDABlock : public ComputeBlock<kernelT, evalT, seedT> {
   static_assert(std::is_same_v<kernelT, double> || std::is_same_v<kernelT, float>,
                 "CUDABlock supports kernelT = double (FP64) or float (mixed precision)");
   static_assert(std::is_same_v<seedT, uint32_t>, "the accelerator generator uses xoshiro128++ (uint32_t seeds)");
-  static constexpr int kElem = std::is_same_v<kernelT, float> ? MF_F32 : MF_F64;
   using Columns = cuda_detail::Columns;
 
  public:
-  explicit CUDABlock(CUDABackend* backend) : backend_(backend) {}
+  explicit CUDABlock(CUDABackend* backend)
+      : backend_(backend),
+        kElem(std::is_same_v<kernelT, float> || (backend && backend->cuda_opts().mixed_precision) ? MF_F32 : MF_F64) {}
   ~CUDABlock() {
     if (kernel_) mf_kernel_free(kernel_);
   }
@@ -175,6 +200,10 @@ class CUDABlock : public ComputeBlock<kernelT, evalT, seedT> {
     const uint32_t ncols = data.ndimensions();
     const uint64_t n = data.nevents();
     if (check(input_->ensure(ncols, n))) return false;
+    if constexpr (std::is_same_v<kernelT, double>)
+      if (kElem == MF_F32)  // mixed precision behind the FP64 interface
+        return !check(mf_events_upload_f64_as(input_->buf, MF_F32, data.get_data(), ncols, n, data.nevents_padded(),
+                                              input_->stride));
     return !check(mf_events_upload(input_->buf, kElem, data.get_data(), ncols, n, data.nevents_padded(),
                                    input_->stride));
   }
@@ -191,6 +220,15 @@ class CUDABlock : public ComputeBlock<kernelT, evalT, seedT> {
     if (!output_ || !output_->buf) return fail("CopyFromOutputBuffer: no output on the device");
     const uint32_t ncols = std::min<uint32_t>(data.ndimensions(), output_->ncols);
     const uint64_t n = std::min<uint64_t>(data.nevents(), output_->n);
+    if constexpr (std::is_same_v<kernelT, double>)
+      if (kElem == MF_F32) {  // FP32 columns into an FP64 EventVector
+        std::vector<float> tmp(size_t(ncols) * n);
+        if (check(mf_events_download(output_->buf, MF_F32, tmp.data(), ncols, n, n, output_->stride))) return false;
+        const uint64_t hs = data.nevents_padded();
+        for (uint32_t c = 0; c < ncols; c++)
+          for (uint64_t i = 0; i < n; i++) data.get_data()[c * hs + i] = double(tmp[c * n + i]);
+        return true;
+      }
     return !check(mf_events_download(output_->buf, kElem, data.get_data(), ncols, n, data.nevents_padded(),
                                      output_->stride));
   }
@@ -358,6 +396,7 @@ class CUDABlock : public ComputeBlock<kernelT, evalT, seedT> {
   }
 
   CUDABackend* backend_;
+  const int kElem;  // element type of the device columns and kernels
   std::shared_ptr<Columns> input_, output_;
   std::vector<kernelT> params_;
   std::vector<evalT> kahan_;

@@ -39,6 +39,7 @@ extern "C" {
 #define MF_ERR_NO_DEVICE 6    /* no CUDA device, or the device is not sm_103 */
 #define MF_ERR_UNSUPPORTED 7  /* valid request this build does not implement */
 #define MF_ERR_TIMEOUT 8      /* a bounded device wait gave up */
+#define MF_ERR_NOT_READY 9    /* an asynchronous result is not ready yet (mf_coalesced_poll) */
 
 /* ---- element types (kernelT of ComputeBlock<kernelT, evalT>) ---- */
 #define MF_F64 0
@@ -56,6 +57,7 @@ extern "C" {
 typedef struct mf_context mf_context;
 typedef struct mf_buffer mf_buffer;
 typedef struct mf_kernel mf_kernel;
+typedef struct mf_coalescer mf_coalescer;
 
 /* Message of the calling thread's last failed call ("" if none). */
 const char* mf_last_error(void);
@@ -276,6 +278,56 @@ int mf_kernel_reduce_async(mf_kernel* k, const mf_buffer* input, uint64_t stride
  * parameter points per host call (several fits' requests, toy batches). */
 int mf_kernel_reduce_many(mf_kernel* k, uint32_t count, const mf_buffer* const* inputs, const uint64_t* strides,
                           const uint64_t* ns, const double* params, uint32_t n_params, mf_buffer* out);
+
+/* Evaluates `count` datasets (inputs[i], column stride strides[i], ns[i] >= 1
+ * events, parameter row i) in ONE launch of the kernel's multi-dataset entry
+ * plus one combine launch, enqueued on the context's stream; row i of `out`
+ * receives dataset i's sums. Each dataset is cut into segments of 2048
+ * events, one block per segment, and its segments' partial sums are combined
+ * in a fixed order, so a dataset's sums are the same bit for bit whatever
+ * else shares the launch (they differ from mf_kernel_reduce's, which sums in
+ * another order, by rounding only). For many small datasets per host call,
+ * where one launch per dataset (mf_kernel_reduce_many) is launch-bound:
+ * concurrent fits, serving ticks. No counterpart in the reference, whose
+ * blocks evaluate one dataset per SubmitKernel (compute.hh:146). */
+int mf_kernel_reduce_multi(mf_kernel* k, uint32_t count, const mf_buffer* const* inputs, const uint64_t* strides,
+                           const uint64_t* ns, const double* params, uint32_t n_params, mf_buffer* out);
+
+/* ---- coalescing of concurrent host fitters ----
+ * The reference runs one fitter per host thread, each calling
+ * ComputeBlock::SubmitKernel + Finish + CopyFromKahanBuffer synchronously
+ * from Minuit2's callbacks (minuit2_grad_fcn, fitter.hh:113-169;
+ * likelihood_and_gradient, fitter.hh:1054-1151). A coalescer gathers the
+ * synchronous evaluations that such threads make at about the same time and
+ * runs them as shared launches (mf_kernel_reduce_multi's entry, one launch
+ * pair per kernel source per tick) on its own stream, from one dispatch
+ * thread.
+ *
+ * mf_coalescer_create starts the dispatch thread and a context of its own on
+ * `device`. A tick starts when a request arrives and launches once every
+ * attached context has a request waiting, `max_batch` requests are waiting
+ * (0 = 256), or `window_us` microseconds have passed, whichever comes first.
+ * mf_context_set_coalescer(ctx, co) routes every later mf_kernel_reduce on
+ * ctx (the call CUDABlock::SubmitKernel makes) through co; NULL detaches.
+ * The calling thread blocks until its tick completes, then returns the sums
+ * as mf_kernel_reduce does (a double-float kernel's non-finite sums are
+ * evaluated again in native FP64 on ctx, alone). A request's sums depend
+ * only on its own data and parameters: the same alone or in any mix.
+ * Detach every context before mf_coalescer_destroy (MF_ERR_INVALID
+ * otherwise). Requests of one context must come from one thread at a time,
+ * as the reference's blocks do. */
+int mf_coalescer_create(int device, uint32_t max_batch, uint32_t window_us, mf_coalescer** out);
+int mf_coalescer_destroy(mf_coalescer* co);
+int mf_context_set_coalescer(mf_context* ctx, mf_coalescer* co);
+/* Asynchronous form: submit returns a ticket at once (parameters copied);
+ * poll with wait = 0 returns MF_ERR_NOT_READY until the tick has run, with
+ * wait != 0 blocks; MF_OK writes the n_outputs sums and retires the ticket.
+ * Sums are the tick's as launched (no native-FP64 re-evaluation). */
+int mf_coalesced_submit(mf_coalescer* co, mf_kernel* k, const mf_buffer* input, uint64_t stride, uint64_t n,
+                        const double* params, uint32_t n_params, uint64_t* ticket);
+int mf_coalesced_poll(mf_coalescer* co, uint64_t ticket, double* sums, int wait);
+/* Ticks run, evaluations served and the largest batch so far. */
+int mf_coalescer_stats(const mf_coalescer* co, uint64_t* ticks, uint64_t* evaluations, uint32_t* max_batch);
 
 /* Compensated sums over events of ncols columns of an SoA event block:
  * sums[c] = sum_{i<n} column c (element type MF_F64 or MF_F32, column stride

@@ -21,6 +21,7 @@ MF_ERR_BUDGET = 5
 MF_ERR_NO_DEVICE = 6
 MF_ERR_UNSUPPORTED = 7
 MF_ERR_TIMEOUT = 8
+MF_ERR_NOT_READY = 9
 
 MF_F64 = 0
 MF_F32 = 1
@@ -30,7 +31,7 @@ MF_KERNEL_GENERATE = 2
 MF_COLUMN_ALIGN = 64
 
 _NAMES = {1: "INVALID", 2: "CUDA", 3: "NVRTC", 4: "PARSE", 5: "BUDGET", 6: "NO_DEVICE", 7: "UNSUPPORTED",
-          8: "TIMEOUT"}
+          8: "TIMEOUT", 9: "NOT_READY"}
 
 
 class MFError(RuntimeError):
@@ -49,6 +50,7 @@ lib = C.CDLL(str(_LIB_PATH))
 c_ctx = C.c_void_p
 c_buf = C.c_void_p
 c_ker = C.c_void_p
+c_coal = C.c_void_p
 c_char_pp = C.POINTER(C.c_char_p)
 c_dbl_p = C.POINTER(C.c_double)
 
@@ -153,6 +155,15 @@ _proto("mf_spd_solve_batch", C.c_int, C.c_uint32, C.c_uint32, c_dbl_p, c_dbl_p, 
 _proto("mf_generate_partition", C.c_int, C.c_uint64, C.c_uint32, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32))
 _proto("mf_lower_source", C.c_int, C.POINTER(KernelDesc), C.c_char_p, C.c_size_t, C.POINTER(C.c_size_t))
 _proto("mf_compile_check", C.c_int, C.POINTER(KernelDesc), C.POINTER(C.c_int), C.POINTER(C.c_int))
+_proto("mf_kernel_reduce_multi", C.c_int, c_ker, C.c_uint32, C.POINTER(c_buf), C.POINTER(C.c_uint64),
+       C.POINTER(C.c_uint64), c_dbl_p, C.c_uint32, c_buf)
+_proto("mf_coalescer_create", C.c_int, C.c_int, C.c_uint32, C.c_uint32, C.POINTER(c_coal))
+_proto("mf_coalescer_destroy", C.c_int, c_coal)
+_proto("mf_context_set_coalescer", C.c_int, c_ctx, c_coal)
+_proto("mf_coalesced_submit", C.c_int, c_coal, c_ker, c_buf, C.c_uint64, C.c_uint64, c_dbl_p, C.c_uint32,
+       C.POINTER(C.c_uint64))
+_proto("mf_coalesced_poll", C.c_int, c_coal, C.c_uint64, c_dbl_p, C.c_int)
+_proto("mf_coalescer_stats", C.c_int, c_coal, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.POINTER(C.c_uint32))
 
 
 def check(rc: int) -> None:
@@ -185,5 +196,6 @@ def exported_symbols() -> list[str]:
         "mf_buffer_d2h_async", "mf_kernel_store_async", "mf_eval_expressions_batch", "mf_kernel_generate_segments",
         "mf_expr_set_create", "mf_expr_set_eval", "mf_expr_set_free", "mf_kernel_fallback_count",
         "mf_histogram", "mf_events_load_file", "mf_splitmix_seed_rows", "mf_buffer_wrap_host",
-        "mf_spd_solve_batch",
+        "mf_spd_solve_batch", "mf_kernel_reduce_multi", "mf_coalescer_create", "mf_coalescer_destroy",
+        "mf_context_set_coalescer", "mf_coalesced_submit", "mf_coalesced_poll", "mf_coalescer_stats",
     ]

@@ -48,8 +48,17 @@ class CUDABackend:
     def synchronize(self) -> None:
         L.check(L.lib.mf_context_synchronize(self._h))
 
+    def set_coalescer(self, coalescer: "Coalescer | None") -> None:
+        """Routes this context's synchronous evaluations through `coalescer`
+        (None detaches): concurrent fitters in other threads share its launches."""
+        L.check(L.lib.mf_context_set_coalescer(self._h, coalescer.handle if coalescer else None))
+        self._coalescer = coalescer
+
     def close(self) -> None:
         if getattr(self, "_h", None):
+            if getattr(self, "_coalescer", None) is not None:
+                L.lib.mf_context_set_coalescer(self._h, None)
+                self._coalescer = None
             L.lib.mf_context_destroy(self._h)
             self._h = None
 
@@ -58,6 +67,30 @@ class CUDABackend:
             self.close()
         except Exception:
             pass
+
+
+class Coalescer:
+    """Gathers the synchronous evaluations of several contexts (one per host
+    thread, each running its own fit) into shared launches (mf_coalescer_*)."""
+
+    def __init__(self, device: int = 0, max_batch: int = 0, window_us: int = 30):
+        h = L.c_coal()
+        L.check(L.lib.mf_coalescer_create(device, max_batch, window_us, C.byref(h)))
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def stats(self) -> dict:
+        t, e, m = C.c_uint64(), C.c_uint64(), C.c_uint32()
+        L.check(L.lib.mf_coalescer_stats(self._h, C.byref(t), C.byref(e), C.byref(m)))
+        return {"ticks": t.value, "evaluations": e.value, "max_batch": m.value}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            L.check(L.lib.mf_coalescer_destroy(self._h))
+            self._h = None
 
 
 class DeviceColumns:

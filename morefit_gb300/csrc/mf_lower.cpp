@@ -603,6 +603,19 @@ __device__ __forceinline__ mf_dw mf_dw_prodf(float x, float y) {
   const float p = __fmul_rn(x, y);
   return mf_dw_make(p, __fmaf_rn(x, y, -p));
 }
+// The same with a double-float factor c = c.h + c.l (a parameter-only
+// coefficient kept to ~48 bits): x * c.h exact as p + e, plus x * c.l.
+__device__ __forceinline__ mf_dw mf_dw_prodfw(float x, mf_dw c) {
+  const float p = __fmul_rn(x, c.h);
+  return mf_dw_make(p, __fmaf_rn(x, c.l, __fmaf_rn(x, c.h, -p)));
+}
+__device__ __forceinline__ void mf_dw_acc_mulfw(mf_dw& a, float x, mf_dw c) {
+  const float p = __fmul_rn(x, c.h);
+  const float e = __fmaf_rn(x, c.l, __fmaf_rn(x, c.h, -p));
+  const mf_dw s = mf_two_sum(a.h, p);
+  a.h = s.h;
+  a.l = __fadd_rn(a.l, __fadd_rn(s.l, e));
+}
 __device__ __forceinline__ void mf_dw_acc_mulf(mf_dw& a, float x, float y) {
   const float p = __fmul_rn(x, y);
   const float e = __fmaf_rn(x, y, -p);
@@ -1227,6 +1240,9 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
     std::map<int, std::vector<std::pair<int, int>>> chains;  // chain root -> its terms (a, b)
     std::vector<std::pair<int, int>> fused(roots.size(), {-1, -1});
     std::vector<int> logprod(roots.size(), -1);  // output j = log(node) summed as a running product
+    // ... plus (or minus) a parameter-only value per event (the normalisation
+    // term of logprob_normalised, pdf.hh:103-106): log(x) + u or log(x) - u
+    std::vector<int> logadd(roots.size(), -1), logsign(roots.size(), 0), lognode(roots.size(), -1);
     // FP32 REDUCE bodies (mixed precision) whose only output is the logarithm
     // of a dot product of per-event values with parameter-only factors (the
     // fitter's NLL kernel for a density linear in its prepared columns): that
@@ -1271,12 +1287,41 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
           terms.push_back({ns[k].a, ns[k].b});
         }
       };
+      // Output r as log(x) [+ or - u]: the Log node (used only there), u, sign.
+      auto log_form = [&](int r, int& lg, int& u, int& sign) {
+        lg = -1;
+        u = -1;
+        sign = 0;
+        const Node& n = ns[r];
+        if (n.uniform || uses[r] != 1) return false;
+        auto is_log = [&](int k) { return ns[k].op == Op::Log && !ns[k].uniform && uses[k] == 1; };
+        if (is_log(r)) {
+          lg = r;
+          return true;
+        }
+        if (n.op == Op::Add || n.op == Op::Sub) {
+          if (is_log(n.a) && ns[n.b].uniform) {
+            lg = n.a;
+            u = n.b;
+            sign = n.op == Op::Add ? 1 : -1;
+            return true;
+          }
+          if (n.op == Op::Add && is_log(n.b) && ns[n.a].uniform) {
+            lg = n.b;
+            u = n.a;
+            sign = 1;
+            return true;
+          }
+        }
+        return false;
+      };
       if (ar == Ar::F32) {
         // only the chain that is the argument of the single output's logarithm
         std::set<int> wanted;
-        for (int r : roots)
-          if (M == 1 && ns[r].op == Op::Log && !ns[r].uniform && uses[r] == 1 && chain[ns[r].a])
-            wanted.insert(ns[r].a);
+        for (int r : roots) {
+          int lg, u, sg;
+          if (M == 1 && log_form(r, lg, u, sg) && chain[ns[lg].a]) wanted.insert(ns[lg].a);
+        }
         for (size_t i = 0; i < ns.size(); i++)
           if (chain[i] && !wanted.count(int(i))) {
             // keep chain marks only below a wanted root
@@ -1307,10 +1352,16 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
       for (size_t j = 0; j < roots.size(); j++) {
         const int r = roots[j];
         const Node& n = ns[r];
+        int lg = -1, u = -1, sg = 0;
+        const bool lf = !skip[r] && log_form(r, lg, u, sg);
         if (ar == Ar::F32) {
-          if (n.op == Op::Log && !n.uniform && uses[r] == 1 && !skip[r] && f32_dw_chain.count(n.a)) {
-            logprod[j] = n.a;
+          if (lf && f32_dw_chain.count(ns[lg].a)) {
+            logprod[j] = ns[lg].a;
+            logadd[j] = u;
+            logsign[j] = sg;
+            lognode[j] = lg;
             skip[r] = 1;
+            skip[lg] = 1;
           }
           continue;
         }
@@ -1318,11 +1369,16 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
           fused[j] = {n.a, n.b};
           skip[r] = 1;
         }
-        // an output that is the logarithm of a per-event value, used nowhere
-        // else: sum of logs = log of the product (one multiply per event)
-        if (n.op == Op::Log && !n.uniform && uses[r] == 1 && !skip[r]) {
-          logprod[j] = n.a;
+        // an output that is the logarithm of a per-event value (plus or minus a
+        // parameter-only value), used nowhere else: sum of logs = log of the
+        // product (one multiply per event), plus the event count times u
+        if (lf && !skip[r]) {
+          logprod[j] = ns[lg].a;
+          logadd[j] = u;
+          logsign[j] = sg;
+          lognode[j] = lg;
           skip[r] = 1;
+          skip[lg] = 1;
         }
       }
     }
@@ -1336,12 +1392,26 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
       const std::string A = n.a >= 0 ? eref(n.a) : "", B = n.b >= 0 ? eref(n.b) : "", Cc = n.c >= 0 ? eref(n.c) : "";
       if (ar == Ar::F32 && skip[id]) return "";
       if (ar == Ar::F32 && chains.count(id)) {
+        // terms value x factor, the parameter-only factor as a double-float
+        // pair (so that the sum follows the FP64 parameters smoothly)
         const std::string e = "e" + std::to_string(id);
         const auto& terms = chains.at(id);
-        std::string c = "mf_dw w" + e + "; { mf_dw t_ = mf_dw_prodf(" + eref(terms[0].first) + ", " +
-                        eref(terms[0].second) + ");";
-        for (size_t q = 1; q < terms.size(); q++)
-          c += " mf_dw_acc_mulf(t_, " + eref(terms[q].first) + ", " + eref(terms[q].second) + ");";
+        std::string c = "mf_dw w" + e + "; { mf_dw t_;";
+        for (size_t q = 0; q < terms.size(); q++) {
+          const bool a_uni = ns[terms[q].first].uniform;
+          const int u = a_uni ? terms[q].first : terms[q].second, v = a_uni ? terms[q].second : terms[q].first;
+          std::string cw;
+          if (ns[u].op == Op::Const) {
+            const float h = float(ns[u].value);
+            char b[96];
+            std::snprintf(b, sizeof b, "mf_dw_make(%af, %af)", double(h), double(float(ns[u].value - double(h))));
+            cw = b;
+          } else {
+            cw = "uw" + std::to_string(u);
+          }
+          c += q == 0 ? " t_ = mf_dw_prodfw(" + eref(v) + ", " + cw + ");"
+                      : " mf_dw_acc_mulfw(t_, " + eref(v) + ", " + cw + ");";
+        }
         return c + " w" + e + " = mf_dw_renorm(t_); } const float " + e + " = w" + e + ".h;";
       }
       if (ar != Ar::DW) {
@@ -1498,6 +1568,20 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
       if (ar != Ar::F64)
         for (int k : uni_used)
           add_slot(k, ns[k].op == Op::Cmp ? UniformSlot::Bool : ar == Ar::DW ? UniformSlot::DwPair : UniformSlot::Float);
+      if (ar == Ar::F32) {  // double-float factors of the compensated NLL dot product ("uw<node>")
+        std::set<int> fac;
+        for (auto& [root, terms] : chains)
+          for (auto& [ta, tb] : terms) {
+            const int u = ns[ta].uniform ? ta : tb;
+            if (ns[u].op != Op::Const) fac.insert(u);
+          }
+        for (int j = 0; j < M; j++)
+          if (logadd[j] >= 0 && ns[logadd[j]].op != Op::Const) fac.insert(logadd[j]);
+        for (int k : fac) {
+          add_slot(k, UniformSlot::DwPair);
+          slot_names[k] = "uw" + std::to_string(k);
+        }
+      }
       out.host_args = true;
       out.nodes = ns;
       out.slots = slots;
@@ -1528,8 +1612,8 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
           case UniformSlot::Float: o << "  const float " << eref(k) << " = " << P << "f[" << off << "];\n"; break;
           case UniformSlot::Bool: o << "  const bool " << eref(k) << " = " << P << "f[" << off << "] != 0.0f;\n"; break;
           case UniformSlot::DwPair:
-            o << "  const mf_dw " << eref(k) << " = mf_dw_make(" << P << "f[" << off << "], " << P << "f["
-              << sl.offset + 1 << "]);\n";
+            o << "  const mf_dw " << (ar == Ar::F32 ? slot_names[k] : eref(k)) << " = mf_dw_make(" << P << "f["
+              << off << "], " << P << "f[" << sl.offset + 1 << "]);\n";
             break;
         }
       }
@@ -1550,21 +1634,41 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
       else
         o << "  mf_dw acc[MF_NOUT];\n#pragma unroll\n  for (int j = 0; j < MF_NOUT; j++) acc[j] = mf_dw_make(0.0f, 0.0f);\n";
       for (int j = 0; j < M; j++)
-        if (logprod[j] >= 0) o << "  mf_dw lpm" << j << " = mf_dw_make(1.0f, 0.0f);\n  int lpe" << j << " = 0;\n";
+        if (logprod[j] >= 0) {
+          o << "  mf_dw lpm" << j << " = mf_dw_make(1.0f, 0.0f);\n  int lpe" << j << " = 0;\n";
+          if (logadd[j] >= 0) o << "  int lpc" << j << " = 0;\n";
+        }
     };
     // Per-thread partials of the log-product outputs, before the block reduction.
     auto acc_finish = [&](std::ostringstream& o) {
       for (int j = 0; j < M; j++) {
         if (logprod[j] < 0) continue;
+        const std::string J = std::to_string(j);
+        o << "  { mf_dw q_ = mf_dw_logprod_log(lpm" << J << ", lpe" << J << ", mf_logtab);\n";
+        if (logadd[j] >= 0) {
+          // plus (minus) the thread's event count times u, the count exact in FP32
+          std::string uw;
+          if (ns[logadd[j]].op == Op::Const) {
+            const float h = float(ns[logadd[j]].value);
+            char b[96];
+            std::snprintf(b, sizeof b, "mf_dw_make(%af, %af)", double(h),
+                          double(float(ns[logadd[j]].value - double(h))));
+            uw = b;
+          } else {
+            uw = ar == Ar::F32 ? "uw" + std::to_string(logadd[j]) : eref(logadd[j]);
+          }
+          o << "    const mf_dw c_ = mf_dw_mul(mf_dw_make((float)lpc" << J << ", 0.0f), " << uw << ");\n"
+            << "    q_ = " << (logsign[j] > 0 ? "mf_dw_add" : "mf_dw_sub") << "(q_, c_);\n";
+        }
         if (ar == Ar::F32)  // as a compensated FP32 partial: (acc, -cmp) = (h, l)
-          o << "  { const mf_dw q_ = mf_dw_logprod_log(lpm" << j << ", lpe" << j << ", mf_logtab); acc[" << j
-            << "] = q_.h; cmp[" << j << "] = -q_.l; }\n";
+          o << "    acc[" << J << "] = q_.h; cmp[" << J << "] = -q_.l; }\n";
         else
-          o << "  acc[" << j << "] = mf_dw_logprod_log(lpm" << j << ", lpe" << j << ", mf_logtab);\n";
+          o << "    acc[" << J << "] = q_; }\n";
       }
     };
     auto acc_add = [&](std::ostringstream& o, const std::string& ind) {
       for (int j = 0; j < M; j++) {
+        if (logadd[j] >= 0) o << ind << "lpc" << j << "++;\n";
         if (ar == Ar::F32 && logprod[j] >= 0) {
           o << ind << "mf_dw_logprod(lpm" << j << ", lpe" << j << ", we" << logprod[j] << ");\n";
           continue;
@@ -1850,6 +1954,38 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
     block_reduce(s);
     s << R"CUDA(  for (int j = threadIdx.x; j < MF_NOUT; j += MF_BLOCK)
     out[(mf_u64)seg * MF_NOUT + j] = mf_dw_to_double(mf_dw_make(mf_blk[j].x, mf_blk[j].y));
+}
+)CUDA";
+    // ---- many datasets in one launch: one block per segment ----
+    // A segment is a run of at most MF_MULTI_CHUNK events of one dataset
+    // (its own columns, stride and parameter row); the block writes its
+    // partial row to `row` of the partial buffer, and <entry>_combine then
+    // reduces each dataset's rows in a fixed order. A dataset's sums depend
+    // only on its own events, parameters and size (segments are cut at fixed
+    // multiples of MF_MULTI_CHUNK), never on what else shares the launch.
+    s << "struct mf_seg { const void* data; mf_u64 stride; mf_u64 first; unsigned count; unsigned req; unsigned row;"
+         " unsigned pad; };\n";
+    s << "extern \"C\" __global__ void __launch_bounds__(MF_BLOCK) " << out.entry
+      << "_multi(const mf_seg* __restrict__ segs, const mf_args* __restrict__ args,"
+      << " float2* __restrict__ partials) {\n";
+    load_table(s);
+    s << "  const mf_seg S = segs[blockIdx.x];\n"
+      << "  const " << DT << "* __restrict__ data = static_cast<const " << DT << "*>(S.data);\n"
+      << "  const mf_u64 stride = S.stride, first = S.first;\n  const unsigned cnt = S.count;\n"
+      << "  const mf_args& P = args[S.req];\n";
+    prologue(s, "P.");
+    acc_decl(s);
+    s << "  for (unsigned i = threadIdx.x; i < cnt; i += MF_BLOCK) {\n";
+    for (int k : out.used_inputs)
+      s << "    const " << XT << " x" << k << " = " << input_value("__ldg(data + (mf_u64)" + std::to_string(k) +
+                                                                   " * stride + first + i)")
+        << ";\n";
+    body(s, "    ");
+    acc_add(s, "    ");
+    s << "  }\n";
+    acc_finish(s);
+    block_reduce(s);
+    s << R"CUDA(  for (int j = threadIdx.x; j < MF_NOUT; j += MF_BLOCK) partials[(mf_u64)S.row * MF_NOUT + j] = mf_blk[j];
 }
 )CUDA";
     // ---- per-dataset preparation of the columns the entries above read ----

@@ -14,6 +14,8 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <condition_variable>
+#include <deque>
 #include <cctype>
 #include <cmath>
 #include <cstdio>
@@ -27,6 +29,7 @@
 #include <sstream>
 #include <string>
 #include <sys/stat.h>
+#include <thread>
 #include <vector>
 
 #include "../../include/morefit_cuda.h"
@@ -217,6 +220,8 @@ struct mf_context {
   size_t ring_cap = 0;  // float2
   unsigned* ring_grids = nullptr;
   size_t ring_grids_cap = 0;
+  // synchronous evaluations routed through a coalescer (mf_context_set_coalescer)
+  mf_coalescer* coalescer = nullptr;
 };
 
 // A copy of a buffer's columns in the layout a REDUCE kernel reads (folded
@@ -284,6 +289,7 @@ struct mf_kernel {
   cudaKernel_t fn_prep = nullptr;  // REDUCE kernels reading prepared columns
   cudaKernel_t fn_part = nullptr;     // REDUCE: per-block partials only (batched evaluations)
   cudaKernel_t fn_combine = nullptr;  // REDUCE: one block per batched evaluation
+  cudaKernel_t fn_multi = nullptr;    // REDUCE: segments of many datasets in one launch
   uint64_t prep_key = 0;
   int blocks_per_sm = 1;
   int max_input = -1;
@@ -866,6 +872,7 @@ int mf_kernel_build(mf_context* c, const mf_kernel_desc* d, mf_kernel** out) {
   if (d->kind == MF_KERNEL_REDUCE) {
     MF_CUDA_TRY(cudaLibraryGetKernel(&k->fn_part, k->lib, (k->lowered.entry + "_part").c_str()));
     MF_CUDA_TRY(cudaLibraryGetKernel(&k->fn_combine, k->lib, (k->lowered.entry + "_combine").c_str()));
+    MF_CUDA_TRY(cudaLibraryGetKernel(&k->fn_multi, k->lib, (k->lowered.entry + "_multi").c_str()));
   }
   if (k->lowered.prep) {
     MF_CUDA_TRY(cudaLibraryGetKernel(&k->fn_prep, k->lib, (k->lowered.entry + "_prep").c_str()));
@@ -1437,10 +1444,32 @@ static int f64_twin(mf_kernel* k) {
   return mf_kernel_build(k->ctx, &d, &k->f64);
 }
 
+static int reduce_direct(mf_kernel* k, const mf_buffer* in, uint64_t stride, uint64_t n, const double* params,
+                         uint32_t n_params, double* sums);
+int coalesced_reduce(mf_kernel* k, const mf_buffer* in, uint64_t stride, uint64_t n, const double* params,
+                     uint32_t n_params, double* sums);
+
 extern "C" {
 
 int mf_kernel_reduce(mf_kernel* k, const mf_buffer* in, uint64_t stride, uint64_t n, const double* params,
                      uint32_t n_params, double* sums) {
+  if (!k || !sums) return fail(MF_ERR_INVALID, "null argument");
+  if (k->kind == MF_KERNEL_REDUCE && k->ctx->coalescer && n > 0) {
+    if (n_params != k->n_params || (n_params && !params))
+      return fail(MF_ERR_INVALID, "parameter count mismatch (" + std::to_string(n_params) + " given, " +
+                                      std::to_string(k->n_params) + " expected)");
+    int rc = check_layout(k, in, stride, n);
+    if (rc) return rc;
+    MF_CUDA_TRY(cudaSetDevice(k->ctx->device));
+    return coalesced_reduce(k, in, stride, n, params, n_params, sums);
+  }
+  return reduce_direct(k, in, stride, n, params, n_params, sums);
+}
+
+}  // extern "C"
+
+static int reduce_direct(mf_kernel* k, const mf_buffer* in, uint64_t stride, uint64_t n, const double* params,
+                         uint32_t n_params, double* sums) {
   if (!k || !sums) return fail(MF_ERR_INVALID, "null argument");
   if (k->kind != MF_KERNEL_REDUCE) return fail(MF_ERR_INVALID, "kernel is not a REDUCE kernel");
   if (n_params != k->n_params || (n_params && !params))
@@ -1475,8 +1504,10 @@ int mf_kernel_reduce(mf_kernel* k, const mf_buffer* in, uint64_t stride, uint64_
   rc = f64_twin(k);
   if (rc) return rc;
   k->fallbacks++;
-  return mf_kernel_reduce(k->f64, in, stride, n, params, n_params, sums);
+  return reduce_direct(k->f64, in, stride, n, params, n_params, sums);
 }
+
+extern "C" {
 
 int mf_kernel_reduce_async(mf_kernel* k, const mf_buffer* in, uint64_t stride, uint64_t n, const double* params,
                            uint32_t n_params, mf_buffer* out, uint64_t out_index) {
@@ -1779,6 +1810,462 @@ int mf_kernel_generate_segments(mf_kernel* k, const uint32_t* seeds, uint32_t nt
   const unsigned st = *c->status_host;
   *c->status_host = 0u;
   if (st) return fail(MF_ERR_TIMEOUT, "generation gave up after max_tries proposals in at least one thread");
+  return MF_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------- many datasets per launch --
+namespace mfi {
+
+constexpr uint64_t kMultiChunk = 2048;  // events per segment of a _multi launch (8 per thread)
+
+struct MultiSeg {  // the generated sources' mf_seg
+  const void* data;
+  uint64_t stride, first;
+  uint32_t count, req, row, pad;
+};
+static_assert(sizeof(MultiSeg) == 40, "mf_seg layout");
+
+// One evaluation of a multi-dataset launch.
+struct MultiItem {
+  mf_kernel* k;          // built from the launch's source: its argument layout
+  const void* data;      // the columns the kernel reads (prepared when it reads prepared columns)
+  uint64_t stride, n;    // n >= 1
+  const double* params;  // k->n_params values
+};
+
+uint64_t multi_segments(uint64_t n) { return std::max<uint64_t>(1, (n + kMultiChunk - 1) / kMultiChunk); }
+
+size_t round16(size_t b) { return (b + 15) / 16 * 16; }
+
+// Host staging bytes launch_multi needs for `items`: the segment table, one
+// argument struct per item, and the per-item segment counts.
+size_t multi_table_bytes(const mf_kernel* k, const std::vector<MultiItem>& items) {
+  uint64_t nseg = 0;
+  for (const auto& it : items) nseg += multi_segments(it.n);
+  return round16(size_t(nseg) * sizeof(MultiSeg)) + round16(items.size() * k->lowered.args_bytes()) +
+         round16(items.size() * sizeof(unsigned));
+}
+
+// Enqueues on c's stream one _multi launch over every segment of every item
+// and one _combine launch (one block per item) that writes item e's sums to
+// out[e * n_outputs ...] (device-visible memory). Every item's kernel is
+// built from k0's source. `host` is staging of multi_table_bytes() bytes that
+// stays untouched until the stream has executed the table copy. Segment s of
+// an item covers its events [s * kMultiChunk, ...): an item's sums depend on
+// nothing but its own events, parameters and size.
+int launch_multi(mf_context* c, mf_kernel* k0, const std::vector<MultiItem>& items, unsigned char* host,
+                 double* out) {
+  if (items.empty()) return MF_OK;
+  const size_t ab = k0->lowered.args_bytes();
+  uint64_t nseg = 0, pmax = 1;
+  for (const auto& it : items) {
+    nseg += multi_segments(it.n);
+    pmax = std::max(pmax, multi_segments(it.n));
+  }
+  if (nseg > 0x7fffffffu) return fail(MF_ERR_INVALID, "too many segments in one launch");
+  const size_t b_seg = round16(size_t(nseg) * sizeof(MultiSeg)), b_args = round16(items.size() * ab);
+  const size_t b_grid = round16(items.size() * sizeof(unsigned));
+  auto* segs = reinterpret_cast<MultiSeg*>(host);
+  unsigned char* args = host + b_seg;
+  auto* grids = reinterpret_cast<unsigned*>(host + b_seg + b_args);
+  uint64_t q = 0;
+  for (size_t e = 0; e < items.size(); e++) {
+    const MultiItem& it = items[e];
+    const uint64_t ns = multi_segments(it.n);
+    for (uint64_t s = 0; s < ns; s++, q++) {
+      const uint64_t first = s * kMultiChunk;
+      segs[q] = MultiSeg{it.data, it.stride, first, uint32_t(std::min<uint64_t>(kMultiChunk, it.n - first)),
+                         uint32_t(e), uint32_t(e * pmax + s), 0u};
+    }
+    grids[e] = unsigned(ns);
+    try {
+      it.k->lowered.fill_args(it.params, it.k->n_params, args + e * ab);
+    } catch (const std::exception& ex) {
+      return fail(MF_ERR_INVALID, std::string("parameter evaluation: ") + ex.what());
+    }
+  }
+  int rc = ensure_stage(c, b_seg + b_args + b_grid);
+  if (rc) return rc;
+  const uint64_t need = uint64_t(items.size()) * pmax * k0->n_outputs;  // float2 partial rows
+  if (c->ring_cap < need) {
+    if (c->ring) {
+      MF_CUDA_TRY(cudaStreamSynchronize(c->stream));
+      cudaFree(c->ring);
+    }
+    c->ring = nullptr;
+    c->ring_cap = 0;
+    const uint64_t cap = std::max<uint64_t>(need + need / 2, uint64_t(1) << 16);
+    MF_CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&c->ring), size_t(cap) * sizeof(float2)));
+    c->ring_cap = size_t(cap);
+  }
+  MF_CUDA_TRY(cudaMemcpyAsync(c->stage_dev, host, b_seg + b_args + b_grid, cudaMemcpyHostToDevice, c->stream));
+  char* base = static_cast<char*>(c->stage_dev);
+  const void* d_segs = base;
+  const void* d_args = base + b_seg;
+  const unsigned* d_grids = reinterpret_cast<const unsigned*>(base + b_seg + b_args);
+  float2* ring = c->ring;
+  void* margs[] = {const_cast<void**>(&d_segs), const_cast<void**>(&d_args), &ring};
+  MF_CUDA_TRY(cudaLaunchKernel(reinterpret_cast<const void*>(k0->fn_multi), dim3(unsigned(nseg)),
+                               dim3(k0->lowered.block), margs, 0, c->stream));
+  const float2* cring = ring;
+  uint64_t pstride = pmax * k0->n_outputs;
+  unsigned count = unsigned(items.size());
+  void* cargs[] = {const_cast<float2**>(&cring), &pstride, const_cast<unsigned**>(&d_grids), &out, &count};
+  MF_CUDA_TRY(cudaLaunchKernel(reinterpret_cast<const void*>(k0->fn_combine), dim3(count), dim3(k0->lowered.block),
+                               cargs, 0, c->stream));
+  return MF_OK;
+}
+
+}  // namespace mfi
+
+// ---------------------------------------------------------------- coalescer --
+// Synchronous evaluations from many host threads (each with its own context,
+// e.g. one fitter and its CUDABlocks per thread) gathered into shared launches.
+namespace {
+
+struct CoalReq {
+  mf_kernel* k = nullptr;
+  const void* data = nullptr;
+  uint64_t stride = 0, n = 0;
+  const double* params = nullptr;
+  double* sums = nullptr;      // host destination, k->n_outputs doubles
+  std::vector<double> owned;   // asynchronous submissions: params, then sums
+  std::atomic<int> state{0};   // 0 pending, 1 done, 2 failed
+  std::string error;
+};
+
+}  // namespace
+
+struct mf_coalescer {
+  int device = 0;
+  mf_context* ctx = nullptr;  // the dispatch stream and its scratch
+  uint32_t max_batch = 256;
+  uint32_t window_us = 30;
+  std::mutex mu;
+  std::condition_variable cv, done_cv;
+  std::deque<CoalReq*> pending;
+  std::map<uint64_t, std::unique_ptr<CoalReq>> tickets;
+  uint64_t next_ticket = 1;
+  int clients = 0;
+  bool stop = false;
+  std::thread worker;
+  std::atomic<uint64_t> ticks{0}, evaluations{0};
+  std::atomic<uint32_t> max_seen{0};
+  double* out_host = nullptr;
+  double* out_dev = nullptr;
+  size_t out_cap = 0;  // doubles
+  unsigned char* tables = nullptr;
+  size_t tables_cap = 0;
+};
+
+namespace {
+
+// Sets every request of the batch to failed with the current error message.
+void coal_fail_all(std::vector<CoalReq*>& batch, const std::string& msg) {
+  for (auto* r : batch) {
+    r->error = msg;
+    r->state.store(2, std::memory_order_release);
+  }
+}
+
+// Launches one tick: the batch grouped by kernel source (one _multi and one
+// _combine launch per group, all on the dispatch stream), then waits for the
+// stream and hands each request its sums.
+void coal_execute(mf_coalescer* co, std::vector<CoalReq*>& batch) {
+  mf_context* c = co->ctx;
+  std::map<const CompiledImage*, std::vector<size_t>> groups;
+  size_t nout_total = 0;
+  for (size_t i = 0; i < batch.size(); i++) {
+    groups[batch[i]->k->image.get()].push_back(i);
+    nout_total += batch[i]->k->n_outputs;
+  }
+  std::vector<std::vector<mfi::MultiItem>> items(groups.size());
+  size_t table_bytes = 0, g = 0;
+  for (auto& [img, idx] : groups) {
+    for (size_t i : idx) {
+      CoalReq* r = batch[i];
+      items[g].push_back(mfi::MultiItem{r->k, r->data, r->stride, r->n, r->params});
+    }
+    table_bytes += mfi::round16(mfi::multi_table_bytes(items[g][0].k, items[g]));
+    g++;
+  }
+  auto cuda_fail = [&](const char* what, cudaError_t e) {
+    coal_fail_all(batch, std::string(what) + ": " + cudaGetErrorString(e));
+  };
+  if (nout_total > co->out_cap) {
+    if (co->out_host) cudaFreeHost(co->out_host);
+    co->out_host = nullptr;
+    co->out_cap = 0;
+    const size_t cap = std::max<size_t>(nout_total * 2, 4096);
+    cudaError_t e = cudaHostAlloc(reinterpret_cast<void**>(&co->out_host), cap * sizeof(double), cudaHostAllocMapped);
+    if (e == cudaSuccess) e = cudaHostGetDevicePointer(reinterpret_cast<void**>(&co->out_dev), co->out_host, 0);
+    if (e != cudaSuccess) return cuda_fail("cudaHostAlloc", e);
+    co->out_cap = cap;
+  }
+  if (table_bytes > co->tables_cap) {
+    if (co->tables) cudaFreeHost(co->tables);
+    co->tables = nullptr;
+    co->tables_cap = 0;
+    const size_t cap = std::max<size_t>(table_bytes * 2, 1 << 16);
+    cudaError_t e = cudaHostAlloc(reinterpret_cast<void**>(&co->tables), cap, cudaHostAllocDefault);
+    if (e != cudaSuccess) return cuda_fail("cudaHostAlloc", e);
+    co->tables_cap = cap;
+  }
+  // Each group stages its tables from its own range of the pinned buffer and
+  // writes its outputs to its own range of the mapped results; the device
+  // stage buffer and partial rows are reused group after group, which stream
+  // order makes safe (a group's table copy runs after the previous group's
+  // kernels).
+  size_t toff = 0, ooff = 0;
+  g = 0;
+  std::vector<size_t> out_off(batch.size());
+  for (auto& [img, idx] : groups) {
+    for (size_t j = 0; j < idx.size(); j++) out_off[idx[j]] = ooff + j * batch[idx[0]]->k->n_outputs;
+    const int rc = mfi::launch_multi(c, items[g][0].k, items[g], co->tables + toff, co->out_dev + ooff);
+    if (rc) return coal_fail_all(batch, mf_last_error());
+    toff += mfi::round16(mfi::multi_table_bytes(items[g][0].k, items[g]));
+    ooff += idx.size() * batch[idx[0]]->k->n_outputs;
+    g++;
+  }
+  const cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_fail("cudaStreamSynchronize", e);
+  for (size_t i = 0; i < batch.size(); i++) {
+    CoalReq* r = batch[i];
+    std::memcpy(r->sums, co->out_host + out_off[i], r->k->n_outputs * sizeof(double));
+    r->state.store(1, std::memory_order_release);
+  }
+  co->ticks++;
+  co->evaluations += batch.size();
+  uint32_t m = co->max_seen.load();
+  while (batch.size() > m && !co->max_seen.compare_exchange_weak(m, uint32_t(batch.size()))) {}
+}
+
+void coal_worker(mf_coalescer* co) {
+  cudaSetDevice(co->device);
+  std::vector<CoalReq*> batch;
+  for (;;) {
+    {
+      std::unique_lock<std::mutex> lk(co->mu);
+      co->cv.wait(lk, [&] { return co->stop || !co->pending.empty(); });
+      if (co->pending.empty()) return;  // stopping, nothing left
+      // gather: until every attached context has a request waiting, the batch
+      // is full, or the window since this wake-up has passed
+      const auto deadline = std::chrono::steady_clock::now() + std::chrono::microseconds(co->window_us);
+      while (!co->stop && co->pending.size() < co->max_batch && int(co->pending.size()) < co->clients)
+        if (co->cv.wait_until(lk, deadline) == std::cv_status::timeout) break;
+      batch.clear();
+      while (!co->pending.empty() && batch.size() < co->max_batch) {
+        batch.push_back(co->pending.front());
+        co->pending.pop_front();
+      }
+    }
+    coal_execute(co, batch);
+    { std::lock_guard<std::mutex> lk(co->mu); }
+    co->done_cv.notify_all();
+  }
+}
+
+void coal_push(mf_coalescer* co, CoalReq* r) {
+  {
+    std::lock_guard<std::mutex> lk(co->mu);
+    co->pending.push_back(r);
+  }
+  co->cv.notify_one();
+}
+
+// Waits for request r: a short spin (a tick often completes within it), then blocks.
+void coal_wait(mf_coalescer* co, CoalReq* r) {
+  const auto t0 = std::chrono::steady_clock::now();
+  while (r->state.load(std::memory_order_acquire) == 0) {
+    if (std::chrono::steady_clock::now() - t0 > std::chrono::microseconds(50)) {
+      std::unique_lock<std::mutex> lk(co->mu);
+      co->done_cv.wait(lk, [&] { return r->state.load(std::memory_order_acquire) != 0; });
+      break;
+    }
+  }
+}
+
+// Fills a request for kernel k over buffer `in`: the columns it reads (its
+// prepared copy, made on the requester's stream) and the requester's stream
+// drained, so that the dispatch stream sees every upload and preparation.
+int coal_prepare(mf_kernel* k, const mf_buffer* in, uint64_t stride, uint64_t n, CoalReq* r) {
+  const void* data = nullptr;
+  int rc = prepare_input(k, in, stride, &data);
+  if (rc) return rc;
+  mf_context* c = k->ctx;
+  if (cudaStreamQuery(c->stream) != cudaSuccess) {
+    cudaGetLastError();  // cudaErrorNotReady is a state, not an error
+    MF_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  }
+  r->k = k;
+  r->data = data;
+  r->stride = stride;
+  r->n = n;
+  return MF_OK;
+}
+
+}  // namespace
+
+// mf_kernel_reduce for a context with a coalescer: the evaluation joins the
+// coalescer's next tick; a non-finite double-float sum is evaluated again on
+// this context in native FP64, not coalesced.
+int coalesced_reduce(mf_kernel* k, const mf_buffer* in, uint64_t stride, uint64_t n, const double* params,
+                     uint32_t n_params, double* sums) {
+  mf_coalescer* co = k->ctx->coalescer;
+  CoalReq r;
+  int rc = coal_prepare(k, in, stride, n, &r);
+  if (rc) return rc;
+  r.params = params;
+  r.sums = sums;
+  coal_push(co, &r);
+  coal_wait(co, &r);
+  if (r.state.load() == 2) return fail(MF_ERR_CUDA, "coalesced evaluation: " + r.error);
+  if (!k->desc || all_finite(sums, k->n_outputs)) return MF_OK;
+  rc = f64_twin(k);
+  if (rc) return rc;
+  k->fallbacks++;
+  return reduce_direct(k->f64, in, stride, n, params, n_params, sums);
+}
+
+extern "C" {
+
+int mf_kernel_reduce_multi(mf_kernel* k, uint32_t count, const mf_buffer* const* inputs, const uint64_t* strides,
+                           const uint64_t* ns, const double* params, uint32_t n_params, mf_buffer* out) {
+  if (!k || !inputs || !strides || !ns || !out || (n_params && !params)) return fail(MF_ERR_INVALID, "null argument");
+  if (k->kind != MF_KERNEL_REDUCE) return fail(MF_ERR_INVALID, "kernel is not a REDUCE kernel");
+  if (n_params != k->n_params) return fail(MF_ERR_INVALID, "parameter count mismatch");
+  if (uint64_t(count) * k->n_outputs * sizeof(double) > out->size)
+    return fail(MF_ERR_INVALID, "output buffer smaller than count x outputs");
+  if (count == 0) return MF_OK;
+  mf_context* c = k->ctx;
+  MF_CUDA_TRY(cudaSetDevice(c->device));
+  std::vector<mfi::MultiItem> items(count);
+  for (uint32_t i = 0; i < count; i++) {
+    int rc = check_layout(k, inputs[i], strides[i], ns[i]);
+    if (rc) return rc;
+    if (ns[i] == 0) return fail(MF_ERR_INVALID, "evaluation with no events");
+    const void* data = nullptr;
+    rc = prepare_input(k, inputs[i], strides[i], &data);
+    if (rc) return rc;
+    items[i] = mfi::MultiItem{k, data, strides[i], ns[i], params + uint64_t(i) * n_params};
+  }
+  // pageable staging: cudaMemcpyAsync has copied it when it returns
+  std::vector<unsigned char> host(mfi::multi_table_bytes(k, items));
+  return mfi::launch_multi(c, k, items, host.data(), static_cast<double*>(out->ptr));
+}
+
+int mf_coalescer_create(int device, uint32_t max_batch, uint32_t window_us, mf_coalescer** out) {
+  if (!out) return fail(MF_ERR_INVALID, "out is null");
+  *out = nullptr;
+  auto co = std::make_unique<mf_coalescer>();
+  int rc = mf_context_create(device, 0, &co->ctx);
+  if (rc) return rc;
+  co->device = device;
+  co->max_batch = max_batch ? max_batch : 256;
+  co->window_us = window_us;
+  try {
+    co->worker = std::thread(coal_worker, co.get());
+  } catch (const std::exception& e) {
+    mf_context_destroy(co->ctx);
+    return fail(MF_ERR_INVALID, std::string("cannot start the dispatch thread: ") + e.what());
+  }
+  *out = co.release();
+  return MF_OK;
+}
+
+int mf_coalescer_destroy(mf_coalescer* co) {
+  if (!co) return MF_OK;
+  {
+    std::lock_guard<std::mutex> lk(co->mu);
+    if (co->clients > 0) return fail(MF_ERR_INVALID, "contexts are still attached to the coalescer");
+    co->stop = true;
+  }
+  co->cv.notify_all();
+  co->worker.join();
+  if (co->out_host) cudaFreeHost(co->out_host);
+  if (co->tables) cudaFreeHost(co->tables);
+  mf_context_destroy(co->ctx);
+  delete co;
+  return MF_OK;
+}
+
+int mf_context_set_coalescer(mf_context* c, mf_coalescer* co) {
+  if (!c) return fail(MF_ERR_INVALID, "null context");
+  if (co && co->device != c->device) return fail(MF_ERR_INVALID, "coalescer and context are on different devices");
+  if (c->coalescer == co) return MF_OK;
+  if (c->coalescer) {
+    std::lock_guard<std::mutex> lk(c->coalescer->mu);
+    c->coalescer->clients--;
+  }
+  c->coalescer = co;
+  if (co) {
+    std::lock_guard<std::mutex> lk(co->mu);
+    co->clients++;
+  }
+  return MF_OK;
+}
+
+int mf_coalesced_submit(mf_coalescer* co, mf_kernel* k, const mf_buffer* in, uint64_t stride, uint64_t n,
+                        const double* params, uint32_t n_params, uint64_t* ticket) {
+  if (!co || !k || !ticket || (n_params && !params)) return fail(MF_ERR_INVALID, "null argument");
+  if (k->kind != MF_KERNEL_REDUCE) return fail(MF_ERR_INVALID, "kernel is not a REDUCE kernel");
+  if (n_params != k->n_params) return fail(MF_ERR_INVALID, "parameter count mismatch");
+  if (k->ctx->device != co->device) return fail(MF_ERR_INVALID, "kernel and coalescer are on different devices");
+  int rc = check_layout(k, in, stride, n);
+  if (rc) return rc;
+  if (n == 0) return fail(MF_ERR_INVALID, "evaluation with no events");
+  MF_CUDA_TRY(cudaSetDevice(k->ctx->device));
+  auto r = std::make_unique<CoalReq>();
+  rc = coal_prepare(k, in, stride, n, r.get());
+  if (rc) return rc;
+  r->owned.assign(params, params + n_params);
+  r->owned.resize(size_t(n_params) + k->n_outputs, 0.0);
+  r->params = r->owned.data();
+  r->sums = r->owned.data() + n_params;
+  CoalReq* raw = r.get();
+  {
+    std::lock_guard<std::mutex> lk(co->mu);
+    *ticket = co->next_ticket++;
+    co->tickets.emplace(*ticket, std::move(r));
+    co->pending.push_back(raw);
+  }
+  co->cv.notify_one();
+  return MF_OK;
+}
+
+int mf_coalesced_poll(mf_coalescer* co, uint64_t ticket, double* sums, int wait) {
+  if (!co || !sums) return fail(MF_ERR_INVALID, "null argument");
+  CoalReq* r = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(co->mu);
+    auto it = co->tickets.find(ticket);
+    if (it == co->tickets.end()) return fail(MF_ERR_INVALID, "unknown ticket");
+    r = it->second.get();
+  }
+  if (r->state.load(std::memory_order_acquire) == 0) {
+    if (!wait) return MF_ERR_NOT_READY;
+    coal_wait(co, r);
+  }
+  const int st = r->state.load();
+  std::unique_ptr<CoalReq> owned;
+  {
+    std::lock_guard<std::mutex> lk(co->mu);
+    auto it = co->tickets.find(ticket);
+    owned = std::move(it->second);
+    co->tickets.erase(it);
+  }
+  if (st == 2) return fail(MF_ERR_CUDA, "coalesced evaluation: " + owned->error);
+  std::memcpy(sums, owned->sums, owned->k->n_outputs * sizeof(double));
+  return MF_OK;
+}
+
+int mf_coalescer_stats(const mf_coalescer* co, uint64_t* ticks, uint64_t* evaluations, uint32_t* max_batch) {
+  if (!co) return fail(MF_ERR_INVALID, "null coalescer");
+  if (ticks) *ticks = co->ticks.load();
+  if (evaluations) *evaluations = co->evaluations.load();
+  if (max_batch) *max_batch = co->max_seen.load();
   return MF_OK;
 }
 

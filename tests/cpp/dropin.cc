@@ -6,20 +6,24 @@
 //   dropin lower <workload>                print the CUDA C the backend generates
 //                                          for every kernel the reference's
 //                                          fitter requests (no GPU needed)
-//   dropin fit <workload> <events.f64> [f32]
+//   dropin fit <workload> <events.f64> [f32|mixed]
 //                                          fit the events of a raw SoA file
 //                                          (ndims x n doubles) with the
 //                                          reference's fitter + Minuit2 MIGRAD
 //                                          and HESSE over CUDABlock<double> (or
-//                                          CUDABlock<float> with f32); prints
-//                                          one JSON line
+//                                          CUDABlock<float> with f32, or
+//                                          CUDABlock<double> with FP32 events
+//                                          and arithmetic inside with mixed);
+//                                          prints one JSON line
 //   dropin genfit <workload> <n> [f32]     generate n events on the GPU with the
 //                                          reference's generator (accelerator
 //                                          partition, seed 229387429), then fit
-//   dropin threads <workload> <nthreads> <events.f64> [f32]
-//                                          nthreads host threads, each with its
-//                                          own fitter and CUDABlocks fitting its
-//                                          own copy of the events, at once
+//   dropin threads <workload> <coalesce|plain|serial> <f64|mixed> <events.f64>...
+//                                          one host thread per event file, each
+//                                          with its own fitter, CUDABlocks and
+//                                          backend fitting that file, at once
+//                                          (one thread after another: serial),
+//                                          through a shared coalescer or not
 #define MOREFIT_H 1
 #include <atomic>
 #include <cassert>
@@ -108,7 +112,34 @@ struct FitResult {
   double first_ms = 0, warm_ms = 0;
   int cov_status = -1;
   bool ok = false;
+  // |Newton step to the minimum of the fitted function| / error, per parameter,
+  // at the fitted point (the fitter's own gradient and Hessian): how far MIGRAD
+  // stopped from the minimum of the function it minimised
+  std::vector<double> newton_sigma;
 };
+
+// Solves h x = g (h: n x n, row major) by Gaussian elimination with partial pivoting.
+static std::vector<double> solve(std::vector<double> h, std::vector<double> g, size_t n) {
+  for (size_t c = 0; c < n; c++) {
+    size_t p = c;
+    for (size_t r = c + 1; r < n; r++)
+      if (std::fabs(h[r * n + c]) > std::fabs(h[p * n + c])) p = r;
+    for (size_t k = 0; k < n; k++) std::swap(h[c * n + k], h[p * n + k]);
+    std::swap(g[c], g[p]);
+    for (size_t r = c + 1; r < n; r++) {
+      const double f = h[r * n + c] / h[c * n + c];
+      for (size_t k = c; k < n; k++) h[r * n + k] -= f * h[c * n + k];
+      g[r] -= f * g[c];
+    }
+  }
+  std::vector<double> x(n);
+  for (size_t c = n; c-- > 0;) {
+    double v = g[c];
+    for (size_t k = c + 1; k < n; k++) v -= h[c * n + k] * x[k];
+    x[c] = v / h[c * n + c];
+  }
+  return x;
+}
 
 // Discards what is written to it; no state, so several threads may write at once.
 struct NullBuf : std::streambuf {
@@ -144,6 +175,14 @@ static FitResult fit_events(CUDABackend& backend, const std::string& which, cons
     r.values.push_back(p->get_value());
     r.errors.push_back(p->get_error());
   }
+  if (capture) {
+    const int np = int(w.params.size());
+    std::vector<double> g(np), h(size_t(np) * np);
+    fit.likelihood_and_gradient(np, g.data());
+    fit.hessian(np, h.data());
+    const std::vector<double> step = solve(h, g, size_t(np));
+    for (int i = 0; i < np; i++) r.newton_sigma.push_back(std::fabs(step[i]) / r.errors[i]);
+  }
   for (size_t i = 0; i < start.size(); i++) {
     w.params[i]->set_value(start[i]);
     w.params[i]->set_start_value(start[i]);
@@ -160,9 +199,10 @@ static FitResult fit_events(CUDABackend& backend, const std::string& which, cons
 static void print_fit(const std::string& which, unsigned n, const char* prec, uint64_t hash, const FitResult& r,
                       const char* extra = "") {
   std::printf("{\"workload\":\"%s\",\"n\":%u,\"kernelT\":\"%s\",\"events_fnv1a\":\"%016llx\",\"ok\":%s,"
-              "\"cov_status\":%d,\"first_fit_ms\":%.3f,\"fit_ms\":%.3f,\"values\":%s,\"errors\":%s%s}\n",
+              "\"cov_status\":%d,\"first_fit_ms\":%.3f,\"fit_ms\":%.3f,\"values\":%s,\"errors\":%s,"
+              "\"newton_sigma\":%s%s}\n",
               which.c_str(), n, prec, (unsigned long long)hash, r.ok ? "true" : "false", r.cov_status, r.first_ms,
-              r.warm_ms, jvec(r.values).c_str(), jvec(r.errors).c_str(), extra);
+              r.warm_ms, jvec(r.values).c_str(), jvec(r.errors).c_str(), jvec(r.newton_sigma).c_str(), extra);
 }
 
 template <typename kT>
@@ -184,9 +224,11 @@ static int cmd_lower(const std::string& which) {
 }
 
 template <typename kT>
-static int cmd_fit(const std::string& which, const std::string& path, const char* prec) {
+static int cmd_fit(const std::string& which, const std::string& path, const char* prec, bool mixed = false) {
   compute_options copts;
-  CUDABackend backend(&copts);
+  cuda_options cu;
+  cu.mixed_precision = mixed;
+  CUDABackend backend(&copts, cu);
   if (!backend.ok()) {
     std::printf("{\"skipped\":\"%s\"}\n", backend.error().c_str());
     return 3;
@@ -241,40 +283,76 @@ static int cmd_genfit(const std::string& which, unsigned n, const char* prec) {
   return r.ok ? 0 : 1;
 }
 
-// Several host threads, each with its own fitter and CUDABlocks (one fitter
-// per host thread, the reference's threading model) over one backend.
-template <typename kT>
-static int cmd_threads(const std::string& which, unsigned nthreads, const std::string& path, const char* prec) {
-  compute_options copts;
-  CUDABackend backend(&copts);
-  if (!backend.ok()) {
-    std::printf("{\"skipped\":\"%s\"}\n", backend.error().c_str());
+// Several host threads, each with its own fitter, CUDABlocks and backend
+// (context), fitting its own dataset: one fitter per host thread, the
+// reference's threading model. mode "coalesce": every backend routes its
+// synchronous evaluations through one shared coalescer; "plain": no
+// coalescer (each context launches on its own stream); "serial": one thread
+// fits the datasets one after another. Each fit is timed from the start of
+// the thread's work on it (kernel builds, upload, MIGRAD + HESSE).
+static int cmd_threads(const std::string& which, const std::string& mode, bool mixed,
+                       const std::vector<std::string>& files) {
+  Workload<double, double> w0 = make_workload<double, double>(which);
+  const size_t T = files.size();
+  std::vector<std::vector<double>> ev(T);
+  std::vector<unsigned> ns(T);
+  for (size_t t = 0; t < T; t++) ev[t] = read_events(files[t], w0.dims.size(), ns[t]);
+  mf_coalescer* co = nullptr;
+  if (mode == "coalesce" && mf_coalescer_create(0, 0, 30, &co) != MF_OK) {
+    std::printf("{\"skipped\":\"%s\"}\n", mf_last_error());
     return 3;
   }
-  Workload<double, double> w0 = make_workload<double, double>(which);
-  unsigned n = 0;
-  std::vector<double> ev = read_events(path, w0.dims.size(), n);
-  std::vector<FitResult> res(nthreads);
-  std::vector<std::thread> th;
+  std::vector<FitResult> res(T);
+  std::vector<double> latency(T);
+  std::atomic<bool> failed{false};
   NullBuf null;
   auto* old = std::cout.rdbuf(&null);
   auto t0 = std::chrono::steady_clock::now();
-  for (unsigned t = 0; t < nthreads; t++)
-    th.emplace_back([&, t]() { res[t] = fit_events<kT>(backend, which, ev, n, false); });
-  for (auto& x : th) x.join();
+  auto one = [&](size_t t) {
+    compute_options copts;
+    cuda_options cu;
+    cu.mixed_precision = mixed;
+    cu.coalescer = co;
+    cu.quiet = true;
+    CUDABackend backend(&copts, cu);
+    if (!backend.ok()) {
+      failed = true;
+      return;
+    }
+    auto a = std::chrono::steady_clock::now();
+    res[t] = fit_events<double>(backend, which, ev[t], ns[t], false);
+    latency[t] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - a).count();
+  };
+  if (mode == "serial") {
+    for (size_t t = 0; t < T; t++) one(t);
+  } else {
+    std::vector<std::thread> th;
+    for (size_t t = 0; t < T; t++) th.emplace_back(one, t);
+    for (auto& x : th) x.join();
+  }
   auto t1 = std::chrono::steady_clock::now();
   std::cout.rdbuf(old);
-  const uint64_t h = fnv1a(ev.data(), ev.size() * sizeof(double));
-  std::printf("{\"workload\":\"%s\",\"n\":%u,\"kernelT\":\"%s\",\"nthreads\":%u,\"events_fnv1a\":\"%016llx\","
-              "\"wall_ms\":%.3f,\"fits\":[",
-              which.c_str(), n, prec, nthreads, (unsigned long long)h,
-              std::chrono::duration<double, std::milli>(t1 - t0).count());
+  uint64_t ticks = 0, evals = 0;
+  uint32_t maxb = 0;
+  if (co) {
+    mf_coalescer_stats(co, &ticks, &evals, &maxb);
+    mf_coalescer_destroy(co);
+  }
+  if (failed) {
+    std::printf("{\"skipped\":\"no CUDA context\"}\n");
+    return 3;
+  }
+  std::printf("{\"workload\":\"%s\",\"mode\":\"%s\",\"mixed\":%s,\"nthreads\":%zu,\"wall_ms\":%.3f,"
+              "\"coalescer\":{\"ticks\":%llu,\"evaluations\":%llu,\"max_batch\":%u},\"fits\":[",
+              which.c_str(), mode.c_str(), mixed ? "true" : "false", T,
+              std::chrono::duration<double, std::milli>(t1 - t0).count(), (unsigned long long)ticks,
+              (unsigned long long)evals, maxb);
   bool ok = true;
-  for (unsigned t = 0; t < nthreads; t++) {
+  for (size_t t = 0; t < T; t++) {
     ok = ok && res[t].ok;
-    std::printf("%s{\"ok\":%s,\"cov_status\":%d,\"fit_ms\":%.3f,\"values\":%s,\"errors\":%s}", t ? "," : "",
-                res[t].ok ? "true" : "false", res[t].cov_status, res[t].warm_ms, jvec(res[t].values).c_str(),
-                jvec(res[t].errors).c_str());
+    std::printf("%s{\"n\":%u,\"ok\":%s,\"latency_ms\":%.3f,\"fit_ms\":%.3f,\"values\":%s,\"errors\":%s}",
+                t ? "," : "", ns[t], res[t].ok ? "true" : "false", latency[t], res[t].warm_ms,
+                jvec(res[t].values).c_str(), jvec(res[t].errors).c_str());
   }
   std::printf("]}\n");
   return ok ? 0 : 1;
@@ -286,8 +364,9 @@ int main(int argc, char** argv) {
   // Minuit2 default (0.01), as the reference's drivers run.
   if (const char* t = std::getenv("MOREFIT_MINUIT_TOLERANCE")) ROOT::Math::MinimizerOptions::SetDefaultTolerance(std::atof(t));
   const std::string usage =
-      "usage: dropin lower <workload> | dropin fit <workload> <events.f64> [f32] | "
-      "dropin genfit <workload> <n> [f32] | dropin threads <workload> <nthreads> <events.f64> [f32]\n";
+      "usage: dropin lower <workload> | dropin fit <workload> <events.f64> [f32|mixed] | "
+      "dropin genfit <workload> <n> [f32] | "
+      "dropin threads <workload> <coalesce|plain|serial> <f64|mixed> <events.f64>...\n";
   if (argc < 3) {
     std::fprintf(stderr, "%s", usage.c_str());
     return 2;
@@ -295,16 +374,17 @@ int main(int argc, char** argv) {
   const std::string mode = argv[1], which = argv[2];
   auto is_f32 = [&](int i) { return argc > i && std::string(argv[i]) == "f32"; };
   if (mode == "lower") return is_f32(3) ? cmd_lower<float>(which) : cmd_lower<double>(which);
-  if (mode == "fit" && argc >= 4)
+  if (mode == "fit" && argc >= 4) {
+    if (argc > 4 && std::string(argv[4]) == "mixed") return cmd_fit<double>(which, argv[3], "double, mixed", true);
     return is_f32(4) ? cmd_fit<float>(which, argv[3], "float") : cmd_fit<double>(which, argv[3], "double");
+  }
   if (mode == "genfit" && argc >= 4) {
     const unsigned n = unsigned(std::stoul(argv[3]));
     return is_f32(4) ? cmd_genfit<float>(which, n, "float") : cmd_genfit<double>(which, n, "double");
   }
-  if (mode == "threads" && argc >= 5) {
-    const unsigned t = unsigned(std::stoul(argv[3]));
-    return is_f32(5) ? cmd_threads<float>(which, t, argv[4], "float")
-                     : cmd_threads<double>(which, t, argv[4], "double");
+  if (mode == "threads" && argc >= 6) {
+    std::vector<std::string> files(argv + 5, argv + argc);
+    return cmd_threads(which, argv[3], std::string(argv[4]) == "mixed", files);
   }
   std::fprintf(stderr, "%s", usage.c_str());
   return 2;

@@ -85,7 +85,7 @@ def test_float_kernels_use_float_literals_and_functions():
     # the NLL-only kernel: the density's dot product with the parameter-only
     # factors compensated, its logarithm summed as a double-float running product
     body = _entry(_src(g, "lh_kernel", L.MF_F32), "mf_reduce(")
-    assert "mf_dw_acc_mulf(" in body and "mf_dw_logprod(" in body and "logf(" not in body
+    assert "mf_dw_acc_mulfw(" in body and "mf_dw_logprod(" in body and "logf(" not in body
     assert " exp(" not in body and " log(" not in body
 
 
