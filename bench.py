@@ -739,43 +739,24 @@ def variants(args):
                "vec": info["vec"], "block": info["block"],
                "rel_diff_vs_first": (np.abs(res - ref) / np.maximum(np.abs(ref), 1.0)).max().item()}
         if args.lone:
-            # synchronous single evaluations (the fitter's call): host time per
-            # call, and the GPU time of each lone launch from events around it
-            lk = sets[0]
-            for _ in range(20):
-                lk.sums("lh_grad_kernel", truth)
-            gpu_us, host_us = [], []
-            for i in range(max(50, K)):
-                li = sets[i % nsets]
-                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            # synchronous single evaluations (Minuit2's call): mf_kernel_reduce
+            # straight through ctypes, parameter vector and sums preallocated,
+            # rotating over the datasets; host time per call
+            sums = np.zeros(kern.nout)
+            pvc = np.ascontiguousarray(pv)
+            calls = [(sets[i].blocks["lh_grad_kernel"].input.buf, sets[i].blocks["lh_grad_kernel"].input.stride)
+                     for i in range(nsets)]
+            for i in range(min(20, args.lone_calls)):
+                buf, st = calls[i % nsets]
+                L.check(L.lib.mf_kernel_reduce(kern.handle, buf, st, n, L.dptr(pvc), len(pvc), L.dptr(sums)))
+            host_us = []
+            for i in range(args.lone_calls):
+                buf, st = calls[i % nsets]
                 t0 = time.perf_counter()
-                a.record(ext)
-                li.sums("lh_grad_kernel", truth)
-                b.record(ext)
+                L.check(L.lib.mf_kernel_reduce(kern.handle, buf, st, n, L.dptr(pvc), len(pvc), L.dptr(sums)))
                 host_us.append((time.perf_counter() - t0) * 1e6)
-                b.synchronize()
-                gpu_us.append(a.elapsed_time(b) * 1e3)
-            row["lone_gpu_us_median"] = statistics.median(gpu_us)
-            row["lone_call_us_median"] = statistics.median(host_us)
-            # the lone launch itself: a spin kernel keeps the stream busy while
-            # the host enqueues event, evaluation and event, so the events
-            # bracket the kernel (and one launch gap) without host latency
-            ob = L.c_buf()
-            L.check(L.lib.mf_buffer_alloc(backend.handle, kern.nout * 8, C.byref(ob)))
-            kus = []
-            with torch.cuda.stream(ext):
-                for i in range(max(50, K)):
-                    li = sets[i % nsets]
-                    torch.cuda._sleep(100000)
-                    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                    a.record(ext)
-                    li.sums_async("lh_grad_kernel", truth, ob, 0)
-                    b.record(ext)
-                    b.synchronize()
-                    kus.append(a.elapsed_time(b) * 1e3)
-            L.lib.mf_buffer_free(ob)
-            row["lone_kernel_us_median"] = statistics.median(kus)
-            row["lone_kernel_us_min"] = min(kus)
+            row["sync_call_us_median"] = statistics.median(host_us)
+            row["sync_call_us_p10"] = sorted(host_us)[len(host_us) // 10]
         print(json.dumps(row), flush=True)
         del sets
 
@@ -931,6 +912,7 @@ def main():
     ap.add_argument("--variant-list", default="")
     ap.add_argument("--sets", type=int, default=5)
     ap.add_argument("--lone", action="store_true", help="with --variants: also time synchronous single evaluations")
+    ap.add_argument("--lone-calls", type=int, default=200)
     args = ap.parse_args()
     if args.warmup < 3 and not args.variants:
         args.warmup = 3

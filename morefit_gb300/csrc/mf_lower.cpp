@@ -1121,8 +1121,12 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
   for (size_t j = 0; j < exprs.size(); j++) s << "//   [" << j << "] " << exprs[j].substr(0, 160) << "\n";
   s << kPrelude;
   s << "#define MF_BLOCK " << out.block << "\n#define MF_NOUT " << M << "\n#define MF_NPAR " << NP << "\n";
+  // launch bounds of the event-loop entries
+  s << "#define MF_BOUNDS __launch_bounds__(MF_BLOCK)\n";
   // partial blocks each last-block thread loads per round (bounded register use)
-  s << "#define MF_Q " << std::max(1, 32 / std::max(1, M)) << "\n";
+  // combine of block partial rows: MF_CC outputs at a time, MF_Q rows of each in flight per thread
+  s << "#define MF_CC " << std::min(M, 8) << "\n";
+  s << "#define MF_Q " << std::max(1, 8 / std::max(1, std::min(M, 8))) << "\n";
   // outputs per block-reduction chunk (one warp each)
   s << "#define MF_RC " << std::max(1, std::min(8, out.block / 32)) << "\n";
   s << "struct mf_par { double v[MF_NPAR]; };\n";
@@ -1741,7 +1745,7 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
 
     s << "struct mf_args { double d[" << out.nd << "]; float f[" << out.nf << "]; };\n";
     // ---- single-dataset reduce ----
-    s << "extern \"C\" __global__ void __launch_bounds__(MF_BLOCK) " << out.entry << "(const " << DT
+    s << "extern \"C\" __global__ void MF_BOUNDS " << out.entry << "(const " << DT
       << "* __restrict__ data, mf_u64 stride, mf_u64 n, mf_args P, float2* __restrict__ partials,"
       << " unsigned* __restrict__ counter, double* __restrict__ out, unsigned* __restrict__ status, unsigned seq) {\n";
     const auto body_mark = s.tellp();
@@ -1848,30 +1852,37 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
     // loads of a round issued before the adds), then a warp tree and a pass
     // over the warps in order. The order depends only on mf_nb, the grid size
     // of the evaluation. Uses red[][], lane and warp.
+    // Outputs are combined MF_CC at a time (registers O(MF_CC), not
+    // O(MF_NOUT)); within each output the order is the one above, so the
+    // chunking changes no result.
     const std::string combine_text = R"CUDA(  {
-    mf_dw s[MF_NOUT];
+    for (int j0 = 0; j0 < MF_NOUT; j0 += MF_CC) {
+      mf_dw s[MF_CC];
 #pragma unroll
-    for (int j = 0; j < MF_NOUT; j++) s[j] = mf_dw_make(0.0f, 0.0f);
-    for (unsigned b0 = 0; b0 < mf_nb; b0 += MF_Q * MF_BLOCK) {
-      float2 v[MF_Q][MF_NOUT];
+      for (int c = 0; c < MF_CC; c++) s[c] = mf_dw_make(0.0f, 0.0f);
+      for (unsigned b0 = 0; b0 < mf_nb; b0 += MF_Q * MF_BLOCK) {
+        float2 v[MF_Q][MF_CC];
 #pragma unroll
-      for (int q = 0; q < MF_Q; q++) {
-        const unsigned b = b0 + q * MF_BLOCK + threadIdx.x;
+        for (int q = 0; q < MF_Q; q++) {
+          const unsigned b = b0 + q * MF_BLOCK + threadIdx.x;
 #pragma unroll
-        for (int j = 0; j < MF_NOUT; j++)
-          v[q][j] = b < mf_nb ? __ldcg(partials + (mf_u64)b * MF_NOUT + j) : make_float2(0.0f, 0.0f);
+          for (int c = 0; c < MF_CC; c++)
+            v[q][c] = (b < mf_nb && j0 + c < MF_NOUT) ? __ldcg(partials + (mf_u64)b * MF_NOUT + j0 + c)
+                                                        : make_float2(0.0f, 0.0f);
+        }
+#pragma unroll
+        for (int q = 0; q < MF_Q; q++)
+#pragma unroll
+          for (int c = 0; c < MF_CC; c++) s[c] = mf_dw_add(s[c], mf_dw_make(v[q][c].x, v[q][c].y));
       }
 #pragma unroll
-      for (int q = 0; q < MF_Q; q++)
+      for (int c = 0; c < MF_CC; c++) {
+        if (j0 + c >= MF_NOUT) break;
+        mf_dw a = s[c];
 #pragma unroll
-        for (int j = 0; j < MF_NOUT; j++) s[j] = mf_dw_add(s[j], mf_dw_make(v[q][j].x, v[q][j].y));
-    }
-#pragma unroll
-    for (int j = 0; j < MF_NOUT; j++) {
-      mf_dw a = s[j];
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) a = mf_dw_add(a, mf_dw_shfl_xor(a, o));
-      if (lane == 0) red[j][warp] = make_float2(a.h, a.l);
+        for (int o = 16; o > 0; o >>= 1) a = mf_dw_add(a, mf_dw_shfl_xor(a, o));
+        if (lane == 0) red[j0 + c][warp] = make_float2(a.h, a.l);
+      }
     }
     __syncthreads();
     for (int j = threadIdx.x; j < MF_NOUT; j += MF_BLOCK) {
@@ -1912,7 +1923,7 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
     // its own work); <entry>_combine then reduces every evaluation's rows
     // (one block each, the same fixed order: the sums equal the
     // single-evaluation entry's).
-    s << "extern \"C\" __global__ void __launch_bounds__(MF_BLOCK) " << out.entry << "_part(const " << DT
+    s << "extern \"C\" __global__ void MF_BOUNDS " << out.entry << "_part(const " << DT
       << "* __restrict__ data, mf_u64 stride, mf_u64 n, mf_args P, float2* __restrict__ partials,"
       << " unsigned* __restrict__ status) {\n"
       << body_text

@@ -26,7 +26,7 @@ def test_shared_subexpressions_evaluated_once():
     assert body.count("= log(") == 2
     assert body.count("__drcp_rn(") == 2
     dw = _src(g, "lh_grad_kernel", L.MF_F64)
-    body = _entry(dw, "void __launch_bounds__(MF_BLOCK) mf_reduce(")
+    body = _entry(dw, "void MF_BOUNDS mf_reduce(")
     # double-float kernel: two events per thread, one reciprocal each; the
     # NLL output log(p) is summed as the log of a running product (one factor
     # per event, one logarithm per thread)
