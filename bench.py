@@ -560,6 +560,7 @@ def ours(args):
                    "capacity_over_serial": cap["fits_per_s"] / serial}
 
     extras = None if args.no_extras else extra_rows(backend)
+    fitters = None if args.no_fitters else fitter_rows(backend, host)
 
     # ---------------- CPU baseline (rank 0, N=1 only) ----------------
     cpu = None
@@ -585,12 +586,22 @@ def ours(args):
         c1_cpu = {"value": mdone / (time.perf_counter() - t0), "unit": "evals/s", "cores": nthreads, "kind": "port",
                   "sample": f"{mdone} NLL+grad evaluations of the mass model over 100k events (~3 s)"}
         nll_gpu = -2.0 * float(like.sums("lh_grad_kernel", truth)[0])
+        # the reference's whole fit (MIGRAD + HESSE) of dataset 0 on its CPU backend, one thread
+        fit_1m = None
+        kit = _refkit()
+        if kit is not None:
+            import tempfile
+            with tempfile.TemporaryDirectory() as td:
+                f0 = Path(td) / "pwave_1M.f64"
+                np.ascontiguousarray(host).tofile(f0)
+                fit_1m = _run_json([kit, "fitevents", "pwave", f0, 1])["fit_ms"]
         cpu = {"value": allc["value"], "unit": "evals/s", "cores": nthreads, "kind": allc["kind"],
                "sample": f"{allc['nevals']} NLL+grad evaluations over all {n} events of dataset 0 "
                          f"(~{args.cpu_seconds:g} s); {allc['how']}",
                "nthreads_1": {"value": one["value"], "unit": "evals/s", "cores": 1, "nevals": one["nevals"]},
                "events_fnv1a": mforacle.fnv1a(host),
-               "nll_rel_diff_vs_gpu": abs(allc["nll"] - nll_gpu) / abs(nll_gpu), "c1_mass_100k": c1_cpu}
+               "nll_rel_diff_vs_gpu": abs(allc["nll"] - nll_gpu) / abs(nll_gpu), "c1_mass_100k": c1_cpu,
+               "fit_1M_ms": fit_1m}
 
     if rank == 0:
         r3 = lambda x: None if x is None else float(f"{x:.4g}")
@@ -612,6 +623,10 @@ def ours(args):
             "serving_p99_ms": r3(serving["p99_ms"]) if serving else None,
             "serving_capacity_over_serial": r3(serving["capacity_over_serial"]) if serving else None,
             "e2e_evals_per_s": r3(world / e2e_s), "fit_loop_evals_per_s": r3(world / fit_loop_s),
+            "reference_fitter_1M_fit_ms": r3(fitters["fit_1M"]["fit_ms"]) if fitters else None,
+            "reference_fitter_threads_capacity_over_serial":
+                r3(fitters["threads_8"]["capacity_over_serial"]) if fitters else None,
+            "cpu_reference_1M_fit_ms": r3(cpu["fit_1M_ms"]) if cpu and cpu.get("fit_1M_ms") else None,
             "cpu_reference_evals_per_s": r3(cpu["value"]) if cpu else None,
             "cpu_reference_1thread_evals_per_s": r3(cpu["nthreads_1"]["value"]) if cpu else None}
         line = {"metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
@@ -641,7 +656,7 @@ def ours(args):
                 "e2e_fit_loop": {"value": world / fit_loop_s, "unit": "evals/s", "h2d_bytes_per_step": 0,
                                  "d2h_bytes_per_step": nout * 8},
                 "native_fp64": native, "mixed": mixed, "spwave_10M": spw, "toys": toys, "serving": serving,
-                "extras": extras,
+                "extras": extras, "reference_fitter": fitters,
                 "headline": headline}
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -759,6 +774,56 @@ def variants(args):
             row["sync_call_us_p10"] = sorted(host_us)[len(host_us) // 10]
         print(json.dumps(row), flush=True)
         del sets
+
+
+def _dropin():
+    p = ROOT / "tests" / "cpp" / "_build" / platform.machine() / "dropin"
+    return p if p.exists() else None
+
+
+def _run_json(cmd, env=None):
+    r = subprocess.run([str(c) for c in cmd], capture_output=True, text=True, check=True, env=env)
+    return json.loads(r.stdout.strip().splitlines()[-1])
+
+
+def fitter_rows(backend, host):
+    """The reference's own fitter + Minuit2 (MIGRAD + HESSE, analytic gradient
+    and Hessian) over the C++ drop-in's CUDABlocks (tests/cpp/dropin, built
+    where the reference sources are present): one fit of dataset 0 (1M P-wave
+    events), and eight host threads each fitting a dataset of its own
+    (20k-200k events) with their evaluations coalesced, against the same eight
+    fits one after another. None where the drop-in is not built."""
+    import tempfile
+    from morefit_gb300.workloads import generate_events, load_spec
+    d = _dropin()
+    if d is None:
+        return None
+    spec = load_spec("pwave")
+    out = {}
+    with tempfile.TemporaryDirectory() as td:
+        f0 = Path(td) / "pwave_1M.f64"
+        np.ascontiguousarray(host).tofile(f0)
+        fit = _run_json([d, "fit", "pwave", f0])
+        out["fit_1M"] = {"fit_ms": fit["fit_ms"], "first_fit_ms": fit["first_fit_ms"], "cov_status": fit["cov_status"],
+                         "events_fnv1a": fit["events_fnv1a"]}
+        files = []
+        for i, n in enumerate([20000, 50000, 100000, 200000] * 2):
+            p = Path(td) / f"pwave_{i}.f64"
+            np.ascontiguousarray(generate_events(backend, spec, n, seed=1 + i).download()).tofile(p)
+            files.append(p)
+        mix = _run_json([d, "threads", "pwave", "coalesce", "f64", *files])
+        serial = _run_json([d, "threads", "pwave", "serial", "f64", *files])
+        plain = _run_json([d, "threads", "pwave", "plain", "f64", *files])
+        lat = sorted(f["latency_ms"] for f in mix["fits"])
+        out["threads_8"] = {"coalesced_ms": mix["wall_ms"], "serial_ms": serial["wall_ms"],
+                            "threads_uncoalesced_ms": plain["wall_ms"],
+                            "capacity_over_serial": serial["wall_ms"] / mix["wall_ms"],
+                            "fit_latency_p50_ms": lat[len(lat) // 2], "fit_latency_max_ms": lat[-1],
+                            "coalescer": mix["coalescer"],
+                            "what": "8 host threads, each the reference's fitter + Minuit2 on its own P-wave dataset "
+                                    "(20k-200k events) over its own CUDABackend, evaluations coalesced; against the "
+                                    "same 8 fits one after another (kernel builds and uploads included)"}
+    return out
 
 
 def extra_rows(backend):
@@ -908,6 +973,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-native", action="store_true")
     ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--no-fitters", action="store_true")
     ap.add_argument("--variants", action="store_true", help="time every kernel variant instead")
     ap.add_argument("--variant-list", default="")
     ap.add_argument("--sets", type=int, default=5)

@@ -418,6 +418,14 @@ int mf_kernel_store_async(mf_kernel* k, const mf_buffer* input, uint64_t in_stri
 int mf_kernel_generate(mf_kernel* k, const uint32_t* seeds, uint32_t nseeds, uint64_t n, uint64_t nper,
                        const double* params, uint32_t n_params, mf_buffer* out, uint64_t out_stride,
                        uint64_t max_tries);
+/* mf_kernel_generate enqueued on the context's stream without waiting (the
+ * seeds are copied before it returns). A thread that gives up sets the
+ * context's error word, which the next synchronous REDUCE call on the context
+ * reports as MF_ERR_TIMEOUT. For admitting many datasets without host round
+ * trips (the serving loop). */
+int mf_kernel_generate_async(mf_kernel* k, const uint32_t* seeds, uint32_t nseeds, uint64_t n, uint64_t nper,
+                             const double* params, uint32_t n_params, mf_buffer* out, uint64_t out_stride,
+                             uint64_t max_tries);
 
 /* GENERATE for many datasets at once (toy studies with a different truth per
  * toy): segment s owns output events [seg_begin[s], seg_begin[s] +

@@ -147,6 +147,8 @@ _proto("mf_histogram", C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_uint64, C.c
 _proto("mf_kernel_store", C.c_int, c_ker, c_buf, C.c_uint64, C.c_uint64, c_dbl_p, C.c_uint32, c_buf, C.c_uint64)
 _proto("mf_kernel_generate", C.c_int, c_ker, C.POINTER(C.c_uint32), C.c_uint32, C.c_uint64, C.c_uint64, c_dbl_p,
        C.c_uint32, c_buf, C.c_uint64, C.c_uint64)
+_proto("mf_kernel_generate_async", C.c_int, c_ker, C.POINTER(C.c_uint32), C.c_uint32, C.c_uint64, C.c_uint64, c_dbl_p,
+       C.c_uint32, c_buf, C.c_uint64, C.c_uint64)
 _proto("mf_eval_expressions", C.c_int, C.c_uint32, c_char_pp, c_dbl_p, C.c_uint32, c_char_pp, c_dbl_p)
 _proto("mf_seed_rows", C.c_int, C.c_uint64, C.c_uint32, C.POINTER(C.c_uint32))
 _proto("mf_splitmix_seed_rows", C.c_int, C.c_uint64, C.c_uint32, C.POINTER(C.c_uint32))
@@ -198,4 +200,5 @@ def exported_symbols() -> list[str]:
         "mf_histogram", "mf_events_load_file", "mf_splitmix_seed_rows", "mf_buffer_wrap_host",
         "mf_spd_solve_batch", "mf_kernel_reduce_multi", "mf_coalescer_create", "mf_coalescer_destroy",
         "mf_context_set_coalescer", "mf_coalesced_submit", "mf_coalesced_poll", "mf_coalescer_stats",
+        "mf_kernel_generate_async",
     ]

@@ -394,8 +394,13 @@ class CUDABlock:
         elif k.kind == L.MF_KERNEL_REDUCE:
             L.check(L.lib.mf_kernel_reduce_async(k.handle, self.input.buf, self.input.stride, self.nevents,
                                                  L.dptr(p), k.nparams, out, out_index))
-        else:
-            raise ValueError("generate kernels have no asynchronous form here")
+        else:  # generate: out = events per generator thread (None: spread over the seed rows)
+            nseeds = self._seeds.shape[-1] if self._seeds.ndim == 2 else self._seeds.size // 4
+            per = out if out else -(-self.nevents // nseeds)
+            self.output.ensure(self._gen, self.nevents)
+            L.check(L.lib.mf_kernel_generate_async(k.handle, self._seeds.ctypes.data_as(C.POINTER(C.c_uint32)),
+                                                   nseeds, self.nevents, per, L.dptr(p), k.nparams, self.output.buf,
+                                                   self.output.stride, 10000 * per))
         return True
 
     def CopyToSeedBuffer(self, seeds: np.ndarray) -> bool:

@@ -1722,9 +1722,9 @@ int mf_kernel_store_async(mf_kernel* k, const mf_buffer* in, uint64_t in_stride,
   return kernel_store(k, in, in_stride, n, params, n_params, out, out_stride, false);
 }
 
-int mf_kernel_generate(mf_kernel* k, const uint32_t* seeds, uint32_t nseeds, uint64_t n, uint64_t nper,
-                       const double* params, uint32_t n_params, mf_buffer* out, uint64_t out_stride,
-                       uint64_t max_tries) {
+static int kernel_generate(mf_kernel* k, const uint32_t* seeds, uint32_t nseeds, uint64_t n, uint64_t nper,
+                           const double* params, uint32_t n_params, mf_buffer* out, uint64_t out_stride,
+                           uint64_t max_tries, bool sync) {
   if (!k || !seeds || !out) return fail(MF_ERR_INVALID, "null argument");
   if (k->kind != MF_KERNEL_GENERATE) return fail(MF_ERR_INVALID, "kernel is not a GENERATE kernel");
   if (n_params != k->n_params || (n_params && !params)) return fail(MF_ERR_INVALID, "parameter count mismatch");
@@ -1739,7 +1739,7 @@ int mf_kernel_generate(mf_kernel* k, const uint32_t* seeds, uint32_t nseeds, uin
   if (rc) return rc;
   MF_CUDA_TRY(cudaMemcpyAsync(c->stage_dev, seeds, size_t(nseeds) * 4 * sizeof(uint32_t), cudaMemcpyHostToDevice,
                               c->stream));
-  *c->status_host = 0u;
+  if (sync) *c->status_host = 0u;
   std::vector<double> pv(std::max<uint32_t>(1, k->n_params), 0.0);
   if (k->n_params) std::memcpy(pv.data(), params, k->n_params * sizeof(double));
   const unsigned* sd = static_cast<const unsigned*>(c->stage_dev);
@@ -1751,11 +1751,24 @@ int mf_kernel_generate(mf_kernel* k, const uint32_t* seeds, uint32_t nseeds, uin
   const unsigned grid = (nseeds + k->lowered.block - 1) / k->lowered.block;
   MF_CUDA_TRY(cudaLaunchKernel(reinterpret_cast<const void*>(k->fn), dim3(grid), dim3(k->lowered.block), args, 0,
                                c->stream));
+  if (!sync) return MF_OK;
   MF_CUDA_TRY(cudaStreamSynchronize(c->stream));
   const unsigned st = *c->status_host;
   *c->status_host = 0u;
   if (st) return fail(MF_ERR_TIMEOUT, "generation gave up after max_tries proposals in at least one thread");
   return MF_OK;
+}
+
+int mf_kernel_generate(mf_kernel* k, const uint32_t* seeds, uint32_t nseeds, uint64_t n, uint64_t nper,
+                       const double* params, uint32_t n_params, mf_buffer* out, uint64_t out_stride,
+                       uint64_t max_tries) {
+  return kernel_generate(k, seeds, nseeds, n, nper, params, n_params, out, out_stride, max_tries, true);
+}
+
+int mf_kernel_generate_async(mf_kernel* k, const uint32_t* seeds, uint32_t nseeds, uint64_t n, uint64_t nper,
+                             const double* params, uint32_t n_params, mf_buffer* out, uint64_t out_stride,
+                             uint64_t max_tries) {
+  return kernel_generate(k, seeds, nseeds, n, nper, params, n_params, out, out_stride, max_tries, false);
 }
 
 int mf_kernel_generate_segments(mf_kernel* k, const uint32_t* seeds, uint32_t nthreads, uint32_t threads_per_seg,

@@ -1,18 +1,20 @@
 """Serving loop: many fits at once on one GPU, their evaluations coalesced.
 
 Fit requests (a model, an event count, a seed, start values) arrive over
-time. Each admitted fit keeps its dataset on the device (generated there,
-precomputed once) and is driven by a host-side variable-metric minimiser
+time. Each admitted fit keeps its dataset on the device (generated there and
+precomputed once, both enqueued without host waits so that admitting many
+requests costs no round trips) and is driven by a host-side minimiser
 written as a coroutine that yields evaluation requests, the way the
 reference's Minuit2 asks its FCN for -2 ln L, the gradient and, with the
 analytic Hessian switched on, the Hessian (include/fitter.hh:113-169). The server runs in ticks: it admits the
 requests that have arrived while the HBM budget and the slots allow, takes
-the pending evaluation of every active fit, issues one batched call per
-(model, kernel) (mf_kernel_reduce_many: consecutive evaluations overlap on the
-device), hands each fit its sums and frees the dataset of every fit that
-finishes. Requests that arrive while others are on the GPU join at the next
-tick (continuous batching). The batched sums are bit-identical to single
-launches, so every fit follows the same trajectory alone and in the mix.
+the pending evaluation of every active fit, issues one launch per (model,
+kernel) over all of them (mf_kernel_reduce_multi: each dataset cut into
+segments of 2048 events, one block each), hands each fit its sums and frees
+the dataset of every fit that finishes. Requests that arrive while others are
+on the GPU join at the next tick (continuous batching). A dataset's sums in
+such a launch do not depend on what else shares it, so every fit follows the
+same trajectory alone and in the mix.
 
 The minimiser uses the information the reference's fit uses with analytic
 derivatives switched on (gradient and Hessian kernels): damped Newton steps
@@ -167,7 +169,9 @@ class ModelRuntime:
         nseeds = int(min(65536, n))
         self.gen.CopyToSeedBuffer(splitmix_seed_rows(nseeds, seed))
         self.gen.SetNevents(n)
-        self.gen.SubmitKernel(nper=-(-n // nseeds))
+        # enqueued without a host wait (a thread that gives up is reported by
+        # the next synchronous call); the precompute follows in stream order
+        self.gen.SubmitKernelAsync(-(-n // nseeds))
         raw = self.gen.output
         self.gen.output = DeviceColumns(self.backend, self.gen.elem)
         if not self.template.has_precompute:
@@ -184,7 +188,9 @@ class ModelRuntime:
         out = DeviceColumns(self.backend, pre.elem)
         out.ensure(k.nout, n)
         p = np.zeros(1)
-        L.check(L.lib.mf_kernel_store(k.handle, raw.buf, raw.stride, n, L.dptr(p), k.nparams, out.buf, out.stride))
+        L.check(L.lib.mf_kernel_store_async(k.handle, raw.buf, raw.stride, n, L.dptr(p), k.nparams, out.buf,
+                                            out.stride))
+        out._keep = raw  # the generated events stay until the fit's columns go (mf_buffer_free waits for the stream)
         return out
 
     def param_rows(self, kernel: str, thetas) -> np.ndarray:
@@ -206,8 +212,9 @@ class ModelRuntime:
             self._out_bytes = max(need, 1 << 16)
             L.check(L.lib.mf_buffer_alloc(self.backend.handle, self._out_bytes, C.byref(self._out)))
         u64p = C.POINTER(C.c_uint64)
-        L.check(L.lib.mf_kernel_reduce_many(k.handle, count, ins, strides.ctypes.data_as(u64p),
-                                            nsa.ctypes.data_as(u64p), L.dptr(rows), rows.shape[1], self._out))
+        # every pending evaluation of the tick in one launch (segments of 2048 events)
+        L.check(L.lib.mf_kernel_reduce_multi(k.handle, count, ins, strides.ctypes.data_as(u64p),
+                                             nsa.ctypes.data_as(u64p), L.dptr(rows), rows.shape[1], self._out))
         res = np.zeros((count, k.nout))
         L.check(L.lib.mf_buffer_d2h(self._out, 0, res.ctypes.data, res.nbytes))
         return res
