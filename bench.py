@@ -519,8 +519,10 @@ def ours(args):
     if not args.no_toys:
         from morefit_gb300.toystudy import ToyStudy
         ts = ToyStudy(backend, spec, seed=229387429 + 1000 * rank)
-        # warm-up: kernels compiled and cached, the segment block size tuned on 1024 toys
-        ts.toy(1024, 2000, poisson=True, clip=(200, 50000), jitter=0.1)
+        # warm-up: kernels compiled and cached, the segment schedule tuned for
+        # the timed study's segment-size histogram (4096 toys of ~2000 events)
+        ts.toy(4096, 2000, poisson=True, clip=(200, 50000), jitter=0.1)
+        tuned = ts.tuning
         r = ts.toy(4096, 2000, poisson=True, clip=(200, 50000), jitter=0.1)
         serial = ts.serial_fits_per_s(r, 32)
         toys = {"value": world * 4096 / r.timing["total_s"], "unit": "toy fits/s",
@@ -532,8 +534,10 @@ def ours(args):
                           "+ precompute for all toys, batched Newton fits over ragged segments (F+grad, Hessian, "
                           "step trials per iteration)",
                 "events": int(r.counts.sum()), "all_converged": bool(r.fit.converged.all()),
-                "segment_block": ts.block,
-                "tuning_launch_ms": {str(k): round(v * 1e3, 4) for k, v in ts.tuning["launch_s"].items()},
+                "segment_schedule": str(ts.schedule),
+                "schedule_reused": bool(ts.tuning and ts.tuning.get("cached")),
+                "tuning_launch_ms": ({k: round(v * 1e3, 4) for k, v in tuned["launch_s"].items()}
+                                     if tuned and "launch_s" in tuned else None),
                 "max_iterations": int(r.fit.iterations.max()), "segment_launches": int(r.fit.evaluations),
                 "pull_mean": [round(float(x), 3) for x in r.pulls.mean(0)],
                 "pull_std": [round(float(x), 3) for x in r.pulls.std(0)]}

@@ -68,6 +68,10 @@ const char* mf_version(void);
 /* Number of visible CUDA devices (0 without a GPU; never an error). */
 int mf_device_count(int* count);
 
+/* Name (NUL-terminated, at most len - 1 characters), SM count and compute
+ * capability of device `device`; any output may be NULL. */
+int mf_device_properties(int device, char* name, size_t len, int* sm_count, int* cc_major, int* cc_minor);
+
 /* ---- context: one stream + scratch on one device ----
  * Replaces ComputeBackend construction (include/compute.hh:98-107; the
  * OpenCL backend's platform/device set-up, include/compute_opencl.hh:30-206).
@@ -391,6 +395,17 @@ int mf_context_stream(mf_context* ctx, void** stream);
 int mf_kernel_reduce_segments(mf_kernel* k, const mf_buffer* input, uint64_t stride, uint32_t nseg,
                               const uint64_t* seg_begin, const uint32_t* seg_count, const double* params,
                               uint32_t n_params, double* sums);
+
+/* mf_kernel_reduce_segments through the multi-dataset entry: each segment is
+ * cut into runs of `events_per_block` events (0: 2048), one block each, whose
+ * partial sums are combined in a fixed order, where mf_kernel_reduce_segments
+ * gives each segment one block. A segment's sums depend on its own events,
+ * parameters and the run length only. For segments long enough that one
+ * block per segment leaves the device idle; the toy study's tuner picks the
+ * entry and the run length. */
+int mf_kernel_reduce_segments_chunked(mf_kernel* k, const mf_buffer* input, uint64_t stride, uint32_t nseg,
+                                      const uint64_t* seg_begin, const uint32_t* seg_count, const double* params,
+                                      uint32_t n_params, uint32_t events_per_block, double* sums);
 
 /* How many mf_kernel_reduce / mf_kernel_reduce_segments calls on `k` were
  * evaluated again in native FP64 because a double-float sum was not finite

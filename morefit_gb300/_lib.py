@@ -94,6 +94,8 @@ def _proto(name, restype, *args):
 _proto("mf_last_error", C.c_char_p)
 _proto("mf_version", C.c_char_p)
 _proto("mf_device_count", C.c_int, C.POINTER(C.c_int))
+_proto("mf_device_properties", C.c_int, C.c_int, C.c_char_p, C.c_size_t, C.POINTER(C.c_int), C.POINTER(C.c_int),
+       C.POINTER(C.c_int))
 _proto("mf_context_create", C.c_int, C.c_int, C.c_uint64, C.POINTER(c_ctx))
 _proto("mf_context_destroy", C.c_int, c_ctx)
 _proto("mf_context_allocated", C.c_int, c_ctx, C.POINTER(C.c_uint64))
@@ -138,6 +140,8 @@ _proto("mf_kernel_store_async", C.c_int, c_ker, c_buf, C.c_uint64, C.c_uint64, c
 _proto("mf_kernel_read_layout", C.c_int, c_ker, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32))
 _proto("mf_kernel_reduce_segments", C.c_int, c_ker, c_buf, C.c_uint64, C.c_uint32, C.POINTER(C.c_uint64),
        C.POINTER(C.c_uint32), c_dbl_p, C.c_uint32, c_dbl_p)
+_proto("mf_kernel_reduce_segments_chunked", C.c_int, c_ker, c_buf, C.c_uint64, C.c_uint32, C.POINTER(C.c_uint64),
+       C.POINTER(C.c_uint32), c_dbl_p, C.c_uint32, C.c_uint32, c_dbl_p)
 _proto("mf_kernel_fallback_count", C.c_int, c_ker, C.POINTER(C.c_uint64))
 _proto("mf_buffer_wrap_host", C.c_int, c_ctx, C.c_void_p, C.c_uint64, C.POINTER(c_buf))
 _proto("mf_events_load_file", C.c_int, c_buf, C.c_int, C.c_uint64, C.c_char_p, C.c_uint64, C.c_int, C.c_uint64,
@@ -187,7 +191,7 @@ def dptr(a) -> c_dbl_p:
 def exported_symbols() -> list[str]:
     """Names of every function the header declares (used by the load test)."""
     return [
-        "mf_last_error", "mf_version", "mf_device_count", "mf_context_create", "mf_context_destroy",
+        "mf_last_error", "mf_version", "mf_device_count", "mf_device_properties", "mf_context_create", "mf_context_destroy",
         "mf_context_allocated", "mf_context_synchronize", "mf_buffer_alloc", "mf_buffer_free", "mf_buffer_size",
         "mf_buffer_device_ptr", "mf_buffer_h2d", "mf_buffer_d2h", "mf_buffer_memset", "mf_column_stride",
         "mf_events_upload", "mf_events_download", "mf_events_upload_f64_as", "mf_kernel_build", "mf_kernel_free",
@@ -200,5 +204,5 @@ def exported_symbols() -> list[str]:
         "mf_histogram", "mf_events_load_file", "mf_splitmix_seed_rows", "mf_buffer_wrap_host",
         "mf_spd_solve_batch", "mf_kernel_reduce_multi", "mf_coalescer_create", "mf_coalescer_destroy",
         "mf_context_set_coalescer", "mf_coalesced_submit", "mf_coalesced_poll", "mf_coalescer_stats",
-        "mf_kernel_generate_async",
+        "mf_kernel_generate_async", "mf_kernel_reduce_segments_chunked",
     ]

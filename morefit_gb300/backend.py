@@ -45,6 +45,13 @@ class CUDABackend:
         L.check(L.lib.mf_context_allocated(self._h, C.byref(v)))
         return v.value
 
+    def properties(self) -> dict:
+        """Name, SM count and compute capability of this backend's device."""
+        name = C.create_string_buffer(256)
+        sms, ma, mi = C.c_int(), C.c_int(), C.c_int()
+        L.check(L.lib.mf_device_properties(self.device, name, 256, C.byref(sms), C.byref(ma), C.byref(mi)))
+        return {"name": name.value.decode(), "sms": sms.value, "cc": (ma.value, mi.value)}
+
     def synchronize(self) -> None:
         L.check(L.lib.mf_context_synchronize(self._h))
 
@@ -480,14 +487,21 @@ class CUDABlock:
         return True
 
     # --- batched ragged segments (toy studies) ---
-    def SubmitSegments(self, seg_begin, seg_count, params_rows) -> np.ndarray:
+    def SubmitSegments(self, seg_begin, seg_count, params_rows, events_per_block: int = 0) -> np.ndarray:
+        """Sums of every segment [seg_begin[s], seg_begin[s] + seg_count[s]) at
+        its own parameter row: one block per segment, or (``events_per_block``
+        > 0) runs of that many events of each segment, one block each."""
         k = self.kernel
         b = np.ascontiguousarray(seg_begin, dtype=np.uint64)
         c = np.ascontiguousarray(seg_count, dtype=np.uint32)
         pr = np.ascontiguousarray(params_rows, dtype=np.float64).reshape(len(b), -1)
         out = np.zeros((len(b), k.nout))
-        L.check(L.lib.mf_kernel_reduce_segments(k.handle, self.input.buf, self.input.stride, len(b),
-                                                b.ctypes.data_as(C.POINTER(C.c_uint64)),
-                                                c.ctypes.data_as(C.POINTER(C.c_uint32)), L.dptr(pr), k.nparams,
-                                                L.dptr(out)))
+        pb, pc = b.ctypes.data_as(C.POINTER(C.c_uint64)), c.ctypes.data_as(C.POINTER(C.c_uint32))
+        if events_per_block > 0:
+            L.check(L.lib.mf_kernel_reduce_segments_chunked(k.handle, self.input.buf, self.input.stride, len(b), pb,
+                                                            pc, L.dptr(pr), k.nparams, events_per_block,
+                                                            L.dptr(out)))
+        else:
+            L.check(L.lib.mf_kernel_reduce_segments(k.handle, self.input.buf, self.input.stride, len(b), pb, pc,
+                                                    L.dptr(pr), k.nparams, L.dptr(out)))
         return out

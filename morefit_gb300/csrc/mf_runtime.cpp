@@ -544,6 +544,23 @@ int mf_device_count(int* count) {
   return MF_OK;
 }
 
+int mf_device_properties(int device, char* name, size_t len, int* sm_count, int* cc_major, int* cc_minor) {
+  int n = 0;
+  mf_device_count(&n);
+  if (n == 0) return fail(MF_ERR_NO_DEVICE, "no CUDA device");
+  if (device < 0 || device >= n) return fail(MF_ERR_INVALID, "device index out of range");
+  cudaDeviceProp p;
+  MF_CUDA_TRY(cudaGetDeviceProperties(&p, device));
+  if (name && len) {
+    std::strncpy(name, p.name, len - 1);
+    name[len - 1] = 0;
+  }
+  if (sm_count) *sm_count = p.multiProcessorCount;
+  if (cc_major) *cc_major = p.major;
+  if (cc_minor) *cc_minor = p.minor;
+  return MF_OK;
+}
+
 int mf_context_create(int device, uint64_t hbm_budget_bytes, mf_context** out) {
   if (!out) return fail(MF_ERR_INVALID, "out is null");
   *out = nullptr;
@@ -1848,15 +1865,15 @@ struct MultiItem {
   const double* params;  // k->n_params values
 };
 
-uint64_t multi_segments(uint64_t n) { return std::max<uint64_t>(1, (n + kMultiChunk - 1) / kMultiChunk); }
+uint64_t multi_segments(uint64_t n, uint64_t chunk = kMultiChunk) { return std::max<uint64_t>(1, (n + chunk - 1) / chunk); }
 
 size_t round16(size_t b) { return (b + 15) / 16 * 16; }
 
 // Host staging bytes launch_multi needs for `items`: the segment table, one
 // argument struct per item, and the per-item segment counts.
-size_t multi_table_bytes(const mf_kernel* k, const std::vector<MultiItem>& items) {
+size_t multi_table_bytes(const mf_kernel* k, const std::vector<MultiItem>& items, uint64_t chunk = kMultiChunk) {
   uint64_t nseg = 0;
-  for (const auto& it : items) nseg += multi_segments(it.n);
+  for (const auto& it : items) nseg += multi_segments(it.n, chunk);
   return round16(size_t(nseg) * sizeof(MultiSeg)) + round16(items.size() * k->lowered.args_bytes()) +
          round16(items.size() * sizeof(unsigned));
 }
@@ -1866,16 +1883,16 @@ size_t multi_table_bytes(const mf_kernel* k, const std::vector<MultiItem>& items
 // out[e * n_outputs ...] (device-visible memory). Every item's kernel is
 // built from k0's source. `host` is staging of multi_table_bytes() bytes that
 // stays untouched until the stream has executed the table copy. Segment s of
-// an item covers its events [s * kMultiChunk, ...): an item's sums depend on
-// nothing but its own events, parameters and size.
+// an item covers its events [s * chunk, ...): an item's sums depend on
+// nothing but its own events, parameters, size and the chunk.
 int launch_multi(mf_context* c, mf_kernel* k0, const std::vector<MultiItem>& items, unsigned char* host,
-                 double* out) {
+                 double* out, uint64_t chunk = kMultiChunk) {
   if (items.empty()) return MF_OK;
   const size_t ab = k0->lowered.args_bytes();
   uint64_t nseg = 0, pmax = 1;
   for (const auto& it : items) {
-    nseg += multi_segments(it.n);
-    pmax = std::max(pmax, multi_segments(it.n));
+    nseg += multi_segments(it.n, chunk);
+    pmax = std::max(pmax, multi_segments(it.n, chunk));
   }
   if (nseg > 0x7fffffffu) return fail(MF_ERR_INVALID, "too many segments in one launch");
   const size_t b_seg = round16(size_t(nseg) * sizeof(MultiSeg)), b_args = round16(items.size() * ab);
@@ -1886,10 +1903,10 @@ int launch_multi(mf_context* c, mf_kernel* k0, const std::vector<MultiItem>& ite
   uint64_t q = 0;
   for (size_t e = 0; e < items.size(); e++) {
     const MultiItem& it = items[e];
-    const uint64_t ns = multi_segments(it.n);
+    const uint64_t ns = multi_segments(it.n, chunk);
     for (uint64_t s = 0; s < ns; s++, q++) {
-      const uint64_t first = s * kMultiChunk;
-      segs[q] = MultiSeg{it.data, it.stride, first, uint32_t(std::min<uint64_t>(kMultiChunk, it.n - first)),
+      const uint64_t first = s * chunk;
+      segs[q] = MultiSeg{it.data, it.stride, first, uint32_t(std::min<uint64_t>(chunk, it.n - first)),
                          uint32_t(e), uint32_t(e * pmax + s), 0u};
     }
     grids[e] = unsigned(ns);
@@ -2283,3 +2300,69 @@ int mf_coalescer_stats(const mf_coalescer* co, uint64_t* ticks, uint64_t* evalua
 }
 
 }  // extern "C"
+
+// ------------------------------------- ragged segments through the multi entry --
+extern "C" int mf_kernel_reduce_segments_chunked(mf_kernel* k, const mf_buffer* in, uint64_t stride, uint32_t nseg,
+                                                 const uint64_t* seg_begin, const uint32_t* seg_count,
+                                                 const double* params, uint32_t n_params, uint32_t events_per_block,
+                                                 double* sums) {
+  if (!k || !in || !seg_begin || !seg_count || !sums || (n_params && !params))
+    return fail(MF_ERR_INVALID, "null argument");
+  const uint64_t chunk = events_per_block ? events_per_block : mfi::kMultiChunk;
+  if (k->kind != MF_KERNEL_REDUCE) return fail(MF_ERR_INVALID, "kernel is not a REDUCE kernel");
+  if (n_params != k->n_params) return fail(MF_ERR_INVALID, "parameter count mismatch");
+  if (nseg == 0) return MF_OK;
+  uint64_t end = 0;
+  for (uint32_t s = 0; s < nseg; s++) end = std::max<uint64_t>(end, seg_begin[s] + seg_count[s]);
+  int rc = check_layout(k, in, stride, end);
+  if (rc) return rc;
+  mf_context* c = k->ctx;
+  MF_CUDA_TRY(cudaSetDevice(c->device));
+  const void* data = nullptr;
+  rc = prepare_input(k, in, stride, &data);
+  if (rc) return rc;
+  // a segment is a dataset that starts `begin` elements into every column
+  const size_t eb = k->lowered.prep ? k->lowered.prep_elem_bytes() : elem_size(k->elem);
+  std::vector<mfi::MultiItem> items;
+  std::vector<uint32_t> where;  // item -> segment (empty segments have no item)
+  items.reserve(nseg);
+  for (uint32_t s = 0; s < nseg; s++) {
+    if (seg_count[s] == 0) continue;
+    items.push_back(mfi::MultiItem{k, static_cast<const char*>(data) + seg_begin[s] * eb, stride, seg_count[s],
+                                   params + uint64_t(s) * n_params});
+    where.push_back(s);
+  }
+  std::fill(sums, sums + size_t(nseg) * k->n_outputs, 0.0);
+  if (items.empty()) return MF_OK;
+  rc = ensure_scratch(c, 0, items.size() * k->n_outputs);
+  if (rc) return rc;
+  std::vector<unsigned char> host(mfi::multi_table_bytes(k, items, chunk));
+  rc = mfi::launch_multi(c, k, items, host.data(), c->out_dev, chunk);
+  if (rc) return rc;
+  MF_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  for (size_t i = 0; i < items.size(); i++)
+    std::memcpy(sums + size_t(where[i]) * k->n_outputs, c->out_host + i * k->n_outputs, k->n_outputs * sizeof(double));
+  if (!k->desc) return MF_OK;
+  // segments whose double-float sums are non-finite: again in native FP64
+  std::vector<uint64_t> b2;
+  std::vector<uint32_t> c2, bad;
+  std::vector<double> p2;
+  for (uint32_t s = 0; s < nseg; s++)
+    if (!all_finite(sums + size_t(s) * k->n_outputs, k->n_outputs)) {
+      bad.push_back(s);
+      b2.push_back(seg_begin[s]);
+      c2.push_back(seg_count[s]);
+      p2.insert(p2.end(), params + uint64_t(s) * n_params, params + uint64_t(s + 1) * n_params);
+    }
+  if (bad.empty()) return MF_OK;
+  rc = f64_twin(k);
+  if (rc) return rc;
+  k->fallbacks++;
+  std::vector<double> s2(bad.size() * k->n_outputs);
+  rc = mf_kernel_reduce_segments(k->f64, in, stride, uint32_t(bad.size()), b2.data(), c2.data(), p2.data(), n_params,
+                                 s2.data());
+  if (rc) return rc;
+  for (size_t i = 0; i < bad.size(); i++)
+    std::copy(s2.begin() + i * k->n_outputs, s2.begin() + (i + 1) * k->n_outputs, sums + size_t(bad[i]) * k->n_outputs);
+  return MF_OK;
+}

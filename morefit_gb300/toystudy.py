@@ -54,11 +54,17 @@ class SegmentLikelihood:
     """-2 ln L, gradient and Hessian of many event segments of one device
     event block (toy s: events [begin[s], begin[s] + count[s]))."""
 
-    def __init__(self, like: Likelihood, begins, counts):
+    def __init__(self, like: Likelihood, begins, counts, events_per_block: int = 0):
+        """``events_per_block``: 0 evaluates each segment in one block
+        (mf_kernel_reduce_segments); n > 0 cuts every segment into runs of n
+        events, one block each, combined in a fixed order
+        (mf_kernel_reduce_segments_chunked). Either way a segment's sums
+        depend on nothing but its own events and parameters."""
         self.like = like
         self.begins = np.ascontiguousarray(begins, dtype=np.uint64)
         self.counts = np.ascontiguousarray(counts, dtype=np.uint32)
         self.params = like.params
+        self.events_per_block = int(events_per_block)
         self.evaluations = 0
 
     def _rows(self, kernel: str, theta: np.ndarray) -> np.ndarray:
@@ -68,7 +74,8 @@ class SegmentLikelihood:
         self.evaluations += 1
         parts = self.like.kernel_parts(kernel)
         rows = self._rows(kernel, theta)
-        return np.concatenate([self.like.blocks[p].SubmitSegments(self.begins[idx], self.counts[idx], rows)
+        return np.concatenate([self.like.blocks[p].SubmitSegments(self.begins[idx], self.counts[idx], rows,
+                                                                  self.events_per_block)
                                for p in parts], axis=1)
 
     def value(self, idx, theta):
@@ -288,6 +295,69 @@ class ToyResult:
     timing: dict
 
 
+@dataclass(frozen=True)
+class SegmentSchedule:
+    """How the ragged-segment kernels cover the toys: ``block`` threads per
+    block; ``events_per_block`` 0 = one block per segment (each thread
+    strides over its segment), else runs of that many events per block
+    (``events_per_block / block`` events per thread) combined per segment."""
+    block: int
+    events_per_block: int = 0
+
+    def __str__(self) -> str:
+        return f"b{self.block}" + (f"_e{self.events_per_block}" if self.events_per_block else "_seg")
+
+
+DEFAULT_SCHEDULE = SegmentSchedule(256, 0)
+
+# Tuned schedules of this process: (model, kernel type, device, log2 of the
+# median and of the largest segment size, log2 of the toy count) -> schedule.
+# With MOREFIT_GB300_CACHE set they are also kept in
+# $MOREFIT_GB300_CACHE/toy_schedules.json and read back by later processes.
+_SCHEDULES: dict = {}
+
+
+def _schedule_file():
+    import os
+    d = os.environ.get("MOREFIT_GB300_CACHE")
+    return None if not d else os.path.join(d, "toy_schedules.json")
+
+
+def _load_schedules() -> dict:
+    import json
+    f = _schedule_file()
+    if f is None:
+        return {}
+    try:
+        with open(f) as fh:
+            return {k: SegmentSchedule(int(v[0]), int(v[1])) for k, v in json.load(fh).items()}
+    except (OSError, ValueError, TypeError, IndexError):
+        return {}
+
+
+def _store_schedule(key: str, sched: SegmentSchedule) -> None:
+    import json
+    import os
+    f = _schedule_file()
+    if f is None:
+        return
+    table = {k: [v.block, v.events_per_block] for k, v in _load_schedules().items()}
+    table[key] = [sched.block, sched.events_per_block]
+    os.makedirs(os.path.dirname(f), exist_ok=True)
+    tmp = f"{f}.{os.getpid()}"
+    with open(tmp, "w") as fh:
+        json.dump(table, fh, indent=1, sort_keys=True)
+    os.replace(tmp, f)
+
+
+def size_histogram_key(counts) -> tuple:
+    """The segment-size histogram a schedule is tuned for, coarsened to
+    powers of two: (median size, largest size, number of segments)."""
+    c = np.asarray(counts)
+    b = lambda x: int(round(math.log2(max(float(x), 1.0))))
+    return (b(np.median(c)), b(c.max()), b(len(c)))
+
+
 class ToyStudy:
     """Toy studies of one model (reference include/toystudy.hh:40-115).
 
@@ -297,47 +367,103 @@ class ToyStudy:
     ``clip``; otherwise every toy has ``nevents`` events (the reference draws
     Poisson counts only for extended PDFs)."""
 
-    # threads per block (= per segment) tried for the segment kernels
+    # threads per block tried for the segment kernels
     BLOCK_CANDIDATES = (64, 128, 256)
+    # events per thread tried for the chunked entry (runs of block x this many
+    # events); runs as long as the largest segment are left out
+    EVENTS_PER_THREAD_CANDIDATES = (2, 4, 8, 16)
     TUNE_MIN_TOYS = 512
 
     def __init__(self, backend: CUDABackend, spec: dict, kernelT=np.float64, limits=None,
-                 seed: int = DEFAULT_SEED, generator_threads: int = 65536, block: int = 0):
-        """``block``: threads per segment of the segment kernels; 0 = tuned on
-        the first study of at least TUNE_MIN_TOYS toys (the candidate whose
-        F + gradient + Hessian launch over that study's toys is fastest on
-        the device),
-        256 until then."""
+                 seed: int = DEFAULT_SEED, generator_threads: int = 65536, block: int = 0,
+                 schedule: SegmentSchedule | None = None):
+        """``schedule`` (or ``block``: threads per segment, one block per
+        segment) fixes how the segment kernels run. Otherwise a study of at
+        least TUNE_MIN_TOYS toys takes the schedule tuned for its model,
+        kernel type, device and segment-size histogram: from this process's
+        table (or the MOREFIT_GB300_CACHE file), else measured there and
+        then (the candidate whose Newton-iteration launches, F + gradient +
+        Hessian and one F trial over that study's toys, take the least
+        time) and stored. Smaller studies without a stored schedule run
+        DEFAULT_SCHEDULE."""
         self.backend = backend
         self.spec = spec
         self.kernelT = kernelT
         self.limits = limits if limits is not None else PWAVE_LIMITS
         self.seed = seed
         self.generator_threads = generator_threads
-        self.block = block
+        if schedule is None and block:
+            schedule = SegmentSchedule(block, 0)
+        self.fixed = schedule
+        self.schedule = schedule or DEFAULT_SCHEDULE
         self.tuning = None
         self._likes = {}
+
+    @property
+    def block(self) -> int:
+        return self.schedule.block
 
     def _likelihood(self, block: int) -> Likelihood:
         if block not in self._likes:  # kernels built once per block size
             self._likes[block] = Likelihood(self.backend, self.spec, self.kernelT, block=block)
         return self._likes[block]
 
-    def _tune(self, cols, begins, counts, truth) -> None:
+    def _schedule_key(self, counts) -> str:
+        dev = self.backend.__dict__.get("_device_key")
+        if dev is None:
+            p = self.backend.properties()
+            dev = self.backend._device_key = f"{p['name']}:{p['sms']}"
+        return "|".join([str(self.spec.get("workload", "model")), np.dtype(self.kernelT).name, dev,
+                         ",".join(map(str, size_histogram_key(counts)))])
+
+    def candidates(self, counts) -> list:
+        """Schedules the tuner measures for segments of these sizes."""
+        cmax = int(np.max(counts))
+        out = []
+        for blk in self.BLOCK_CANDIDATES:
+            out.append(SegmentSchedule(blk, 0))
+            for e in self.EVENTS_PER_THREAD_CANDIDATES:
+                if blk * e < cmax:
+                    out.append(SegmentSchedule(blk, blk * e))
+        return out
+
+    def _choose(self, cols, begins, counts, truth) -> None:
+        if self.fixed is not None:
+            return
+        key = self._schedule_key(counts)
+        if key not in _SCHEDULES:
+            _SCHEDULES.update({k: v for k, v in _load_schedules().items() if k not in _SCHEDULES})
+        if key in _SCHEDULES:
+            self.schedule = _SCHEDULES[key]
+            self.tuning = {"schedule": str(self.schedule), "cached": True, "key": key}
+        elif len(counts) >= self.TUNE_MIN_TOYS:
+            self._tune(cols, begins, counts, truth, key)
+        else:
+            self.schedule = DEFAULT_SCHEDULE
+
+    def _tune(self, cols, begins, counts, truth, key) -> None:
         import time
         idx = np.arange(len(counts))
         times = {}
-        for blk in self.BLOCK_CANDIDATES:
-            like = self._likelihood(blk)
+        for sched in self.candidates(counts):
+            like = self._likelihood(sched.block)
             like.set_device_data(cols)
-            sl = SegmentLikelihood(like, begins, counts)
-            sl.value_gradient_hessian(idx, truth)  # builds the kernels and the prepared copy
-            t0 = time.perf_counter()
+            sl = SegmentLikelihood(like, begins, counts, sched.events_per_block)
+            # once to build the kernels and the prepared copy, then timed
+            sl.value_gradient_hessian(idx, truth)
+            sl.value(idx, truth)
+            best = math.inf
             for _ in range(3):
+                t0 = time.perf_counter()
                 sl.value_gradient_hessian(idx, truth)
-            times[blk] = (time.perf_counter() - t0) / 3
-        self.block = min(times, key=times.get)
-        self.tuning = {"block": self.block, "launch_s": times, "toys": len(counts)}
+                sl.value(idx, truth)
+                best = min(best, time.perf_counter() - t0)
+            times[sched] = best
+        self.schedule = min(times, key=times.get)
+        _SCHEDULES[key] = self.schedule
+        _store_schedule(key, self.schedule)
+        self.tuning = {"schedule": str(self.schedule), "cached": False, "key": key, "toys": len(counts),
+                       "launch_s": {str(k): v for k, v in times.items()}}
 
     def serial_fits_per_s(self, result: "ToyResult", ntoys: int = 32) -> float:
         """The per-fit serial baseline: the first ``ntoys`` toys of ``result``'s
@@ -347,7 +473,7 @@ class ToyStudy:
         sl_all = self._last_segments
         t0 = time.perf_counter()
         for t in range(min(ntoys, len(result.counts))):
-            sl = SegmentLikelihood(sl_all.like, sl_all.begins[t:t + 1], sl_all.counts[t:t + 1])
+            sl = SegmentLikelihood(sl_all.like, sl_all.begins[t:t + 1], sl_all.counts[t:t + 1], sl_all.events_per_block)
             fit_segments(sl, result.truth[t:t + 1], self.limits)
         return min(ntoys, len(result.counts)) / (time.perf_counter() - t0)
 
@@ -375,13 +501,12 @@ class ToyStudy:
             truth = np.tile(base, (nruns, 1))
             cols = generate_events(self.backend, self.spec, total, seed=self.seed,
                                    max_workitems=self.generator_threads, kernelT=np.float64)
-        if self.block == 0 and nruns >= self.TUNE_MIN_TOYS:
-            self._tune(cols, begins, counts, truth)
-        like = self._likelihood(self.block or 256)
+        self._choose(cols, begins, counts, truth)
+        like = self._likelihood(self.schedule.block)
         like.set_device_data(cols)
         self.backend.synchronize()
         t1 = time.perf_counter()
-        sl = SegmentLikelihood(like, begins, counts)
+        sl = SegmentLikelihood(like, begins, counts, self.schedule.events_per_block)
         self._last_segments = sl
         fit = fit_segments(sl, truth, self.limits)
         t2 = time.perf_counter()

@@ -231,6 +231,29 @@ def test_hessian_split_in_parts(backend, kernelT):
         assert np.all(np.abs(split - whole) <= tol * np.abs(whole).max())
         many = like.sums_many("lh_hessian_kernel", np.array([pt["params"]] * 2))
         assert np.array_equal(many[0], split) and np.array_equal(many[1], split)
+    # ragged segments through the parts (the toy fits' Hessian): the golden
+    # events as one segment and as three, joined parts against the single kernel
+    from morefit_gb300.toystudy import SegmentLikelihood, _unpack_hessian
+    counts = np.array([2000, 700, 1, 1299])
+    begins = np.array([0, 0, 700, 701])
+    th = np.array([pt["params"] for pt in g["points"]] + [g["points"][0]["params"]])
+    for epb in (0, 512):
+        sl = SegmentLikelihood(like, begins, counts, epb)
+        hs = sl.hessian(np.arange(4), th)
+        npar = th.shape[1]
+        for s_ in range(4):
+            b.CopyToParameterBuffer(like.param_vector("lh_hessian_kernel", th[s_]))
+            if s_ == 0:
+                b.SubmitKernel()
+                whole = _unpack_hessian(b.CopyFromKahanBuffer()[None], npar)[0]
+            else:
+                one = b.SubmitSegments([begins[s_]], [counts[s_]], like.param_rows("lh_hessian_kernel", th[s_:s_ + 1]))
+                whole = _unpack_hessian(one, npar)[0]
+            assert np.all(np.abs(hs[s_] - whole) <= tol * np.abs(whole).max()), (epb, s_)
+        # segments 1-3 at the same point cover the set once
+        th3 = np.array([th[0]] * 3)
+        parts3 = sl.hessian(np.arange(1, 4), th3).sum(0)
+        assert np.all(np.abs(parts3 - hs[0]) <= tol * np.abs(hs[0]).max()), epb
     pw = Likelihood(backend, load_golden("pwave_n1000.json"), kernelT)
     assert pw.kernel_parts("lh_hessian_kernel") == ["lh_hessian_kernel"]
 
@@ -431,7 +454,12 @@ def test_gpu_generator_reproduces_reference_stream_spwave(backend, n):
         assert np.array_equal(ev, golden_events("spwave", n))
 
 
-def test_ragged_segments(backend):
+@pytest.mark.parametrize("events_per_block", [0, 64, 256, 2048])
+def test_ragged_segments(backend, events_per_block):
+    """Segments of one event block at their own parameter rows, one block per
+    segment (0) or in runs of ``events_per_block`` events combined per
+    segment: each within the FP64 bar of the oracle, and a segment's sums the
+    same bit for bit alone and among the others."""
     from morefit_gb300.workloads import Likelihood
     g = load_golden("pwave_n1000.json")
     ev = golden_events("pwave", 1000)
@@ -447,12 +475,15 @@ def test_ragged_segments(backend):
         th = np.array(g["points"][s % 3]["params"]) + rng.normal(0, 0.01, 8)
         rows.append(like.param_vector("lh_grad_kernel", th))
     rows = np.array(rows)
-    out = like.blocks["lh_grad_kernel"].SubmitSegments(begins, counts, rows)
+    blk = like.blocks["lh_grad_kernel"]
+    out = blk.SubmitSegments(begins, counts, rows, events_per_block)
     for s in range(len(counts)):
         sl = cols[:, begins[s]:begins[s] + counts[s]]
         ref = sk.reduce(sl, rows[s]) if counts[s] else np.zeros(9)
         scale = np.abs(sk.store(sl, rows[s])).sum(axis=1) if counts[s] else np.zeros(9)
         assert_sums_close(out[s], ref, scale, what=f"segment {s}")
+        alone = blk.SubmitSegments(begins[s:s + 1], counts[s:s + 1], rows[s:s + 1], events_per_block)
+        assert np.array_equal(alone[0], out[s]), f"segment {s} alone"
 
 
 def test_prepared_columns_follow_writes(backend, oracle_lib):

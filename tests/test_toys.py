@@ -154,3 +154,49 @@ def test_fit_moves_where_the_reference_fit_stays(backend):
         f_min, grad = like.likelihood_and_gradient(r.values[0])
         assert f_min < f_start - 1.0, (f_min, f_start)
         assert np.abs(grad).max() < 1e-3, grad
+
+
+def test_segment_schedule_tuned_and_reused(backend, tmp_path, monkeypatch):
+    """The toy study's tuner measures every candidate schedule of the segment
+    kernels (threads per block; one block per segment, or runs of block x
+    2..16 events per block combined per segment), keeps the fastest, and a
+    later study of the same model and segment-size histogram reuses it
+    without measuring: from the process's table, and in a process whose
+    table is empty from the MOREFIT_GB300_CACHE file. Fits run with the
+    chosen schedule converge, and a toy fitted alone with it gives the
+    batch's result bit for bit."""
+    from morefit_gb300 import toystudy as T
+    from morefit_gb300.workloads import load_spec
+    monkeypatch.setenv("MOREFIT_GB300_CACHE", str(tmp_path))
+    monkeypatch.setattr(T, "_SCHEDULES", {})
+    spec = load_spec("pwave")
+    cfg = dict(poisson=True, clip=(200, 50000), jitter=0.1)
+    a = T.ToyStudy(backend, spec, seed=11)
+    ra = a.toy(512, 2000, **cfg)
+    assert a.tuning is not None and not a.tuning["cached"]
+    times = a.tuning["launch_s"]
+    cands = a.candidates(ra.counts)
+    assert len(times) == len(cands) and any(c.events_per_block for c in cands)
+    assert str(a.schedule) == min(times, key=times.get)
+    assert ra.fit.converged.all()
+    print("segment schedules (ms per Newton iteration's launches):",
+          {k: round(v * 1e3, 3) for k, v in sorted(times.items(), key=lambda kv: kv[1])})
+    assert (tmp_path / "toy_schedules.json").exists()
+
+    b = T.ToyStudy(backend, spec, seed=12)
+    rb = b.toy(512, 2000, **cfg)
+    assert b.tuning["cached"] and b.schedule == a.schedule and "launch_s" not in b.tuning
+    assert rb.fit.converged.all()
+
+    monkeypatch.setattr(T, "_SCHEDULES", {})  # another process: the file only
+    c = T.ToyStudy(backend, spec, seed=11)
+    rc = c.toy(512, 2000, **cfg)
+    assert c.tuning["cached"] and c.schedule == a.schedule
+    assert np.array_equal(rc.fit.values, ra.fit.values)
+
+    # a toy alone under the chosen schedule
+    t = 7
+    sl = c._last_segments
+    one = T.SegmentLikelihood(sl.like, sl.begins[t:t + 1], sl.counts[t:t + 1], c.schedule.events_per_block)
+    r1 = T.fit_segments(one, rc.truth[t:t + 1], c.limits)
+    assert np.array_equal(r1.values[0], rc.fit.values[t])
