@@ -628,6 +628,8 @@ def ours(args):
             "serving_capacity_over_serial": r3(serving["capacity_over_serial"]) if serving else None,
             "e2e_evals_per_s": r3(world / e2e_s), "fit_loop_evals_per_s": r3(world / fit_loop_s),
             "reference_fitter_1M_fit_ms": r3(fitters["fit_1M"]["fit_ms"]) if fitters else None,
+            "reference_fitter_fcn_grad_call_us":
+                r3(fitters["fcn_call_us_1M"]["likelihood_and_gradient"]["p50"]) if fitters else None,
             "reference_fitter_threads_capacity_over_serial":
                 r3(fitters["threads_8"]["capacity_over_serial"]) if fitters else None,
             "cpu_reference_1M_fit_ms": r3(cpu["fit_1M_ms"]) if cpu and cpu.get("fit_1M_ms") else None,
@@ -810,6 +812,15 @@ def fitter_rows(backend, host):
         fit = _run_json([d, "fit", "pwave", f0])
         out["fit_1M"] = {"fit_ms": fit["fit_ms"], "first_fit_ms": fit["first_fit_ms"], "cov_status": fit["cov_status"],
                          "events_fnv1a": fit["events_fnv1a"]}
+        # one FCN evaluation as MIGRAD makes it (hoisted parameter buffers on
+        # the host, CopyToParameterBuffer, SubmitKernel, Finish,
+        # CopyFromKahanBuffer), per call, at the fitted point
+        calls = _run_json([d, "calls", "pwave", f0, 2000])
+        calls_mixed = _run_json([d, "calls", "pwave", f0, 2000, "mixed"])
+        out["fcn_call_us_1M"] = {"likelihood_and_gradient": calls["likelihood_and_gradient_us"],
+                                 "likelihood": calls["likelihood_us"],
+                                 "mixed_likelihood_and_gradient": calls_mixed["likelihood_and_gradient_us"],
+                                 "mixed_likelihood": calls_mixed["likelihood_us"]}
         files = []
         for i, n in enumerate([20000, 50000, 100000, 200000] * 2):
             p = Path(td) / f"pwave_{i}.f64"

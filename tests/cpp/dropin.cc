@@ -24,7 +24,15 @@
 //                                          backend fitting that file, at once
 //                                          (one thread after another: serial),
 //                                          through a shared coalescer or not
+//   dropin calls <workload> <events.f64> <count> [mixed]
+//                                          latency of the fitter's FCN
+//                                          evaluations after one fit: count
+//                                          calls each of likelihood_and_gradient
+//                                          (what MIGRAD calls) and likelihood,
+//                                          at the fitted point; prints
+//                                          percentiles in microseconds
 #define MOREFIT_H 1
+#include <algorithm>
 #include <atomic>
 #include <cassert>
 #include <chrono>
@@ -283,6 +291,64 @@ static int cmd_genfit(const std::string& which, unsigned n, const char* prec) {
   return r.ok ? 0 : 1;
 }
 
+// Per-call latency of the reference fitter's evaluations over CUDABlock: one
+// fit builds the kernels and uploads the events, then each timed call is one
+// FCN evaluation as Minuit2 makes it (hoisted parameter buffers on the host,
+// CopyToParameterBuffer, SubmitKernel, Finish, CopyFromKahanBuffer).
+static int cmd_calls(const std::string& which, const std::string& path, int count, bool mixed) {
+  typedef double kT;
+  typedef double eT;
+  compute_options copts;
+  cuda_options cu;
+  cu.mixed_precision = mixed;
+  CUDABackend backend(&copts, cu);
+  if (!backend.ok()) {
+    std::printf("{\"skipped\":\"%s\"}\n", backend.error().c_str());
+    return 3;
+  }
+  Workload<kT, eT> w = make_workload<kT, eT>(which);
+  unsigned n = 0;
+  std::vector<double> ev = read_events(path, w.dims.size(), n);
+  const size_t nd = w.dims.size();
+  EventVector<kT, eT> data(w.dims, n);
+  for (size_t d = 0; d < nd; d++)
+    for (unsigned i = 0; i < n; i++) data(i, d) = ev[d * n + i];
+  fitter_options fo = make_fit_opts(w);
+  fitter<kT, eT, CUDABackend, CUDABlock<kT, eT>> fit(&fo, &backend);
+  std::ostringstream log;
+  std::streambuf* old = std::cout.rdbuf(log.rdbuf());
+  const bool ok = fit.fit(w.pdf, w.params, &data);
+  std::cout.rdbuf(old);
+  const int np = int(w.params.size());
+  std::vector<double> g(np);
+  auto pct = [](std::vector<double> t) {
+    std::sort(t.begin(), t.end());
+    char b[160];
+    std::snprintf(b, sizeof b, "{\"p10\":%.3f,\"p50\":%.3f,\"p90\":%.3f}", t[t.size() / 10], t[t.size() / 2],
+                  t[t.size() * 9 / 10]);
+    return std::string(b);
+  };
+  std::vector<double> tg, tl;
+  double sink = 0.0;
+  for (int i = 0; i < count + 50; i++) {
+    auto t0 = std::chrono::steady_clock::now();
+    sink += fit.likelihood_and_gradient(np, g.data());
+    auto t1 = std::chrono::steady_clock::now();
+    if (i >= 50) tg.push_back(std::chrono::duration<double, std::micro>(t1 - t0).count());
+  }
+  for (int i = 0; i < count + 50; i++) {
+    auto t0 = std::chrono::steady_clock::now();
+    sink += fit.likelihood();
+    auto t1 = std::chrono::steady_clock::now();
+    if (i >= 50) tl.push_back(std::chrono::duration<double, std::micro>(t1 - t0).count());
+  }
+  std::printf("{\"workload\":\"%s\",\"n\":%u,\"mixed\":%s,\"fit_ok\":%s,\"count\":%d,"
+              "\"likelihood_and_gradient_us\":%s,\"likelihood_us\":%s,\"finite\":%s}\n",
+              which.c_str(), n, mixed ? "true" : "false", ok ? "true" : "false", count, pct(tg).c_str(),
+              pct(tl).c_str(), std::isfinite(sink) ? "true" : "false");
+  return ok ? 0 : 1;
+}
+
 // Several host threads, each with its own fitter, CUDABlocks and backend
 // (context), fitting its own dataset: one fitter per host thread, the
 // reference's threading model. mode "coalesce": every backend routes its
@@ -366,7 +432,8 @@ int main(int argc, char** argv) {
   const std::string usage =
       "usage: dropin lower <workload> | dropin fit <workload> <events.f64> [f32|mixed] | "
       "dropin genfit <workload> <n> [f32] | "
-      "dropin threads <workload> <coalesce|plain|serial> <f64|mixed> <events.f64>...\n";
+      "dropin threads <workload> <coalesce|plain|serial> <f64|mixed> <events.f64>... | "
+      "dropin calls <workload> <events.f64> <count> [mixed]\n";
   if (argc < 3) {
     std::fprintf(stderr, "%s", usage.c_str());
     return 2;
@@ -382,6 +449,8 @@ int main(int argc, char** argv) {
     const unsigned n = unsigned(std::stoul(argv[3]));
     return is_f32(4) ? cmd_genfit<float>(which, n, "float") : cmd_genfit<double>(which, n, "double");
   }
+  if (mode == "calls" && argc >= 5)
+    return cmd_calls(which, argv[3], std::atoi(argv[4]), argc > 5 && std::string(argv[5]) == "mixed");
   if (mode == "threads" && argc >= 6) {
     std::vector<std::string> files(argv + 5, argv + argc);
     return cmd_threads(which, argv[3], std::string(argv[4]) == "mixed", files);
