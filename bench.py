@@ -816,9 +816,15 @@ def fitter_rows(backend, host):
         # the host, CopyToParameterBuffer, SubmitKernel, Finish,
         # CopyFromKahanBuffer), per call, at the fitted point
         calls = _run_json([d, "calls", "pwave", f0, 2000])
+        launch = _run_json([d, "calls", "pwave", f0, 2000, "launch"])
         calls_mixed = _run_json([d, "calls", "pwave", f0, 2000, "mixed"])
         out["fcn_call_us_1M"] = {"likelihood_and_gradient": calls["likelihood_and_gradient_us"],
                                  "likelihood": calls["likelihood_us"],
+                                 "migrad_pattern_per_call": calls["migrad_pattern_us_per_call"],
+                                 "resident_stats": calls["resident_stats"],
+                                 "launch_per_call": {"likelihood_and_gradient": launch["likelihood_and_gradient_us"],
+                                                     "likelihood": launch["likelihood_us"],
+                                                     "migrad_pattern_per_call": launch["migrad_pattern_us_per_call"]},
                                  "mixed_likelihood_and_gradient": calls_mixed["likelihood_and_gradient_us"],
                                  "mixed_likelihood": calls_mixed["likelihood_us"]}
         files = []

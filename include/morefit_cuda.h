@@ -333,6 +333,32 @@ int mf_coalesced_poll(mf_coalescer* co, uint64_t ticket, double* sums, int wait)
 /* Ticks run, evaluations served and the largest batch so far. */
 int mf_coalescer_stats(const mf_coalescer* co, uint64_t* ticks, uint64_t* evaluations, uint32_t* max_batch);
 
+/* ---- resident evaluations ----
+ * With idle_us > 0, the synchronous mf_kernel_reduce calls of this context
+ * (no coalescer attached) are watched; after a few calls the library builds,
+ * in the background, a module with the REDUCE kernels used most (up to two
+ * with the same block size, e.g. a fit's likelihood and likelihood+gradient)
+ * and then serves their synchronous evaluations from one resident grid that
+ * waits for requests in mapped host memory instead of launching a grid per
+ * call. The sums are those of the kernel's own launch, bit for bit: each
+ * request runs the kernel's own block partition and combine. The grid leaves
+ * after idle_us without requests, or when any other work of this library is
+ * launched on the device (by any context), and calls then launch as usual
+ * until it is started again. Needs host-native atomics and cooperative
+ * launches (MF_ERR_UNSUPPORTED otherwise). idle_us = 0 turns it off.
+ * No counterpart in the reference (its backends launch per SubmitKernel). */
+int mf_context_set_resident(mf_context* ctx, uint32_t idle_us);
+/* state: -1 off, 0 watching calls, 1 building, 2 ready, 3 unavailable;
+ * grids: resident grids launched; served: evaluations they served; blocks:
+ * the resident grid's size (0 before it is built). */
+int mf_context_resident_stats(const mf_context* ctx, int* state, uint64_t* grids, uint64_t* served, int* blocks);
+/* The resident module for one or two REDUCE kernel descriptions, lowered and
+ * compiled with NVRTC (no device needed): registers, spilled bytes and, when
+ * source is non-NULL, its CUDA C (truncated to len). */
+int mf_compile_check_resident(const mf_kernel_desc* const* descs, uint32_t count, int* regs, int* spill,
+                              char* source, size_t len);
+
+
 /* Compensated sums over events of ncols columns of an SoA event block:
  * sums[c] = sum_{i<n} column c (element type MF_F64 or MF_F32, column stride
  * `stride`), one launch, fixed summation order. Replaces the host-side

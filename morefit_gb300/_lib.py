@@ -94,6 +94,11 @@ def _proto(name, restype, *args):
 _proto("mf_last_error", C.c_char_p)
 _proto("mf_version", C.c_char_p)
 _proto("mf_device_count", C.c_int, C.POINTER(C.c_int))
+_proto("mf_context_set_resident", C.c_int, c_ctx, C.c_uint32)
+_proto("mf_context_resident_stats", C.c_int, c_ctx, C.POINTER(C.c_int), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64),
+       C.POINTER(C.c_int))
+_proto("mf_compile_check_resident", C.c_int, C.c_void_p, C.c_uint32, C.POINTER(C.c_int), C.POINTER(C.c_int),
+       C.c_char_p, C.c_size_t)
 _proto("mf_device_properties", C.c_int, C.c_int, C.c_char_p, C.c_size_t, C.POINTER(C.c_int), C.POINTER(C.c_int),
        C.POINTER(C.c_int))
 _proto("mf_context_create", C.c_int, C.c_int, C.c_uint64, C.POINTER(c_ctx))
@@ -191,7 +196,8 @@ def dptr(a) -> c_dbl_p:
 def exported_symbols() -> list[str]:
     """Names of every function the header declares (used by the load test)."""
     return [
-        "mf_last_error", "mf_version", "mf_device_count", "mf_device_properties", "mf_context_create", "mf_context_destroy",
+        "mf_last_error", "mf_version", "mf_device_count", "mf_device_properties", "mf_context_set_resident",
+        "mf_context_resident_stats", "mf_compile_check_resident", "mf_context_create", "mf_context_destroy",
         "mf_context_allocated", "mf_context_synchronize", "mf_buffer_alloc", "mf_buffer_free", "mf_buffer_size",
         "mf_buffer_device_ptr", "mf_buffer_h2d", "mf_buffer_d2h", "mf_buffer_memset", "mf_column_stride",
         "mf_events_upload", "mf_events_download", "mf_events_upload_f64_as", "mf_kernel_build", "mf_kernel_free",

@@ -25,11 +25,16 @@ from . import _lib as L
 class CUDABackend:
     """One device, one stream, an HBM budget (ComputeBackend, compute.hh:98-107)."""
 
-    def __init__(self, device: int = 0, hbm_budget_bytes: int = 0):
+    def __init__(self, device: int = 0, hbm_budget_bytes: int = 0, resident_idle_us: int = 2000):
+        """``resident_idle_us``: synchronous evaluations of the two most used
+        kernels are served by a resident grid that leaves after this long
+        without requests (``set_resident``); 0 launches per evaluation."""
         h = L.c_ctx()
         L.check(L.lib.mf_context_create(device, hbm_budget_bytes, C.byref(h)))
         self._h = h
         self.device = device
+        if resident_idle_us:
+            L.lib.mf_context_set_resident(h, int(resident_idle_us))  # unsupported: launches as usual
 
     def required_padding(self) -> int:
         # The device layout pads each column internally; host EventVectors
@@ -60,6 +65,18 @@ class CUDABackend:
         (None detaches): concurrent fitters in other threads share its launches."""
         L.check(L.lib.mf_context_set_coalescer(self._h, coalescer.handle if coalescer else None))
         self._coalescer = coalescer
+
+    def set_resident(self, idle_us: int) -> None:
+        """Serve this context's synchronous evaluations of its most used
+        REDUCE kernels from a resident grid (mf_context_set_resident) that
+        leaves after ``idle_us`` without requests; 0 turns it off."""
+        L.check(L.lib.mf_context_set_resident(self._h, int(idle_us)))
+
+    def resident_stats(self) -> dict:
+        st, grids, served, blocks = C.c_int(), C.c_uint64(), C.c_uint64(), C.c_int()
+        L.check(L.lib.mf_context_resident_stats(self._h, C.byref(st), C.byref(grids), C.byref(served),
+                                                C.byref(blocks)))
+        return {"state": st.value, "grids": grids.value, "served": served.value, "blocks": blocks.value}
 
     def close(self) -> None:
         if getattr(self, "_h", None):
@@ -275,6 +292,23 @@ def compile_check(name: str, kind: int, elem: int, inputs, params, exprs, gen=No
     r, s = C.c_int(), C.c_int()
     L.check(L.lib.mf_compile_check(C.byref(d), C.byref(r), C.byref(s)))
     return {"registers": r.value, "spill_bytes": s.value}
+
+
+def compile_check_resident(kernels, elem: int, native_f64: bool = False, f32_arith: bool = False) -> dict:
+    """NVRTC-compiles the resident module of one or two REDUCE kernels, each
+    given as (name, inputs, params, exprs), without a GPU: registers, spilled
+    bytes and the module's CUDA C."""
+    descs, keep = [], []
+    for name, inputs, params, exprs in kernels:
+        d, k = make_desc(name, L.MF_KERNEL_REDUCE, elem, inputs, params, exprs, None, native_f64, 0, 0, f32_arith,
+                         False, 0, None)
+        descs.append(d)
+        keep.append(k)
+    arr = (C.c_void_p * len(descs))(*[C.addressof(d) for d in descs])
+    r, s = C.c_int(), C.c_int()
+    buf = C.create_string_buffer(1 << 22)
+    L.check(L.lib.mf_compile_check_resident(arr, len(descs), C.byref(r), C.byref(s), buf, len(buf)))
+    return {"registers": r.value, "spill_bytes": s.value, "source": buf.value.decode()}
 
 
 def eval_expressions(names: Sequence[str], values: Sequence[float], exprs: Sequence[str]) -> np.ndarray:

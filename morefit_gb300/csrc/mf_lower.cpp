@@ -1744,6 +1744,7 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
     const std::string XT = ar == Ar::F32 ? "float" : (ar == Ar::F64 || ar == Ar::F32S) ? "double" : "mf_dw";
 
     s << "struct mf_args { double d[" << out.nd << "]; float f[" << out.nf << "]; };\n";
+    const auto entry_mark = s.tellp();
     // ---- single-dataset reduce ----
     s << "extern \"C\" __global__ void MF_BOUNDS " << out.entry << "(const " << DT
       << "* __restrict__ data, mf_u64 stride, mf_u64 n, mf_args P, float2* __restrict__ partials,"
@@ -1914,8 +1915,23 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
     __syncthreads();
     if (threadIdx.x == 0) *reinterpret_cast<volatile unsigned*>(status + 1) = seq;
   }
-}
 )CUDA";
+    if (!out.pipelined) {
+      std::string work = s.str().substr(size_t(body_mark));
+      auto replace_all = [](std::string& t, const std::string& from, const std::string& to) {
+        for (size_t p = t.find(from); p != std::string::npos; p = t.find(from, p + to.size())) t.replace(p, from.size(), to);
+      };
+      replace_all(work, "blockIdx.x", "mf_vb");
+      replace_all(work, "gridDim.x", "mf_grid");
+      out.resident_prefix = s.str().substr(0, size_t(entry_mark));
+      out.resident_data_type = DT;
+      out.resident_body = "__device__ __forceinline__ void mf_rbody(const " + DT +
+                          "* __restrict__ data, mf_u64 stride, mf_u64 n, const mf_args& P, float2* __restrict__ "
+                          "partials, unsigned* __restrict__ counter, double* __restrict__ out, unsigned* "
+                          "__restrict__ status, unsigned seq, unsigned mf_vb, unsigned mf_grid) {\n" +
+                          work + "}\n";
+    }
+    s << "}\n";
     // ---- batched evaluations: per-block partials only, then one combine ----
     // Evaluation e of a batch writes its partial rows to its own slot of the
     // batch's partial buffer without counting or combining, so consecutive

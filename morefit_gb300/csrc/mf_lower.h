@@ -88,6 +88,17 @@ struct LoweredKernel {
   // memory directly (pipelined = false).
   bool pipelined = false;
   int tile = 0, stages = 0;
+  // REDUCE kernels with direct loads: the single-evaluation entry's work as a
+  // device function for a resident module (mf_runtime.cpp), which holds one
+  // grid on the device and runs evaluations posted by the host:
+  // resident_prefix is the translation unit up to the entry points (helpers,
+  // macros, the argument struct), resident_body defines
+  //   mf_rbody(data, stride, n, const mf_args& P, partials, counter, out,
+  //            status, seq, unsigned block, unsigned grid)
+  // doing block `block` of a grid of `grid` blocks, i.e. the entry with
+  // blockIdx.x and gridDim.x replaced. Empty when not available.
+  std::string resident_prefix, resident_body;
+  std::string resident_data_type;  // element type mf_rbody reads ("float2", "double", "float")
   size_t smem_bytes = 0;  // dynamic shared memory of the main entry
   // REDUCE kernels: host-evaluated argument struct
   // Prepared input (REDUCE): the kernel reads `prep_cols.size()` columns that

@@ -180,6 +180,8 @@ int compile_source(const std::string& src, const std::string& name, std::shared_
 }  // namespace
 
 // ----------------------------------------------------------------- objects --
+struct ResState;  // resident evaluations of a context (the resident runtime below)
+
 struct mf_context {
   // Owner reference plus one per live buffer and kernel: the context (stream,
   // scratch) outlives everything allocated through it, whatever order the
@@ -222,6 +224,10 @@ struct mf_context {
   size_t ring_grids_cap = 0;
   // synchronous evaluations routed through a coalescer (mf_context_set_coalescer)
   mf_coalescer* coalescer = nullptr;
+  // resident evaluations (mf_context_set_resident): idle time after which the
+  // resident grid exits (0: off), and their state
+  uint64_t res_idle_ns = 0;
+  ResState* res = nullptr;
 };
 
 // A copy of a buffer's columns in the layout a REDUCE kernel reads (folded
@@ -310,10 +316,16 @@ int launch_reduce(mf_kernel* k, const void* data, uint64_t stride, uint64_t n, c
 // ---------------------------------------------------------------- helpers --
 namespace {
 
+void res_shutdown(mf_context* c);
+void res_drop(mf_context* c);
+void res_yield(mf_context* c);
+void res_forget(mf_kernel* k);
+
 void release_context(mf_context* c) {
   if (!c) return;
   if (c->refs.fetch_sub(1) != 1) return;
   cudaSetDevice(c->device);
+  res_shutdown(c);
   cudaStreamSynchronize(c->stream);
   if (c->partials) cudaFree(c->partials);
   if (c->counter) cudaFree(c->counter);
@@ -507,6 +519,7 @@ int prepare_input(const mf_kernel* k, const mf_buffer* in, uint64_t stride, cons
   void* dst = d->ptr;
   uint64_t rows = stride;
   void* args[] = {const_cast<void**>(&src), &stride, &rows, &dst};
+  res_yield(c);
   MF_CUDA_TRY(cudaLaunchKernel(reinterpret_cast<const void*>(k->fn_prep), dim3(grid), dim3(256), args, 0, c->stream));
   d->gen = in->gen;
   d->n = stride;
@@ -586,7 +599,9 @@ int mf_context_create(int device, uint64_t hbm_budget_bytes, mf_context** out) {
   MF_CUDA_TRY(cudaMemset(c->counter, 0, sizeof(unsigned)));
   MF_CUDA_TRY(cudaHostAlloc(reinterpret_cast<void**>(&c->status_host), 64, cudaHostAllocMapped));
   MF_CUDA_TRY(cudaHostGetDevicePointer(reinterpret_cast<void**>(&c->status), c->status_host, 0));
-  *c->status_host = 0u;
+  // all words: [1] is the completion word the first synchronous call waits
+  // for, and page-locked memory comes back from earlier allocations unzeroed
+  std::memset(c->status_host, 0, 64);
   int rc = ensure_scratch(c.get(), size_t(c->num_sms) * 8 * 64, 4096);
   if (rc) return rc;
   *out = c.release();
@@ -597,6 +612,11 @@ int mf_context_destroy(mf_context* c) {
   if (!c) return MF_OK;
   if (c->destroyed) return fail(MF_ERR_INVALID, "context destroyed twice");
   c->destroyed = true;
+  if (c->res) {
+    cudaSetDevice(c->device);
+    res_drop(c);  // the resident grid leaves now, not when the last kernel is freed
+    c->res_idle_ns = 0;
+  }
   release_context(c);
   return MF_OK;
 }
@@ -1274,6 +1294,7 @@ int mf_kernel_free(mf_kernel* k) {
   if (!k) return MF_OK;
   if (k->f64) mf_kernel_free(k->f64);
   mf_context* c = k->ctx;
+  res_forget(k);
   if (k->lib) {
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
@@ -1359,6 +1380,7 @@ int launch_reduce(mf_kernel* k, const void* data, uint64_t stride, uint64_t n, c
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
   cfg.numAttrs = dependent ? 1 : 0;
+  res_yield(k->ctx);
   MF_CUDA_TRY(cudaLaunchKernelExC(&cfg, reinterpret_cast<const void*>(k->fn), args));
   return MF_OK;
 }
@@ -1424,6 +1446,7 @@ int launch_batched(mf_kernel* k, uint32_t count, const void* const* data, const 
       attr[0].val.programmaticStreamSerializationAllowed = 1;
       cfg.attrs = attr;
       cfg.numAttrs = i > 0 ? 1 : 0;
+      res_yield(k->ctx);
       MF_CUDA_TRY(cudaLaunchKernelExC(&cfg, reinterpret_cast<const void*>(k->fn_part), args));
     }
     // pageable source: the copy is staged before the call returns
@@ -1463,6 +1486,10 @@ static int f64_twin(mf_kernel* k) {
 
 static int reduce_direct(mf_kernel* k, const mf_buffer* in, uint64_t stride, uint64_t n, const double* params,
                          uint32_t n_params, double* sums);
+namespace {
+int res_reduce(mf_kernel* k, const mf_buffer* in, uint64_t stride, uint64_t n, const double* params, double* sums,
+               bool* served);
+}
 int coalesced_reduce(mf_kernel* k, const mf_buffer* in, uint64_t stride, uint64_t n, const double* params,
                      uint32_t n_params, double* sums);
 
@@ -1479,6 +1506,13 @@ int mf_kernel_reduce(mf_kernel* k, const mf_buffer* in, uint64_t stride, uint64_
     if (rc) return rc;
     MF_CUDA_TRY(cudaSetDevice(k->ctx->device));
     return coalesced_reduce(k, in, stride, n, params, n_params, sums);
+  }
+  if (k->kind == MF_KERNEL_REDUCE && k->ctx->res && k->ctx->res_idle_ns && n_params == k->n_params &&
+      (params || !n_params) && check_layout(k, in, stride, n) == MF_OK) {
+    MF_CUDA_TRY(cudaSetDevice(k->ctx->device));
+    bool served = false;
+    const int rc = res_reduce(k, in, stride, n, params, sums, &served);
+    if (rc || served) return rc;
   }
   return reduce_direct(k, in, stride, n, params, n_params, sums);
 }
@@ -1523,6 +1557,552 @@ static int reduce_direct(mf_kernel* k, const mf_buffer* in, uint64_t stride, uin
   k->fallbacks++;
   return reduce_direct(k->f64, in, stride, n, params, n_params, sums);
 }
+
+// ---------------------------------------------------- resident evaluations --
+// A context with resident evaluations on (mf_context_set_resident) watches its
+// synchronous REDUCE calls. After kResWarmCalls of them it builds, on a
+// background thread, one module holding the per-block work (mf_rbody) of the
+// kernels those calls used most, each in a namespace of its own, and a
+// resident entry. That grid is launched once (cooperative: all its blocks
+// co-resident) and loops: block 0 waits for a request in mapped host memory,
+// copies it to device memory and releases the other blocks; every block then
+// runs the blocks [blockIdx.x, blockIdx.x + gridDim.x, ...) of the kernel's
+// own grid for that request (grid_for, as a launch would), and the block
+// that completes the count combines the partials and writes the sums and the
+// completion word as the single-evaluation entry does. A request's sums are
+// those of a launch of the kernel, bit for bit; what it saves is the launch.
+// The grid exits when idle for res_idle_ns, or when asked to (a launch of any
+// other work on the device, a kernel of the group freed, the context
+// destroyed): block 0 swaps the doorbell to kResExit with a system-scope
+// compare-and-swap only while no request is pending, so a posted request is
+// never dropped, and the host's compare-and-swap of the next request then
+// fails and it launches instead. Every wait on the device is bounded.
+constexpr unsigned kResExit = 0xffffffffu;
+constexpr size_t kResArgsMax = 2048;  // bytes of a member's argument struct
+constexpr unsigned kResWarmCalls = 8;
+constexpr size_t kResMaxMembers = 2;  // per-block shared memory: ~19 KB per member
+constexpr uint64_t kResMaxEvents = uint64_t(1) << 31;
+constexpr int64_t kResHoldNs = 20000000;  // no new grid for 20 ms after one was asked to exit
+
+struct ResReq {  // the generated mfr_req
+  uint64_t data, stride, n;
+  double* out;
+  uint32_t which, grid, seq, pad;
+  unsigned char args[kResArgsMax];
+};
+static_assert(sizeof(ResReq) % 16 == 0, "the request is copied in 16-byte words");
+struct ResMail {  // the generated mfr_mail (mapped host memory)
+  unsigned seq;   // last posted request; kResExit once the grid has left its loop
+  unsigned stop;  // nonzero: leave the loop when idle
+  unsigned pad[30];
+  ResReq req;
+};
+
+struct ResState {
+  // warm-up: the REDUCE kernels of the first synchronous calls, with call counts
+  std::vector<std::pair<mf_kernel*, unsigned>> seen;
+  unsigned calls = 0;
+  std::thread builder;
+  std::atomic<int> state{0};  // 0 watching, 1 building, 2 ready, 3 unavailable
+  std::string error;
+  // the module (valid once state == 2)
+  std::vector<mf_kernel*> members;
+  cudaLibrary_t lib = nullptr;
+  cudaKernel_t fn = nullptr;
+  int grid = 0, block = 0;
+  ResMail* mail = nullptr;  // mapped host memory
+  ResMail* mail_dev = nullptr;
+  ResReq* req = nullptr;  // device copy of the current request
+  unsigned* go = nullptr;
+  float2* partials = nullptr;
+  unsigned* counter = nullptr;
+  cudaStream_t stream = nullptr;
+  // the grid (alive and the device's owner table change under g_res_mu)
+  bool alive = false;
+  unsigned posted = 0;
+  std::atomic<int64_t> hold_until{0};
+  uint64_t served = 0, grids = 0;
+};
+
+namespace {
+
+std::mutex g_res_mu;
+mf_context* g_res_owner[64] = {};  // per device: the context whose grid is up
+std::atomic<int> g_res_up[64];     // per device: a grid may be up (checked without the lock)
+
+int64_t steady_ns() {
+  return std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now().time_since_epoch())
+      .count();
+}
+
+// Asks the grid up on c's device (whichever context owns it) to exit once
+// idle; called before every other launch of this library on the device.
+void res_yield(mf_context* c) {
+  const int d = c->device;
+  if (d < 0 || d >= 64 || !g_res_up[d].load(std::memory_order_acquire)) return;
+  std::lock_guard<std::mutex> lk(g_res_mu);
+  mf_context* o = g_res_owner[d];
+  if (!o || !o->res || !o->res->alive) return;
+  __atomic_store_n(&o->res->mail->stop, 1u, __ATOMIC_RELEASE);
+  o->res->hold_until.store(steady_ns() + kResHoldNs);
+}
+
+// After the grid left (or was asked to leave) its loop: wait for it and
+// release the device.
+void res_end(mf_context* c) {
+  ResState& r = *c->res;
+  cudaStreamSynchronize(r.stream);
+  std::lock_guard<std::mutex> lk(g_res_mu);
+  r.alive = false;
+  if (g_res_owner[c->device] == c) {
+    g_res_owner[c->device] = nullptr;
+    g_res_up[c->device].store(0, std::memory_order_release);
+  }
+}
+
+void res_stop(mf_context* c) {
+  ResState* r = c->res;
+  if (!r || !r->alive) return;
+  __atomic_store_n(&r->mail->stop, 1u, __ATOMIC_RELEASE);
+  res_end(c);
+}
+
+// Drops the module and the warm-up record (the grid stopped first).
+void res_drop(mf_context* c) {
+  ResState& r = *c->res;
+  res_stop(c);
+  if (r.builder.joinable()) r.builder.join();
+  if (r.stream) cudaStreamSynchronize(r.stream);  // a grid that left while idle may still be finishing
+  if (r.lib) cudaLibraryUnload(r.lib);
+  if (r.mail) cudaFreeHost(r.mail);
+  if (r.req) cudaFree(r.req);
+  if (r.go) cudaFree(r.go);
+  if (r.partials) cudaFree(r.partials);
+  if (r.counter) cudaFree(r.counter);
+  if (r.stream) cudaStreamDestroy(r.stream);
+  r.lib = nullptr;
+  r.fn = nullptr;
+  r.mail = r.mail_dev = nullptr;
+  r.req = nullptr;
+  r.go = r.counter = nullptr;
+  r.partials = nullptr;
+  r.stream = nullptr;
+  r.members.clear();
+  r.seen.clear();
+  r.calls = 0;
+  r.state.store(0);
+}
+
+void res_shutdown(mf_context* c) {
+  if (!c->res) return;
+  res_drop(c);
+  delete c->res;
+  c->res = nullptr;
+}
+
+void res_forget(mf_kernel* k) {
+  mf_context* c = k->ctx;
+  if (!c || !c->res) return;
+  ResState& r = *c->res;
+  if (r.builder.joinable()) r.builder.join();
+  bool used = std::find(r.members.begin(), r.members.end(), k) != r.members.end();
+  for (auto& e : r.seen) used = used || e.first == k;
+  if (used) res_drop(c);
+}
+
+// The resident module's source: every member's translation unit up to its
+// entry points plus mf_rbody, in namespace mfr<i> (its macros undefined after
+// it), and the resident entry.
+std::string res_source(const std::vector<const mf::LoweredKernel*>& m, int block, int min_blocks = 1) {
+  std::ostringstream s;
+  s << "// MoreFit CUDA backend: resident evaluations of " << m.size() << " REDUCE kernels\n";
+  for (size_t i = 0; i < m.size(); i++) {
+    const mf::LoweredKernel& L = *m[i];
+    s << "namespace mfr" << i << " {\n" << L.resident_prefix << L.resident_body << "}  // namespace mfr" << i << "\n";
+    std::vector<std::string> macros;
+    std::istringstream t(L.resident_prefix);
+    for (std::string line; std::getline(t, line);)
+      if (line.rfind("#define ", 0) == 0) {
+        size_t e = 8;
+        while (e < line.size() && (std::isalnum((unsigned char)line[e]) || line[e] == '_')) e++;
+        macros.push_back(line.substr(8, e - 8));
+      }
+    for (const auto& x : macros) s << "#undef " << x << "\n";
+  }
+  s << "typedef unsigned long long mfr_u64;\n"
+    << "struct mfr_req { mfr_u64 data, stride, n; double* out; unsigned which, grid, seq, pad; unsigned char args["
+    << kResArgsMax << "]; };\n"
+    << "struct mfr_mail { unsigned seq; unsigned stop; unsigned pad[30]; mfr_req req; };\n"
+    << "#define MFR_EXIT 0xffffffffu\n#define MFR_BLOCK " << block << "\n#define MFR_MINB " << min_blocks << "\n";
+  size_t args_max = 8;
+  for (const auto* L : m) args_max = std::max(args_max, L->args_bytes());
+  s << "#define MFR_WORDS " << (48 + args_max + 3) / 4 << "  // request header (48 bytes) and the largest argument struct\n";
+  s << R"CUDA(__device__ __forceinline__ unsigned mfr_ld_acq_sys(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.sys.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ unsigned mfr_ld_rlx_sys(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.relaxed.sys.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ unsigned mfr_ld_acq_gpu(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void mfr_st_rel_gpu(unsigned* p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned mfr_cas_sys(unsigned* p, unsigned cmp, unsigned val) {
+  unsigned old;
+  asm volatile("atom.acq_rel.sys.global.cas.b32 %0, [%1], %2, %3;" : "=r"(old) : "l"(p), "r"(cmp), "r"(val) : "memory");
+  return old;
+}
+__device__ __forceinline__ mfr_u64 mfr_now() {
+  mfr_u64 t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// status[0] bit 8: a block gave up waiting for block 0 (the grid then leaves).
+extern "C" __global__ void __launch_bounds__(MFR_BLOCK, MFR_MINB) mf_resident(mfr_mail* mail, mfr_req* req, unsigned* go,
+                                                                   float2* partials, unsigned* counter,
+                                                                   unsigned* status, mfr_u64 idle_ns) {
+  __shared__ unsigned mfr_v;
+  __shared__ __align__(16) unsigned mfr_rq[MFR_WORDS];
+  unsigned seen = 0u;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      const mfr_u64 t0 = mfr_now();
+      unsigned v = seen;
+      if (blockIdx.x == 0) {
+        // the host's doorbell; idle (or asked to stop): leave, unless a request
+        // was posted meanwhile (the compare-and-swap then fails and returns it)
+        for (unsigned it = 0;; it++) {
+          v = mfr_ld_acq_sys(&mail->seq);
+          if (v != seen) break;
+          if ((it & 3u) == 3u && (mfr_ld_rlx_sys(&mail->stop) != 0u || mfr_now() - t0 > idle_ns)) {
+            const unsigned o = mfr_cas_sys(&mail->seq, seen, MFR_EXIT);
+            v = o == seen ? MFR_EXIT : o;
+            break;
+          }
+          __nanosleep(32);
+        }
+      } else {
+        // block 0's release of the request; block 0 leaves after idle_ns at
+        // most and releases the exit the same way
+        for (unsigned it = 0;; it++) {
+          v = mfr_ld_acq_gpu(go);
+          if (v != seen) break;
+          if ((it & 63u) == 63u && mfr_now() - t0 > idle_ns + 2000000000ull) {
+            atomicOr(status, 8u);
+            v = MFR_EXIT;
+            break;
+          }
+          __nanosleep(32);
+        }
+      }
+      mfr_v = v;
+    }
+    __syncthreads();
+    const unsigned v = mfr_v;
+    if (blockIdx.x == 0) {
+      if (v != MFR_EXIT) {
+        const uint4* src = reinterpret_cast<const uint4*>(&mail->req);
+        uint4* dst = reinterpret_cast<uint4*>(req);
+        for (unsigned q = threadIdx.x; q < sizeof(mfr_req) / 16; q += MFR_BLOCK) dst[q] = __ldcv(src + q);
+        __threadfence();
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) mfr_st_rel_gpu(go, v);
+    }
+    __syncthreads();
+    if (v == MFR_EXIT) return;
+    seen = v;
+    // the request's header and argument struct, staged in shared memory by
+    // the first warps: loads of the same words by every thread of the grid
+    // would all go to one L2 slice
+    for (unsigned w = threadIdx.x; w < MFR_WORDS; w += MFR_BLOCK)
+      mfr_rq[w] = __ldcg(reinterpret_cast<const unsigned*>(req) + w);
+    __syncthreads();
+    const mfr_u64* h64 = reinterpret_cast<const mfr_u64*>(mfr_rq);
+    const void* data = reinterpret_cast<const void*>(h64[0]);
+    const mfr_u64 stride = h64[1], n = h64[2];
+    double* out = reinterpret_cast<double*>(h64[3]);
+    const unsigned which = mfr_rq[8], grid = mfr_rq[9], seq = mfr_rq[10];
+    switch (which) {
+)CUDA";
+  for (size_t i = 0; i < m.size(); i++) {
+    const std::string ns = "mfr" + std::to_string(i);
+    s << "    case " << i << ": {\n"
+      << "      const " << ns << "::mf_args& A = *reinterpret_cast<const " << ns << "::mf_args*>(mfr_rq + 12);\n"
+      << "      for (unsigned vb = blockIdx.x; vb < grid; vb += gridDim.x) {\n"
+      << "        __syncthreads();\n"
+      << "        " << ns << "::mf_rbody(static_cast<const " << m[i]->resident_data_type
+      << "*>(data), stride, n, A, partials, counter, out, status, seq, vb, grid);\n"
+      << "      }\n      break;\n    }\n";
+  }
+  s << "    default: break;\n    }\n  }\n}\n";
+  return s.str();
+}
+
+// Background build of the module for `members` (sets state 2, or 3 with error).
+void res_build(mf_context* c, std::vector<mf_kernel*> members) {
+  ResState& r = *c->res;
+  auto give_up = [&](const std::string& why) {
+    r.error = why;
+    r.state.store(3, std::memory_order_release);
+  };
+  if (cudaSetDevice(c->device) != cudaSuccess) return give_up("cudaSetDevice");
+  const int block = members[0]->lowered.block;
+  size_t part = 0;
+  for (mf_kernel* k : members)
+    part = std::max(part, size_t(c->num_sms) * size_t(k->blocks_per_sm) * size_t(k->n_outputs));
+  std::vector<const mf::LoweredKernel*> lowered;
+  for (mf_kernel* k : members) lowered.push_back(&k->lowered);
+  int member_spill = 0, want = 1;
+  for (mf_kernel* k : members) {
+    member_spill = std::max(member_spill, k->image ? k->image->spill : 0);
+    want = std::max(want, k->blocks_per_sm);
+  }
+  // as many resident blocks per SM as the member that launches the most
+  // (fewer make its blocks run in rounds): the largest count down from there
+  // whose register cap spills no more than the kernels themselves
+  std::shared_ptr<CompiledImage> img;
+  for (int mb = want; mb >= 1 && !img; mb--)
+    if (compile_source(res_source(lowered, block, mb), "mf_resident", img, "mf_resident") != MF_OK ||
+        img->spill > member_spill)
+      img.reset();
+  if (!img) return give_up("the resident module spills more than its kernels");
+  if (cudaLibraryLoadData(&r.lib, img->cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0) != cudaSuccess ||
+      cudaLibraryGetKernel(&r.fn, r.lib, "mf_resident") != cudaSuccess)
+    return give_up("loading the resident module");
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, reinterpret_cast<const void*>(r.fn), block, 0) !=
+          cudaSuccess ||
+      nb < 1)
+    return give_up("the resident entry does not fit on an SM");
+  r.grid = c->num_sms * std::min(nb, want);
+  r.block = block;
+  if (cudaHostAlloc(reinterpret_cast<void**>(&r.mail), sizeof(ResMail), cudaHostAllocMapped) != cudaSuccess ||
+      cudaHostGetDevicePointer(reinterpret_cast<void**>(&r.mail_dev), r.mail, 0) != cudaSuccess ||
+      cudaMalloc(reinterpret_cast<void**>(&r.req), sizeof(ResReq)) != cudaSuccess ||
+      cudaMalloc(reinterpret_cast<void**>(&r.go), sizeof(unsigned)) != cudaSuccess ||
+      cudaMalloc(reinterpret_cast<void**>(&r.counter), sizeof(unsigned)) != cudaSuccess ||
+      cudaMalloc(reinterpret_cast<void**>(&r.partials), std::max<size_t>(part, 1) * sizeof(float2)) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&r.stream, cudaStreamNonBlocking) != cudaSuccess)
+    return give_up("resident scratch allocation");
+  std::memset(r.mail, 0, sizeof(ResMail));
+  r.members = std::move(members);
+  r.state.store(2, std::memory_order_release);
+}
+
+// Launches the grid (the device's previous owner gone): false when another
+// context's grid holds the device or the launch failed.
+bool res_start(mf_context* c) {
+  ResState& r = *c->res;
+  r.mail->seq = 0u;
+  r.mail->stop = 0u;
+  r.posted = 0u;
+  {
+    std::lock_guard<std::mutex> lk(g_res_mu);
+    mf_context*& o = g_res_owner[c->device];
+    if (o && o != c) {
+      // another context's grid: still up unless it has left its loop (idle);
+      // its owner learns that from its next post
+      if (__atomic_load_n(&o->res->mail->seq, __ATOMIC_ACQUIRE) != kResExit) return false;
+      o->res->alive = false;
+    }
+    o = c;
+    g_res_up[c->device].store(1, std::memory_order_release);
+    r.alive = true;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(unsigned(r.grid));
+  cfg.blockDim = dim3(unsigned(r.block));
+  cfg.stream = r.stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  ResMail* mail = r.mail_dev;
+  ResReq* req = r.req;
+  unsigned* go = r.go;
+  float2* partials = r.partials;
+  unsigned* counter = r.counter;
+  unsigned* status = c->status;
+  unsigned long long idle = c->res_idle_ns;
+  void* args[] = {&mail, &req, &go, &partials, &counter, &status, &idle};
+  if (cudaMemsetAsync(r.go, 0, sizeof(unsigned), r.stream) != cudaSuccess ||
+      cudaMemsetAsync(r.counter, 0, sizeof(unsigned), r.stream) != cudaSuccess ||
+      cudaLaunchKernelExC(&cfg, reinterpret_cast<const void*>(r.fn), args) != cudaSuccess) {
+    cudaGetLastError();
+    res_end(c);
+    r.state.store(3);
+    r.error = "cooperative launch of the resident grid failed";
+    return false;
+  }
+  r.grids++;
+  return true;
+}
+
+// One synchronous evaluation through the resident grid. *served false: not
+// served, nothing changed (the caller launches as usual).
+int res_reduce(mf_kernel* k, const mf_buffer* in, uint64_t stride, uint64_t n, const double* params, double* sums,
+               bool* served) {
+  *served = false;
+  mf_context* c = k->ctx;
+  ResState& r = *c->res;
+  if (k->lowered.resident_body.empty() || k->lowered.args_bytes() > kResArgsMax || n == 0 || n > kResMaxEvents)
+    return MF_OK;
+  const int st = r.state.load(std::memory_order_acquire);
+  if (st == 0) {
+    auto it = std::find_if(r.seen.begin(), r.seen.end(), [&](const auto& e) { return e.first == k; });
+    if (it != r.seen.end())
+      it->second++;
+    else if (r.seen.empty() || r.seen[0].first->lowered.block == k->lowered.block)
+      r.seen.emplace_back(k, 1u);
+    if (++r.calls >= kResWarmCalls) {
+      auto by_use = r.seen;
+      std::stable_sort(by_use.begin(), by_use.end(), [](const auto& a, const auto& b) { return a.second > b.second; });
+      std::vector<mf_kernel*> members;
+      for (size_t i = 0; i < by_use.size() && i < kResMaxMembers; i++) members.push_back(by_use[i].first);
+      r.state.store(1);
+      r.builder = std::thread(res_build, c, std::move(members));
+    }
+    return MF_OK;
+  }
+  if (st != 2) return MF_OK;
+  const auto mit = std::find(r.members.begin(), r.members.end(), k);
+  if (mit == r.members.end()) return MF_OK;
+  // the prepared copy must be current (a launch makes it) and nothing may be
+  // pending on the context's stream (it could write what this reads)
+  const void* data = in->ptr;
+  if (k->lowered.prep) {
+    data = nullptr;
+    for (const auto& x : in->derived)
+      if (x.key == k->prep_key && x.gen == in->gen && x.stride == stride) data = x.ptr;
+    if (!data) return MF_OK;
+  }
+  if (cudaStreamQuery(c->stream) != cudaSuccess) {
+    cudaGetLastError();
+    return MF_OK;
+  }
+  if (r.alive && __atomic_load_n(&r.mail->stop, __ATOMIC_ACQUIRE)) {
+    res_end(c);  // asked to make room (another launch on the device): it leaves now, idle
+    return MF_OK;
+  }
+  if (!r.alive) {
+    if (steady_ns() < r.hold_until.load()) return MF_OK;
+    if (!res_start(c)) return MF_OK;
+  }
+  int rc = ensure_scratch(c, 0, k->n_outputs);
+  if (rc) return rc;
+  ResReq& q = r.mail->req;
+  q.data = reinterpret_cast<uint64_t>(data);
+  q.stride = stride;
+  q.n = n;
+  q.out = c->out_dev;
+  q.which = uint32_t(mit - r.members.begin());
+  q.grid = uint32_t(mfi::grid_for(k, n));
+  if (++c->sync_seq == 0u) c->sync_seq = 1u;
+  const unsigned seq = c->sync_seq;
+  q.seq = seq;
+  try {
+    k->lowered.fill_args(params, k->n_params, q.args);
+  } catch (const std::exception& e) {
+    return fail(MF_ERR_INVALID, std::string("parameter evaluation: ") + e.what());
+  }
+  *c->status_host = 0u;
+  unsigned expected = r.posted;
+  unsigned desired = r.posted + 1u;
+  if (desired == kResExit || desired == 0u) desired = 1u;
+  if (!__atomic_compare_exchange_n(&r.mail->seq, &expected, desired, false, __ATOMIC_RELEASE, __ATOMIC_RELAXED)) {
+    res_end(c);  // the grid left its loop; launch instead
+    return MF_OK;
+  }
+  r.posted = desired;
+  *served = true;
+  // completion word; the grid's waits are bounded, so is this one
+  const int64_t t0 = steady_ns();
+  for (unsigned spins = 0; __atomic_load_n(c->status_host + 1, __ATOMIC_ACQUIRE) != seq; spins++) {
+    if ((spins & 1023u) == 0u && steady_ns() - t0 > int64_t(10) * 1000000000) {
+      __atomic_store_n(&r.mail->stop, 1u, __ATOMIC_RELEASE);
+      res_end(c);
+      return fail(MF_ERR_TIMEOUT, "a resident evaluation did not complete");
+    }
+  }
+  std::memcpy(sums, c->out_host, k->n_outputs * sizeof(double));
+  r.served++;
+  rc = check_status(c);
+  if (rc || !k->desc || all_finite(sums, k->n_outputs)) return rc;
+  rc = f64_twin(k);
+  if (rc) return rc;
+  k->fallbacks++;
+  return reduce_direct(k->f64, in, stride, n, params, k->n_params, sums);
+}
+
+}  // namespace
+
+extern "C" {
+
+int mf_context_set_resident(mf_context* c, uint32_t idle_us) {
+  if (!c) return fail(MF_ERR_INVALID, "null context");
+  if (idle_us == 0) {
+    if (c->res) res_drop(c);
+    c->res_idle_ns = 0;
+    return MF_OK;
+  }
+  int atomics = 0, coop = 0;
+  MF_CUDA_TRY(cudaDeviceGetAttribute(&atomics, cudaDevAttrHostNativeAtomicSupported, c->device));
+  MF_CUDA_TRY(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, c->device));
+  if (!atomics || !coop)
+    return fail(MF_ERR_UNSUPPORTED, "resident evaluations need host-native atomics and cooperative launches");
+  if (!c->res) c->res = new ResState();
+  c->res_idle_ns = uint64_t(idle_us) * 1000u;
+  return MF_OK;
+}
+
+int mf_compile_check_resident(const mf_kernel_desc* const* descs, uint32_t count, int* regs, int* spill,
+                              char* source, size_t len) {
+  if (!descs || count == 0 || count > kResMaxMembers) return fail(MF_ERR_INVALID, "one or two kernel descriptions");
+  std::vector<mf::LoweredKernel> lk(count);
+  std::vector<const mf::LoweredKernel*> ptrs;
+  for (uint32_t i = 0; i < count; i++) {
+    if (!descs[i] || descs[i]->kind != MF_KERNEL_REDUCE) return fail(MF_ERR_INVALID, "REDUCE kernels only");
+    int rc = lower_desc(descs[i], lk[i]);
+    if (rc) return rc;
+    if (lk[i].resident_body.empty()) return fail(MF_ERR_UNSUPPORTED, "kernel has no resident form");
+    if (lk[i].block != lk[0].block) return fail(MF_ERR_INVALID, "members differ in block size");
+    ptrs.push_back(&lk[i]);
+  }
+  const std::string src = res_source(ptrs, lk[0].block);
+  if (source && len) {
+    const size_t n = std::min(len - 1, src.size());
+    std::memcpy(source, src.data(), n);
+    source[n] = '\0';
+  }
+  std::shared_ptr<CompiledImage> img;
+  int rc = compile_source(src, "mf_resident", img, "mf_resident");
+  if (rc) return rc;
+  if (regs) *regs = img->regs;
+  if (spill) *spill = img->spill;
+  return MF_OK;
+}
+
+int mf_context_resident_stats(const mf_context* c, int* state, uint64_t* grids, uint64_t* served, int* blocks) {
+  if (!c) return fail(MF_ERR_INVALID, "null context");
+  const ResState* r = c->res;
+  if (blocks) *blocks = r && r->state.load() == 2 ? r->grid : 0;
+  if (state) *state = r ? r->state.load() : -1;
+  if (grids) *grids = r ? r->grids : 0;
+  if (served) *served = r ? r->served : 0;
+  return MF_OK;
+}
+
+}  // extern "C"
 
 extern "C" {
 
@@ -1666,6 +2246,7 @@ int mf_kernel_reduce_segments(mf_kernel* k, const mf_buffer* in, uint64_t stride
   rc = prepare_input(k, in, stride, &data);
   if (rc) return rc;
   void* args[] = {const_cast<void**>(&data), &stride, &d_begin, &d_count, const_cast<void**>(&d_par), &outp};
+  res_yield(k->ctx);
   MF_CUDA_TRY(cudaLaunchKernel(reinterpret_cast<const void*>(k->fn_seg), dim3(nseg), dim3(k->lowered.block), args, 0,
                                c->stream));
   MF_CUDA_TRY(cudaStreamSynchronize(c->stream));
@@ -1723,6 +2304,7 @@ static int kernel_store(mf_kernel* k, const mf_buffer* in, uint64_t in_stride, u
   void* outp = out->ptr;
   out->gen++;
   void* args[] = {const_cast<void**>(&data), &in_stride, &n, pv.data(), &outp, &out_stride};
+  res_yield(k->ctx);
   MF_CUDA_TRY(cudaLaunchKernel(reinterpret_cast<const void*>(k->fn), dim3(grid), dim3(k->lowered.block), args, 0,
                                c->stream));
   if (sync) MF_CUDA_TRY(cudaStreamSynchronize(c->stream));
@@ -1766,6 +2348,7 @@ static int kernel_generate(mf_kernel* k, const uint32_t* seeds, uint32_t nseeds,
   unsigned long long mt = max_tries ? max_tries : 1000000000ULL;
   void* args[] = {&sd, &nseeds, &n, &nper, pv.data(), &outp, &out_stride, &status, &mt};
   const unsigned grid = (nseeds + k->lowered.block - 1) / k->lowered.block;
+  res_yield(k->ctx);
   MF_CUDA_TRY(cudaLaunchKernel(reinterpret_cast<const void*>(k->fn), dim3(grid), dim3(k->lowered.block), args, 0,
                                c->stream));
   if (!sync) return MF_OK;
@@ -1834,6 +2417,7 @@ int mf_kernel_generate_segments(mf_kernel* k, const uint32_t* seeds, uint32_t nt
   void* args[] = {&d_seeds, &nthreads, &threads_per_seg, &d_begin, &d_count, const_cast<void**>(&d_par), &d_max,
                   &outp, &out_stride, &status, &mt};
   const unsigned grid = (nthreads + k->lowered.block - 1) / k->lowered.block;
+  res_yield(k->ctx);
   MF_CUDA_TRY(cudaLaunchKernel(reinterpret_cast<const void*>(k->fn_seg), dim3(grid), dim3(k->lowered.block), args, 0,
                                c->stream));
   MF_CUDA_TRY(cudaStreamSynchronize(c->stream));
@@ -1937,6 +2521,7 @@ int launch_multi(mf_context* c, mf_kernel* k0, const std::vector<MultiItem>& ite
   const unsigned* d_grids = reinterpret_cast<const unsigned*>(base + b_seg + b_args);
   float2* ring = c->ring;
   void* margs[] = {const_cast<void**>(&d_segs), const_cast<void**>(&d_args), &ring};
+  res_yield(k0->ctx);
   MF_CUDA_TRY(cudaLaunchKernel(reinterpret_cast<const void*>(k0->fn_multi), dim3(unsigned(nseg)),
                                dim3(k0->lowered.block), margs, 0, c->stream));
   const float2* cring = ring;

@@ -24,13 +24,16 @@
 //                                          backend fitting that file, at once
 //                                          (one thread after another: serial),
 //                                          through a shared coalescer or not
-//   dropin calls <workload> <events.f64> <count> [mixed]
+//   dropin calls <workload> <events.f64> <count> [mixed] [launch]
 //                                          latency of the fitter's FCN
 //                                          evaluations after one fit: count
 //                                          calls each of likelihood_and_gradient
-//                                          (what MIGRAD calls) and likelihood,
-//                                          at the fitted point; prints
-//                                          percentiles in microseconds
+//                                          (what MIGRAD calls), likelihood, and
+//                                          MIGRAD's pattern (a gradient, two
+//                                          values), at the fitted point, served
+//                                          by the resident grid (default) or
+//                                          with a launch per call (launch);
+//                                          prints percentiles in microseconds
 #define MOREFIT_H 1
 #include <algorithm>
 #include <atomic>
@@ -295,12 +298,13 @@ static int cmd_genfit(const std::string& which, unsigned n, const char* prec) {
 // fit builds the kernels and uploads the events, then each timed call is one
 // FCN evaluation as Minuit2 makes it (hoisted parameter buffers on the host,
 // CopyToParameterBuffer, SubmitKernel, Finish, CopyFromKahanBuffer).
-static int cmd_calls(const std::string& which, const std::string& path, int count, bool mixed) {
+static int cmd_calls(const std::string& which, const std::string& path, int count, bool mixed, bool launch) {
   typedef double kT;
   typedef double eT;
   compute_options copts;
   cuda_options cu;
   cu.mixed_precision = mixed;
+  if (launch) cu.resident_idle_us = 0;
   CUDABackend backend(&copts, cu);
   if (!backend.ok()) {
     std::printf("{\"skipped\":\"%s\"}\n", backend.error().c_str());
@@ -342,10 +346,26 @@ static int cmd_calls(const std::string& which, const std::string& path, int coun
     auto t1 = std::chrono::steady_clock::now();
     if (i >= 50) tl.push_back(std::chrono::duration<double, std::micro>(t1 - t0).count());
   }
-  std::printf("{\"workload\":\"%s\",\"n\":%u,\"mixed\":%s,\"fit_ok\":%s,\"count\":%d,"
-              "\"likelihood_and_gradient_us\":%s,\"likelihood_us\":%s,\"finite\":%s}\n",
-              which.c_str(), n, mixed ? "true" : "false", ok ? "true" : "false", count, pct(tg).c_str(),
-              pct(tl).c_str(), std::isfinite(sink) ? "true" : "false");
+  // MIGRAD's pattern: a gradient, then line-search values
+  std::vector<double> ta;
+  for (int i = 0; i < count + 50; i++) {
+    auto t0 = std::chrono::steady_clock::now();
+    sink += fit.likelihood_and_gradient(np, g.data());
+    sink += fit.likelihood();
+    sink += fit.likelihood();
+    auto t1 = std::chrono::steady_clock::now();
+    if (i >= 50) ta.push_back(std::chrono::duration<double, std::micro>(t1 - t0).count() / 3.0);
+  }
+  int state = -1, blocks = 0;
+  uint64_t grids = 0, served = 0;
+  mf_context_resident_stats(backend.context(), &state, &grids, &served, &blocks);
+  std::printf("{\"workload\":\"%s\",\"n\":%u,\"mixed\":%s,\"resident\":%s,\"fit_ok\":%s,\"count\":%d,"
+              "\"likelihood_and_gradient_us\":%s,\"likelihood_us\":%s,\"migrad_pattern_us_per_call\":%s,"
+              "\"resident_stats\":{\"state\":%d,\"grids\":%llu,\"served\":%llu,\"blocks\":%d},"
+              "\"finite\":%s}\n",
+              which.c_str(), n, mixed ? "true" : "false", launch ? "false" : "true", ok ? "true" : "false", count,
+              pct(tg).c_str(), pct(tl).c_str(), pct(ta).c_str(), state, (unsigned long long)grids,
+              (unsigned long long)served, blocks, std::isfinite(sink) ? "true" : "false");
   return ok ? 0 : 1;
 }
 
@@ -433,7 +453,7 @@ int main(int argc, char** argv) {
       "usage: dropin lower <workload> | dropin fit <workload> <events.f64> [f32|mixed] | "
       "dropin genfit <workload> <n> [f32] | "
       "dropin threads <workload> <coalesce|plain|serial> <f64|mixed> <events.f64>... | "
-      "dropin calls <workload> <events.f64> <count> [mixed]\n";
+      "dropin calls <workload> <events.f64> <count> [mixed] [launch]\n";
   if (argc < 3) {
     std::fprintf(stderr, "%s", usage.c_str());
     return 2;
@@ -449,8 +469,14 @@ int main(int argc, char** argv) {
     const unsigned n = unsigned(std::stoul(argv[3]));
     return is_f32(4) ? cmd_genfit<float>(which, n, "float") : cmd_genfit<double>(which, n, "double");
   }
-  if (mode == "calls" && argc >= 5)
-    return cmd_calls(which, argv[3], std::atoi(argv[4]), argc > 5 && std::string(argv[5]) == "mixed");
+  if (mode == "calls" && argc >= 5) {
+    bool mixed = false, launch = false;
+    for (int i = 5; i < argc; i++) {
+      mixed = mixed || std::string(argv[i]) == "mixed";
+      launch = launch || std::string(argv[i]) == "launch";
+    }
+    return cmd_calls(which, argv[3], std::atoi(argv[4]), mixed, launch);
+  }
   if (mode == "threads" && argc >= 6) {
     std::vector<std::string> files(argv + 5, argv + argc);
     return cmd_threads(which, argv[3], std::string(argv[4]) == "mixed", files);

@@ -150,3 +150,28 @@ def test_expression_set_matches_single_evaluation():
     got = ExpressionSet(names, exprs).eval(rows)
     for r in range(len(rows)):
         assert np.array_equal(got[r], eval_expressions(names, rows[r], exprs))
+
+
+@pytest.mark.parametrize("workload", ["pwave", "mass", "spwave"])
+@pytest.mark.parametrize("elem", [0, 1])
+def test_resident_module_compiles(workload, elem):
+    """The resident module of a fit's two synchronous kernels (NLL and
+    NLL + gradient): each kernel's per-block work in its own namespace, its
+    macros undefined after it, one resident entry; it compiles for sm_103a
+    (spills as its kernels do), and each member's work is its
+    single-evaluation entry's with blockIdx.x / gridDim.x as parameters."""
+    from morefit_gb300 import _lib as L
+    from morefit_gb300.backend import compile_check_resident
+    g = load_golden(f"{workload}_n1000.json" if workload != "spwave" else "spwave_n2000.json")
+    ks = [kernel_spec(g, n) for n in ("lh_kernel", "lh_grad_kernel")]
+    info = compile_check_resident([(k["name"], k["inputs"], k["params"], k["exprs"]) for k in ks], elem)
+    # as for the kernels themselves: the P-wave never spills; a double-float
+    # body that calls an FP64 function (exp in the mass fit) may keep a call frame
+    assert info["registers"] > 0 and info["spill_bytes"] <= (0 if workload == "pwave" else 64), info
+    src = info["source"]
+    assert "namespace mfr0 {" in src and "namespace mfr1 {" in src and "#undef MF_NOUT" in src
+    assert src.count('extern "C"') == 1 and "mf_resident(" in src
+    body = src[src.index("void mf_rbody("):src.index("}  // namespace mfr0")]
+    assert "blockIdx.x" not in body and "gridDim.x" not in body
+    single = _entry(_src(g, "lh_kernel", elem), "mf_reduce(")
+    assert single.count("__syncthreads()") == body.count("__syncthreads()")
