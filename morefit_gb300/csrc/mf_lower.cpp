@@ -12,6 +12,12 @@
 
 namespace mf {
 
+// REDUCE kernels with more than kAccRegMax outputs keep the per-thread
+// partials of as many outputs as fit in kAccSmemBytes of shared memory per
+// block there (the last ones), and at least kAccRegMin in registers.
+constexpr int kAccRegMax = 64, kAccRegMin = 8;
+constexpr size_t kAccSmemBytes = 40 * 1024;
+
 namespace {
 
 bool is_unary_fn(Op op) {
@@ -1081,6 +1087,20 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
     // on GB300 (K*mumu gradient 11.4 vs 12.1 us per 1M-event evaluation in
     // double-float, 5.9 vs 6.5 us in FP32); Hessian-sized kernels keep their
     // accumulators in registers with one iteration in flight.
+    // Many-output double-float kernels (the S+P-wave Hessian: 105 outputs)
+    // cannot keep every per-thread partial in registers: the outputs beyond
+    // acc_reg keep theirs in shared memory instead (each thread its own
+    // column, 8 bytes per output), in blocks of 64 threads unless a block
+    // size is asked for, so that the kernel neither spills nor reads the
+    // dataset more than once (S+P-wave Hessian at 1M events, batched: 157 us,
+    // against 301 us spilling and 189 us as three register-only kernels).
+    // FP32 partials are cheap enough that the shared-memory traffic costs more
+    // than it saves (85 us against 49 us as three kernels): not for FP32.
+    if (!out.pipelined && int(exprs.size()) > kAccRegMax && dw_default) {
+      if (block_req == 0) out.block = 64;
+      const int room = int(kAccSmemBytes / (8 * size_t(out.block)));
+      out.acc_reg = std::max(int(exprs.size()) - room, kAccRegMin);
+    }
     if (out.pipelined)
       out.stages = stages_req >= 2 && stages_req <= 8 ? stages_req : (dw_default ? 3 : 4);
     else
@@ -1120,13 +1140,19 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
   s << "// outputs:\n";
   for (size_t j = 0; j < exprs.size(); j++) s << "//   [" << j << "] " << exprs[j].substr(0, 160) << "\n";
   s << kPrelude;
+  if (out.acc_reg <= 0 || out.acc_reg > M) out.acc_reg = M;
+  const int NREG = out.acc_reg;
   s << "#define MF_BLOCK " << out.block << "\n#define MF_NOUT " << M << "\n#define MF_NPAR " << NP << "\n";
+  // per-thread partials of outputs [0, MF_NREG) in registers, the rest in shared memory
+  s << "#define MF_NREG " << NREG << "\n";
   // launch bounds of the event-loop entries
   s << "#define MF_BOUNDS __launch_bounds__(MF_BLOCK)\n";
   // partial blocks each last-block thread loads per round (bounded register use)
   // combine of block partial rows: MF_CC outputs at a time, MF_Q rows of each in flight per thread
   s << "#define MF_CC " << std::min(M, 8) << "\n";
-  s << "#define MF_Q " << std::max(1, 8 / std::max(1, std::min(M, 8))) << "\n";
+  // (many-output kernels, whose grids of small blocks leave thousands of
+  // partial rows to the last block, keep four times as many loads in flight)
+  s << "#define MF_Q " << (M > kAccRegMax ? 4 : std::max(1, 8 / std::max(1, std::min(M, 8)))) << "\n";
   // outputs per block-reduction chunk (one warp each)
   s << "#define MF_RC " << std::max(1, std::min(8, out.block / 32)) << "\n";
   s << "struct mf_par { double v[MF_NPAR]; };\n";
@@ -1247,6 +1273,10 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
     // ... plus (or minus) a parameter-only value per event (the normalisation
     // term of logprob_normalised, pdf.hh:103-106): log(x) + u or log(x) - u
     std::vector<int> logadd(roots.size(), -1), logsign(roots.size(), 0), lognode(roots.size(), -1);
+    // Double-float outputs x + u or x - u with u parameter-only (the
+    // normalisation terms of Hessian outputs): x is accumulated and the
+    // thread's event count times u added once, before the block reduction.
+    std::vector<int> addu(roots.size(), -1), addsign(roots.size(), 0), accnode(roots);
     // FP32 REDUCE bodies (mixed precision) whose only output is the logarithm
     // of a dot product of per-event values with parameter-only factors (the
     // fitter's NLL kernel for a density linear in its prepared columns): that
@@ -1373,6 +1403,29 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
           fused[j] = {n.a, n.b};
           skip[r] = 1;
         }
+        if (ar == Ar::DW && !lf && !skip[r] && uses[r] == 1 && !n.uniform && (n.op == Op::Add || n.op == Op::Sub)) {
+          int x = -1, u = -1, sg = 0;
+          if (ns[n.b].uniform && !ns[n.a].uniform) {
+            x = n.a;
+            u = n.b;
+            sg = n.op == Op::Add ? 1 : -1;
+          } else if (n.op == Op::Add && ns[n.a].uniform && !ns[n.b].uniform) {
+            x = n.b;
+            u = n.a;
+            sg = 1;
+          }
+          if (x >= 0 && !skip[x] && !chains.count(x)) {
+            addu[j] = u;
+            addsign[j] = sg;
+            accnode[j] = x;
+            skip[r] = 1;
+            const Node& xn = ns[x];
+            if (xn.op == Op::Mul && uses[x] == 1 && ns[x].op != Op::Input) {
+              fused[j] = {xn.a, xn.b};
+              skip[x] = 1;
+            }
+          }
+        }
         // an output that is the logarithm of a per-event value (plus or minus a
         // parameter-only value), used nowhere else: sum of logs = log of the
         // product (one multiply per event), plus the event count times u
@@ -1386,6 +1439,8 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
         }
       }
     }
+    bool has_addu = false;
+    for (int u : addu) has_addu = has_addu || u >= 0;
     auto estmt = [&](int id) -> std::string {
       const Node& n = ns[id];
       if (ar == Ar::F32S && dnode[id])
@@ -1632,19 +1687,46 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
     // Accumulation of output j from the body's value (per thread).
     auto acc_decl = [&](std::ostringstream& o) {
       if (ar == Ar::F32 || ar == Ar::F32S)
-        o << "  float acc[MF_NOUT], cmp[MF_NOUT];\n#pragma unroll\n  for (int j = 0; j < MF_NOUT; j++) { acc[j] = 0.0f; cmp[j] = 0.0f; }\n";
+        o << "  float acc[MF_NREG], cmp[MF_NREG];\n#pragma unroll\n  for (int j = 0; j < MF_NREG; j++) { acc[j] = 0.0f; cmp[j] = 0.0f; }\n";
       else if (ar == Ar::F64)
-        o << "  double acc[MF_NOUT];\n#pragma unroll\n  for (int j = 0; j < MF_NOUT; j++) acc[j] = 0.0;\n";
+        o << "  double acc[MF_NREG];\n#pragma unroll\n  for (int j = 0; j < MF_NREG; j++) acc[j] = 0.0;\n";
       else
-        o << "  mf_dw acc[MF_NOUT];\n#pragma unroll\n  for (int j = 0; j < MF_NOUT; j++) acc[j] = mf_dw_make(0.0f, 0.0f);\n";
+        o << "  mf_dw acc[MF_NREG];\n#pragma unroll\n  for (int j = 0; j < MF_NREG; j++) acc[j] = mf_dw_make(0.0f, 0.0f);\n";
+      if (NREG < M) {  // this thread's column of the shared partials
+        if (ar == Ar::F32 || ar == Ar::F32S)
+          o << "  __shared__ float mf_sacc[MF_NOUT - MF_NREG][MF_BLOCK], mf_scmp[MF_NOUT - MF_NREG][MF_BLOCK];\n"
+            << "  for (int j = 0; j < MF_NOUT - MF_NREG; j++) { mf_sacc[j][threadIdx.x] = 0.0f; "
+               "mf_scmp[j][threadIdx.x] = 0.0f; }\n";
+        else if (ar == Ar::F64)
+          o << "  __shared__ double mf_sacc[MF_NOUT - MF_NREG][MF_BLOCK];\n"
+            << "  for (int j = 0; j < MF_NOUT - MF_NREG; j++) mf_sacc[j][threadIdx.x] = 0.0;\n";
+        else
+          o << "  __shared__ mf_dw mf_sacc[MF_NOUT - MF_NREG][MF_BLOCK];\n"
+            << "  for (int j = 0; j < MF_NOUT - MF_NREG; j++) mf_sacc[j][threadIdx.x] = mf_dw_make(0.0f, 0.0f);\n";
+      }
       for (int j = 0; j < M; j++)
         if (logprod[j] >= 0) {
           o << "  mf_dw lpm" << j << " = mf_dw_make(1.0f, 0.0f);\n  int lpe" << j << " = 0;\n";
           if (logadd[j] >= 0) o << "  int lpc" << j << " = 0;\n";
         }
+      if (has_addu) o << "  int mf_cnt = 0;  // events of this thread (for the x + u outputs)\n";
+    };
+    // A thread's partial of output j (and its FP32 compensation): a register
+    // or the thread's slot of the shared partials.
+    auto accref = [&](int j) {
+      return j < NREG ? "acc[" + std::to_string(j) + "]"
+                      : "mf_sacc[" + std::to_string(j - NREG) + "][threadIdx.x]";
+    };
+    auto cmpref = [&](int j) {
+      return j < NREG ? "cmp[" + std::to_string(j) + "]"
+                      : "mf_scmp[" + std::to_string(j - NREG) + "][threadIdx.x]";
     };
     // Per-thread partials of the log-product outputs, before the block reduction.
     auto acc_finish = [&](std::ostringstream& o) {
+      for (int j = 0; j < M; j++)
+        if (addu[j] >= 0)
+          o << "  " << accref(j) << " = " << (addsign[j] > 0 ? "mf_dw_add" : "mf_dw_sub") << "(mf_dw_renorm("
+            << accref(j) << "), mf_dw_mul(mf_dw_make((float)mf_cnt, 0.0f), " << eref(addu[j]) << "));\n";
       for (int j = 0; j < M; j++) {
         if (logprod[j] < 0) continue;
         const std::string J = std::to_string(j);
@@ -1665,37 +1747,96 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
             << "    q_ = " << (logsign[j] > 0 ? "mf_dw_add" : "mf_dw_sub") << "(q_, c_);\n";
         }
         if (ar == Ar::F32)  // as a compensated FP32 partial: (acc, -cmp) = (h, l)
-          o << "    acc[" << J << "] = q_.h; cmp[" << J << "] = -q_.l; }\n";
+          o << "    " << accref(j) << " = q_.h; " << cmpref(j) << " = -q_.l; }\n";
         else
-          o << "    acc[" << J << "] = q_; }\n";
+          o << "    " << accref(j) << " = q_; }\n";
       }
     };
-    auto acc_add = [&](std::ostringstream& o, const std::string& ind) {
-      for (int j = 0; j < M; j++) {
+    auto acc_one = [&](std::ostringstream& o, const std::string& ind, int j) {
+      {
         if (logadd[j] >= 0) o << ind << "lpc" << j << "++;\n";
         if (ar == Ar::F32 && logprod[j] >= 0) {
           o << ind << "mf_dw_logprod(lpm" << j << ", lpe" << j << ", we" << logprod[j] << ");\n";
-          continue;
+          return;
         }
-        const std::string r = eref(roots[j]);
+        const std::string r = eref(accnode[j]);
         if (ar == Ar::F32 || ar == Ar::F32S)
-          o << ind << "mf_kahan_f32(acc[" << j << "], cmp[" << j << "], " << r << ");\n";
+          o << ind << "mf_kahan_f32(" << accref(j) << ", " << cmpref(j) << ", " << r << ");\n";
         else if (ar == Ar::F64)
-          o << ind << "acc[" << j << "] += " << r << ";\n";
+          o << ind << accref(j) << " += " << r << ";\n";
         else if (logprod[j] >= 0)
           o << ind << "mf_dw_logprod(lpm" << j << ", lpe" << j << ", " << eref(logprod[j]) << ");\n";
         else if (fused[j].first >= 0)
-          o << ind << "mf_dw_acc_mul(acc[" << j << "], " << eref(fused[j].first) << ", " << eref(fused[j].second)
-            << ");\n";
+          o << ind << "mf_dw_acc_mul(" << accref(j) << ", " << eref(fused[j].first) << ", "
+            << eref(fused[j].second) << ");\n";
         else
-          o << ind << "mf_dw_acc(acc[" << j << "], " << r << ");\n";
+          o << ind << "mf_dw_acc(" << accref(j) << ", " << r << ");\n";
+      }
+    };
+    auto acc_add = [&](std::ostringstream& o, const std::string& ind) {
+      for (int j = 0; j < M; j++) acc_one(o, ind, j);
+    };
+    // Kernels with many outputs (Hessians) accumulate each output as soon as
+    // the values it needs exist, instead of after the whole body: the outputs'
+    // values then need not all be live at once (105 for the S+P-wave Hessian,
+    // two registers each in double-float). Same operations in the same order
+    // per output, so the same sums.
+    const bool interleave = M > 16;
+    std::vector<std::vector<int>> ready_after(ns.size() + 1);  // [ns.size()]: before the first statement
+    if (interleave) {
+      auto in_body = [&](int id) { return id >= 0 && live[id] && !ns[id].uniform && ns[id].op != Op::Input; };
+      for (int j = 0; j < M; j++) {
+        std::vector<int> deps{accnode[j]};
+        if (ar == Ar::F32 && logprod[j] >= 0)
+          deps = {logprod[j]};
+        else if (ar == Ar::DW && logprod[j] >= 0)
+          deps = {logprod[j]};
+        else if (ar == Ar::DW && fused[j].first >= 0)
+          deps = {fused[j].first, fused[j].second};
+        int at = -1;
+        for (int d : deps)
+          if (in_body(d)) at = std::max(at, d);
+        ready_after[at < 0 ? ns.size() : size_t(at)].push_back(j);
+      }
+    }
+    // The body and the accumulation of every output; `guard` (a condition, or
+    // empty) decides whether this event counts.
+    auto body_acc = [&](std::ostringstream& o, const std::string& ind, const std::string& guard) {
+      if (has_addu) o << ind << (guard.empty() ? "" : "if (" + guard + ") ") << "mf_cnt++;\n";
+      auto accs = [&](const std::vector<int>& js) {
+        if (js.empty()) return;
+        if (!guard.empty()) o << ind << "if (" << guard << ") {\n";
+        for (int j : js) acc_one(o, guard.empty() ? ind : ind + "  ", j);
+        if (!guard.empty()) o << ind << "}\n";
+      };
+      if (!interleave) {
+        body(o, ind);
+        std::vector<int> all(M);
+        for (int j = 0; j < M; j++) all[j] = j;
+        accs(all);
+        return;
+      }
+      accs(ready_after[ns.size()]);
+      for (size_t i = 0; i < ns.size(); i++) {
+        if (!live[i] || ns[i].uniform || ns[i].op == Op::Input) continue;
+        const std::string st = estmt(int(i));
+        if (!st.empty()) o << ind << st << "\n";
+        accs(ready_after[i]);
       }
     };
     // A thread's partial of output J as a double-float value (expression).
     auto thread_dw = [&](const std::string& J) -> std::string {
-      if (ar == Ar::F32 || ar == Ar::F32S) return "mf_two_sum(acc[" + J + "], -cmp[" + J + "])";
-      if (ar == Ar::F64) return "mf_dw_split(acc[" + J + "])";
-      return "mf_dw_renorm(acc[" + J + "])";
+      auto one = [&](const std::string& a, const std::string& c) {
+        if (ar == Ar::F32 || ar == Ar::F32S) return "mf_two_sum(" + a + ", -" + c + ")";
+        if (ar == Ar::F64) return "mf_dw_split(" + a + ")";
+        return "mf_dw_renorm(" + a + ")";
+      };
+      if (NREG == M) return one("acc[" + J + "]", "cmp[" + J + "]");
+      // J is a constant once the loop is unrolled; both indices stay in bounds
+      const std::string r = "((" + J + ") < MF_NREG ? (" + J + ") : 0)";
+      const std::string sh = "[(" + J + ") < MF_NREG ? 0 : (" + J + ") - MF_NREG][threadIdx.x]";
+      return "((" + J + ") < MF_NREG ? " + one("acc[" + r + "]", "cmp[" + r + "]") + " : " +
+             one("mf_sacc" + sh, "mf_scmp" + sh) + ")";
     };
     // Block reduction of every output into mf_blk[] (shared): outputs go in
     // chunks of MF_RC through a [MF_RC][MF_BLOCK] staging array; warp w sums
@@ -1769,10 +1910,8 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
         s << ind << "{\n";
         for (int k : out.used_inputs)
           s << ind << "  const " << XT << " x" << k << " = " << input_value(lane_of(k, v)) << ";\n";
-        body(s, ind + "  ");
-        s << ind << "  if (" << valid_base << " + " << v << " < n) {\n";
-        acc_add(s, ind + "    ");
-        s << ind << "  }\n" << ind << "}\n";
+        body_acc(s, ind + "  ", valid_base + " + " + std::to_string(v) + " < n");
+        s << ind << "}\n";
       }
       (void)idx0;
     };
@@ -1974,8 +2113,7 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
       s << "    const " << XT << " x" << k << " = " << input_value("__ldg(data + (mf_u64)" + std::to_string(k) +
                                                                    " * stride + first + i)")
         << ";\n";
-    body(s, "    ");
-    acc_add(s, "    ");
+    body_acc(s, "    ", "");
     s << "  }\n";
     acc_finish(s);
     block_reduce(s);
@@ -2007,8 +2145,7 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
       s << "    const " << XT << " x" << k << " = " << input_value("__ldg(data + (mf_u64)" + std::to_string(k) +
                                                                    " * stride + first + i)")
         << ";\n";
-    body(s, "    ");
-    acc_add(s, "    ");
+    body_acc(s, "    ", "");
     s << "  }\n";
     acc_finish(s);
     block_reduce(s);

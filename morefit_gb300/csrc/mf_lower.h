@@ -83,6 +83,7 @@ struct LoweredKernel {
   std::vector<int> used_inputs;  // input columns read by the kernel
   int vec = 1;                   // events per thread per iteration
   int block = 256;
+  int acc_reg = 0;               // REDUCE: outputs whose per-thread partials are registers (the rest: shared memory)
   // REDUCE kernels stream tiles of `tile` events through `stages` shared-memory
   // buffers with bulk asynchronous copies (pipelined = true) or read global
   // memory directly (pipelined = false).

@@ -193,13 +193,12 @@ class Likelihood:
     def kernel_parts(self, kernel: str) -> list:
         """Kernels whose outputs, concatenated, are ``kernel``'s: the kernel
         itself, or for a Hessian kernel that spills more than
-        COMBINED_MAX_SPILL bytes of registers (the S+P wave's 105 outputs),
-        equal slices of its outputs of at most HESSIAN_PART_OUTPUTS each, one
-        kernel per slice, built on first use (each part repeats the per-event
-        work the slice needs but keeps its accumulators in registers, and
-        reads its own prepared copy of the dataset: worth it for a dataset
-        evaluated many times, not for the serving loop's one-fit datasets,
-        which keep the single kernel)."""
+        COMBINED_MAX_SPILL bytes of registers, equal slices of its outputs of
+        at most HESSIAN_PART_OUTPUTS each, one kernel per slice, built on
+        first use (each part repeats the per-event work the slice needs and
+        reads the dataset again). The lowering keeps many-output kernels
+        such as the S+P-wave Hessian (105 outputs) from spilling (partials
+        beyond MF_NREG in shared memory), so they stay one kernel."""
         parts = self.__dict__.setdefault("_parts", {})
         if kernel in parts:
             return parts[kernel]

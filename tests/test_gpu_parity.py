@@ -207,40 +207,57 @@ def test_combined_gradient_hessian_kernel(backend, workload):
 
 
 @pytest.mark.parametrize("kernelT", [np.float64, np.float32])
-def test_hessian_split_in_parts(backend, kernelT):
-    """A Hessian kernel that spills (the S+P wave's 105 outputs) is evaluated
-    as parts of at most 36 outputs that do not spill; the concatenated sums
-    equal the single kernel's to 1e-12 (FP64) / 1e-6 (FP32) of the largest
-    element, single and batched, and the P-wave Hessian stays one kernel."""
+def test_many_output_hessian_one_pass(backend, kernelT):
+    """The S+P-wave Hessian (105 outputs). In double-float it is one kernel
+    that neither spills nor reads the dataset more than once: the per-thread
+    partials of the outputs beyond MF_NREG live in shared memory. In FP32 the
+    single kernel spills and Likelihood splits its outputs into kernels of at
+    most 36 that keep every partial in registers. Either way the sums equal,
+    to 1e-12 (FP64) / 1e-6 (FP32) of the largest element, those of the other
+    form (the FP64 split forced), single, batched and over ragged segments;
+    the P-wave Hessian keeps all 36 partials in registers."""
+    from morefit_gb300.toystudy import SegmentLikelihood, _unpack_hessian
     from morefit_gb300.workloads import Likelihood
     g = load_golden("spwave_n2000.json")
+    ev = golden_events("spwave", 2000)
     like = Likelihood(backend, g, kernelT)
-    like.set_data(golden_events("spwave", 2000))
-    parts = like.kernel_parts("lh_hessian_kernel")
-    assert len(parts) == 3
-    assert all(like.blocks[p].kernel.info()["spill_bytes"] == 0 for p in parts)
-    tol = 1e-12 if kernelT == np.float64 else 1e-6
+    like.set_data(ev)
     b = like.blocks["lh_hessian_kernel"]
+    split = Likelihood(backend, g, kernelT)
+    split.COMBINED_MAX_SPILL = -1  # the split into register-only parts, for FP64 forced
+    split.set_data(ev)
+    parts = split.kernel_parts("lh_hessian_kernel")
+    assert len(parts) == 3
+    assert all(split.blocks[p].kernel.info()["spill_bytes"] == 0 for p in parts)
+    if kernelT == np.float64:
+        assert like.kernel_parts("lh_hessian_kernel") == ["lh_hessian_kernel"]
+        assert b.kernel.info()["spill_bytes"] == 0
+        src = b.kernel.source()
+        nreg = int(src.split("#define MF_NREG ")[1].split()[0])
+        assert nreg < 105 and "mf_sacc[" in src
+    else:
+        assert len(like.kernel_parts("lh_hessian_kernel")) == 3
+    tol = 1e-12 if kernelT == np.float64 else 1e-6
     for pt in g["points"]:
         pv = like.param_vector("lh_hessian_kernel", pt["params"])
         b.CopyToParameterBuffer(pv)
         b.SubmitKernel()
-        whole = b.CopyFromKahanBuffer()
-        split = like.sums("lh_hessian_kernel", pt["params"])
-        assert split.shape == whole.shape
-        assert np.all(np.abs(split - whole) <= tol * np.abs(whole).max())
+        whole = b.CopyFromKahanBuffer()  # the single kernel
+        joined = split.sums("lh_hessian_kernel", pt["params"])
+        assert joined.shape == whole.shape
+        assert np.all(np.abs(joined - whole) <= tol * np.abs(whole).max())
+        one = like.sums("lh_hessian_kernel", pt["params"])
         many = like.sums_many("lh_hessian_kernel", np.array([pt["params"]] * 2))
-        assert np.array_equal(many[0], split) and np.array_equal(many[1], split)
-    # ragged segments through the parts (the toy fits' Hessian): the golden
-    # events as one segment and as three, joined parts against the single kernel
-    from morefit_gb300.toystudy import SegmentLikelihood, _unpack_hessian
+        assert np.array_equal(many[0], one) and np.array_equal(many[1], one)
+    # ragged segments (the toy fits' Hessian): the golden events as one segment
+    # and as three, against the single-dataset kernel
     counts = np.array([2000, 700, 1, 1299])
     begins = np.array([0, 0, 700, 701])
     th = np.array([pt["params"] for pt in g["points"]] + [g["points"][0]["params"]])
+    npar = th.shape[1]
     for epb in (0, 512):
         sl = SegmentLikelihood(like, begins, counts, epb)
         hs = sl.hessian(np.arange(4), th)
-        npar = th.shape[1]
         for s_ in range(4):
             b.CopyToParameterBuffer(like.param_vector("lh_hessian_kernel", th[s_]))
             if s_ == 0:
@@ -256,6 +273,8 @@ def test_hessian_split_in_parts(backend, kernelT):
         assert np.all(np.abs(parts3 - hs[0]) <= tol * np.abs(hs[0]).max()), epb
     pw = Likelihood(backend, load_golden("pwave_n1000.json"), kernelT)
     assert pw.kernel_parts("lh_hessian_kernel") == ["lh_hessian_kernel"]
+    psrc = pw.blocks["lh_hessian_kernel"].kernel.source()
+    assert "#define MF_NREG 36" in psrc and "mf_sacc[" not in psrc
 
 
 @pytest.mark.parametrize("workload", ["pwave", "mass", "mass_w"])
