@@ -2089,9 +2089,10 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
       << "}\n";
     s << "extern \"C\" __global__ void __launch_bounds__(MF_BLOCK) " << out.entry
       << "_combine(const float2* __restrict__ partials_all, mf_u64 pstride, const unsigned* __restrict__ grids,"
-      << " double* __restrict__ out_all, unsigned count) {\n"
+      << " double* __restrict__ out_all, unsigned count, unsigned grid_all) {\n"
       << "  const unsigned e = blockIdx.x;\n  if (e >= count) return;\n"
-      << "  const unsigned mf_nb = grids[e];\n"
+      << "  // every evaluation's grid size, or (grids null) the one they all share\n"
+      << "  const unsigned mf_nb = grids ? grids[e] : grid_all;\n"
       << "  const float2* __restrict__ partials = partials_all + (mf_u64)e * pstride;\n"
       << "  double* __restrict__ out = out_all + (mf_u64)e * MF_NOUT;\n"
       << "  __shared__ float2 red[MF_NOUT][MF_BLOCK / 32];\n"

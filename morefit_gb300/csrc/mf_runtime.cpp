@@ -1449,15 +1449,20 @@ int launch_batched(mf_kernel* k, uint32_t count, const void* const* data, const 
       res_yield(k->ctx);
       MF_CUDA_TRY(cudaLaunchKernelExC(&cfg, reinterpret_cast<const void*>(k->fn_part), args));
     }
-    // pageable source: the copy is staged before the call returns
-    MF_CUDA_TRY(cudaMemcpyAsync(c->ring_grids, grids.data(), m * sizeof(unsigned), cudaMemcpyHostToDevice,
-                                c->stream));
+    // the chunk's grid sizes: one value when they are all equal (evaluations
+    // of one size, the common case), else a copy (pageable source: staged
+    // before the call returns) that the combine reads
+    const bool one_grid = std::all_of(grids.begin(), grids.begin() + m, [&](unsigned x) { return x == grids[0]; });
+    if (!one_grid)
+      MF_CUDA_TRY(cudaMemcpyAsync(c->ring_grids, grids.data(), m * sizeof(unsigned), cudaMemcpyHostToDevice,
+                                  c->stream));
     const float2* ring = c->ring;
     uint64_t ps = pstride;
-    const unsigned* g = c->ring_grids;
+    const unsigned* g = one_grid ? nullptr : c->ring_grids;
+    unsigned grid_all = grids[0];
     double* o = static_cast<double*>(out->ptr) + uint64_t(first) * k->n_outputs;
     uint32_t mm = m;
-    void* cargs[] = {const_cast<float2**>(&ring), &ps, const_cast<unsigned**>(&g), &o, &mm};
+    void* cargs[] = {const_cast<float2**>(&ring), &ps, const_cast<unsigned**>(&g), &o, &mm, &grid_all};
     MF_CUDA_TRY(cudaLaunchKernel(reinterpret_cast<const void*>(k->fn_combine), dim3(m), dim3(k->lowered.block),
                                  cargs, 0, c->stream));
   }
@@ -2527,7 +2532,9 @@ int launch_multi(mf_context* c, mf_kernel* k0, const std::vector<MultiItem>& ite
   const float2* cring = ring;
   uint64_t pstride = pmax * k0->n_outputs;
   unsigned count = unsigned(items.size());
-  void* cargs[] = {const_cast<float2**>(&cring), &pstride, const_cast<unsigned**>(&d_grids), &out, &count};
+  unsigned grid_all = 0;  // unused: per-item counts in d_grids
+  void* cargs[] = {const_cast<float2**>(&cring), &pstride, const_cast<unsigned**>(&d_grids), &out, &count,
+                   &grid_all};
   MF_CUDA_TRY(cudaLaunchKernel(reinterpret_cast<const void*>(k0->fn_combine), dim3(count), dim3(k0->lowered.block),
                                cargs, 0, c->stream));
   return MF_OK;
