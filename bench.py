@@ -306,17 +306,19 @@ def ours(args):
         u64p = C.POINTER(C.c_uint64)
 
         def request(count):
+            """The call's arguments, marshalled for ctypes (the arrays are kept
+            alive by the returned tuple)."""
             ins = (L.c_buf * count)(*[sets[i % len(sets)].blocks["lh_grad_kernel"].input.buf for i in range(count)])
             strides = np.array([sets[i % len(sets)].blocks["lh_grad_kernel"].input.stride for i in range(count)],
                                dtype=np.uint64)
             ns = np.full(count, n, dtype=np.uint64)
             rows = np.ascontiguousarray(np.tile(pv, (count, 1)))
-            return (count, ins, strides, ns, rows)
+            args = (kern.handle, count, ins, strides.ctypes.data_as(u64p), ns.ctypes.data_as(u64p), L.dptr(rows),
+                    len(pv), out_buf)
+            return args, (strides, ns, rows)
 
         def enqueue(req):
-            count, ins, strides, ns, rows = req
-            L.check(L.lib.mf_kernel_reduce_many(kern.handle, count, ins, strides.ctypes.data_as(u64p),
-                                                ns.ctypes.data_as(u64p), L.dptr(rows), len(pv), out_buf))
+            L.check(L.lib.mf_kernel_reduce_many(*req[0]))
 
         # one untimed launch per dataset first: each makes the dataset's
         # prepared columns (folded, pre-split) that the kernel reads
@@ -689,6 +691,8 @@ VARIANTS = {
     "f64_dw_v1_u2": (np.float64, False, 1, 256, False, 2),
     "f64_dw_v2_u1": (np.float64, False, 2, 256, False, 1),
     "f64_dw_v1_u1": (np.float64, False, 1, 256, False, 1),
+    "f64_dw_v1_b128": (np.float64, False, 1, 128, False, 0),
+    "f64_dw_v1_b512": (np.float64, False, 1, 512, False, 0),
     "f32_u2": (np.float32, False, 4, 256, False, 2),
     "f32_v2_u2": (np.float32, False, 2, 256, False, 2),
     "f32_b512": (np.float32, False, 4, 512, False, 0),
@@ -712,7 +716,8 @@ def variants(args):
     from morefit_gb300.workloads import Likelihood, generate_events, load_spec
     torch.cuda.set_device(0)
     backend = CUDABackend(0, resident_idle_us=0)  # the launched kernels are the subject here
-    spec = load_spec("pwave")
+    spec = load_spec(args.model)
+    kname = args.kernel
     truth = np.array(spec["truth"])
     n = args.nevents
     nsets = args.sets
@@ -731,15 +736,15 @@ def variants(args):
             else:
                 like.set_data(raw[r].download())
             sets.append(like)
-        kern = sets[0].blocks["lh_grad_kernel"].kernel
-        pv = sets[0].param_vector("lh_grad_kernel", truth)
+        kern = sets[0].blocks[kname].kernel
+        pv = sets[0].param_vector(kname, truth)
         K, W = args.steps, args.warmup
         out = L.c_buf()
         L.check(L.lib.mf_buffer_alloc(backend.handle, max(K, W, nsets, 1) * kern.nout * 8, C.byref(out)))
 
         def enqueue(count):
-            ins = (L.c_buf * count)(*[sets[i % nsets].blocks["lh_grad_kernel"].input.buf for i in range(count)])
-            st = np.array([sets[i % nsets].blocks["lh_grad_kernel"].input.stride for i in range(count)], np.uint64)
+            ins = (L.c_buf * count)(*[sets[i % nsets].blocks[kname].input.buf for i in range(count)])
+            st = np.array([sets[i % nsets].blocks[kname].input.stride for i in range(count)], np.uint64)
             ns = np.full(count, n, dtype=np.uint64)
             rows = np.ascontiguousarray(np.tile(pv, (count, 1)))
             u = C.POINTER(C.c_uint64)
@@ -774,7 +779,7 @@ def variants(args):
             # rotating over the datasets; host time per call
             sums = np.zeros(kern.nout)
             pvc = np.ascontiguousarray(pv)
-            calls = [(sets[i].blocks["lh_grad_kernel"].input.buf, sets[i].blocks["lh_grad_kernel"].input.stride)
+            calls = [(sets[i].blocks[kname].input.buf, sets[i].blocks[kname].input.stride)
                      for i in range(nsets)]
             for i in range(min(20, args.lone_calls)):
                 buf, st = calls[i % nsets]
@@ -1009,6 +1014,8 @@ def main():
     ap.add_argument("--sets", type=int, default=5)
     ap.add_argument("--lone", action="store_true", help="with --variants: also time synchronous single evaluations")
     ap.add_argument("--lone-calls", type=int, default=200)
+    ap.add_argument("--model", default="pwave", help="with --variants: the model (a spec in morefit_gb300/specs)")
+    ap.add_argument("--kernel", default="lh_grad_kernel", help="with --variants: the REDUCE kernel timed")
     args = ap.parse_args()
     if args.warmup < 3 and not args.variants:
         args.warmup = 3

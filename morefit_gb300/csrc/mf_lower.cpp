@@ -2090,6 +2090,9 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
     s << "extern \"C\" __global__ void __launch_bounds__(MF_BLOCK) " << out.entry
       << "_combine(const float2* __restrict__ partials_all, mf_u64 pstride, const unsigned* __restrict__ grids,"
       << " double* __restrict__ out_all, unsigned count, unsigned grid_all) {\n"
+      << "  // launched as a programmatic dependent of the last evaluation: its partials\n"
+      << "  // (and every earlier one's) are complete and visible after this\n"
+      << "  mf_grid_dependency_wait();\n"
       << "  const unsigned e = blockIdx.x;\n  if (e >= count) return;\n"
       << "  // every evaluation's grid size, or (grids null) the one they all share\n"
       << "  const unsigned mf_nb = grids ? grids[e] : grid_all;\n"

@@ -1463,8 +1463,19 @@ int launch_batched(mf_kernel* k, uint32_t count, const void* const* data, const 
     double* o = static_cast<double*>(out->ptr) + uint64_t(first) * k->n_outputs;
     uint32_t mm = m;
     void* cargs[] = {const_cast<float2**>(&ring), &ps, const_cast<unsigned**>(&g), &o, &mm, &grid_all};
-    MF_CUDA_TRY(cudaLaunchKernel(reinterpret_cast<const void*>(k->fn_combine), dim3(m), dim3(k->lowered.block),
-                                 cargs, 0, c->stream));
+    // a programmatic dependent of the chunk's last evaluation (which completes
+    // after every earlier one): the combine is resident before that grid ends
+    // and waits for it in the kernel (unless the grid table copy sits between)
+    cudaLaunchConfig_t ccfg = {};
+    ccfg.gridDim = dim3(m);
+    ccfg.blockDim = dim3(k->lowered.block);
+    ccfg.stream = c->stream;
+    cudaLaunchAttribute cattr[1];
+    cattr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    cattr[0].val.programmaticStreamSerializationAllowed = 1;
+    ccfg.attrs = cattr;
+    ccfg.numAttrs = one_grid ? 1 : 0;
+    MF_CUDA_TRY(cudaLaunchKernelExC(&ccfg, reinterpret_cast<const void*>(k->fn_combine), cargs));
   }
   return MF_OK;
 }
@@ -2156,7 +2167,10 @@ int mf_kernel_reduce_many(mf_kernel* k, uint32_t count, const mf_buffer* const* 
   // A buffer that appears with two column strides in one batch would have its
   // prepared copy remade between uses: prepare and launch one by one.
   bool one_by_one = false;
-  if (k->lowered.prep) {
+  if (k->lowered.prep && count <= 64) {  // small batches: a scan, no allocation
+    for (uint32_t i = 0; i < count && !one_by_one; i++)
+      for (uint32_t j = 0; j < i && !one_by_one; j++) one_by_one = inputs[j] == inputs[i] && strides[j] != strides[i];
+  } else if (k->lowered.prep) {
     std::map<const mf_buffer*, uint64_t> layout;
     for (uint32_t i = 0; i < count && !one_by_one; i++) {
       auto [it, fresh] = layout.emplace(inputs[i], strides[i]);
