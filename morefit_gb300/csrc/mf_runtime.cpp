@@ -1827,7 +1827,7 @@ extern "C" __global__ void __launch_bounds__(MFR_BLOCK, MFR_MINB) mf_resident(mf
       if (v != MFR_EXIT) {
         const uint4* src = reinterpret_cast<const uint4*>(&mail->req);
         uint4* dst = reinterpret_cast<uint4*>(req);
-        for (unsigned q = threadIdx.x; q < sizeof(mfr_req) / 16; q += MFR_BLOCK) dst[q] = __ldcv(src + q);
+        for (unsigned q = threadIdx.x; q < (MFR_WORDS + 3) / 4; q += MFR_BLOCK) dst[q] = __ldcv(src + q);
         __threadfence();
       }
       __syncthreads();
