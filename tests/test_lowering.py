@@ -175,3 +175,30 @@ def test_resident_module_compiles(workload, elem):
     assert "blockIdx.x" not in body and "gridDim.x" not in body
     single = _entry(_src(g, "lh_kernel", elem), "mf_reduce(")
     assert single.count("__syncthreads()") == body.count("__syncthreads()")
+
+
+def test_many_output_kernels_keep_partials_in_shared_memory():
+    """Double-float kernels of more than 64 outputs keep the per-thread
+    partials beyond MF_NREG in shared memory (64-thread blocks) and sum
+    outputs x + u as x plus the event count times u; the S+P-wave Hessian then
+    compiles without spilling. FP32 kernels and smaller ones keep every partial
+    in registers."""
+    import re
+    from morefit_gb300 import _lib as L
+    from morefit_gb300.backend import compile_check, lower_source
+    g = load_golden("spwave_n2000.json")
+    k = kernel_spec(g, "lh_hessian_kernel")
+    defs = dict(g["hessian_buffers"])
+    pd = [defs.get(p, "") for p in k["params"]]
+    src = lower_source("h", L.MF_KERNEL_REDUCE, L.MF_F64, k["inputs"], k["params"], k["exprs"], param_defs=pd)
+    nreg = int(re.search(r"#define MF_NREG (\d+)", src).group(1))
+    assert "#define MF_BLOCK 64" in src and nreg < 105 and "mf_sacc[" in src
+    assert "mf_cnt++" in src and "(float)mf_cnt" in src
+    info = compile_check("h", L.MF_KERNEL_REDUCE, L.MF_F64, k["inputs"], k["params"], k["exprs"], param_defs=pd)
+    assert info["spill_bytes"] == 0, info
+    f32 = lower_source("h", L.MF_KERNEL_REDUCE, L.MF_F32, k["inputs"], k["params"], k["exprs"], param_defs=pd)
+    assert "#define MF_NREG 105" in f32 and "mf_sacc[" not in f32
+    pw = load_golden("pwave_n1000.json")
+    kp = kernel_spec(pw, "lh_hessian_kernel")
+    psrc = lower_source("h", L.MF_KERNEL_REDUCE, L.MF_F64, kp["inputs"], kp["params"], kp["exprs"])
+    assert "#define MF_NREG 36" in psrc and "#define MF_BLOCK 256" in psrc and "mf_sacc[" not in psrc
