@@ -467,6 +467,15 @@ int mf_kernel_generate(mf_kernel* k, const uint32_t* seeds, uint32_t nseeds, uin
 int mf_kernel_generate_async(mf_kernel* k, const uint32_t* seeds, uint32_t nseeds, uint64_t n, uint64_t nper,
                              const double* params, uint32_t n_params, mf_buffer* out, uint64_t out_stride,
                              uint64_t max_tries);
+/* mf_kernel_generate_async with nstreams streams seeded on the device: stream
+ * t starts from the state mf_splitmix_seed_rows(seed, nstreams) gives row t,
+ * so the events equal those of that seed table, without building or copying
+ * it (16 bytes per stream). For generations that need independent streams
+ * rather than the reference's jump partition (e.g. a server generating each
+ * request's dataset at admission). */
+int mf_kernel_generate_splitmix_async(mf_kernel* k, uint64_t seed, uint32_t nstreams, uint64_t n, uint64_t nper,
+                                      const double* params, uint32_t n_params, mf_buffer* out, uint64_t out_stride,
+                                      uint64_t max_tries);
 
 /* GENERATE for many datasets at once (toy studies with a different truth per
  * toy): segment s owns output events [seg_begin[s], seg_begin[s] +

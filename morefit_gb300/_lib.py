@@ -158,6 +158,8 @@ _proto("mf_kernel_generate", C.c_int, c_ker, C.POINTER(C.c_uint32), C.c_uint32, 
        C.c_uint32, c_buf, C.c_uint64, C.c_uint64)
 _proto("mf_kernel_generate_async", C.c_int, c_ker, C.POINTER(C.c_uint32), C.c_uint32, C.c_uint64, C.c_uint64, c_dbl_p,
        C.c_uint32, c_buf, C.c_uint64, C.c_uint64)
+_proto("mf_kernel_generate_splitmix_async", C.c_int, c_ker, C.c_uint64, C.c_uint32, C.c_uint64, C.c_uint64, c_dbl_p,
+       C.c_uint32, c_buf, C.c_uint64, C.c_uint64)
 _proto("mf_eval_expressions", C.c_int, C.c_uint32, c_char_pp, c_dbl_p, C.c_uint32, c_char_pp, c_dbl_p)
 _proto("mf_seed_rows", C.c_int, C.c_uint64, C.c_uint32, C.POINTER(C.c_uint32))
 _proto("mf_splitmix_seed_rows", C.c_int, C.c_uint64, C.c_uint32, C.POINTER(C.c_uint32))
@@ -210,5 +212,5 @@ def exported_symbols() -> list[str]:
         "mf_histogram", "mf_events_load_file", "mf_splitmix_seed_rows", "mf_buffer_wrap_host",
         "mf_spd_solve_batch", "mf_kernel_reduce_multi", "mf_coalescer_create", "mf_coalescer_destroy",
         "mf_context_set_coalescer", "mf_coalesced_submit", "mf_coalesced_poll", "mf_coalescer_stats",
-        "mf_kernel_generate_async", "mf_kernel_reduce_segments_chunked",
+        "mf_kernel_generate_async", "mf_kernel_reduce_segments_chunked", "mf_kernel_generate_splitmix_async",
     ]

@@ -444,6 +444,18 @@ class CUDABlock:
                                                    self.output.stride, 10000 * per))
         return True
 
+    def SubmitGenerateSplitmixAsync(self, seed: int, nstreams: int, nper: int) -> bool:
+        """Generation without a seed table: `nstreams` streams seeded on the
+        device as splitmix_seed_rows(nstreams, seed) seeds them (the same
+        events), enqueued without a host wait (mf_kernel_generate_splitmix_async)."""
+        k = self.kernel
+        p = self.params if self.params.size else np.zeros(1)
+        self.output.ensure(self._gen, self.nevents)
+        L.check(L.lib.mf_kernel_generate_splitmix_async(k.handle, int(seed), int(nstreams), self.nevents, int(nper),
+                                                        L.dptr(p), k.nparams, self.output.buf, self.output.stride,
+                                                        10000 * int(nper)))
+        return True
+
     def CopyToSeedBuffer(self, seeds: np.ndarray) -> bool:
         self._seeds = np.ascontiguousarray(seeds, dtype=np.uint32)
         return True

@@ -2214,9 +2214,21 @@ __device__ __forceinline__ unsigned mf_xoshiro(unsigned* s) {
     if (!ar32) s << dw_log_table() << kDwPrelude;
     s << "extern \"C\" __global__ void __launch_bounds__(MF_BLOCK) " << out.entry
       << "(const unsigned* __restrict__ seeds, unsigned nseeds, mf_u64 n, mf_u64 nper, mf_par P, " << ST
-      << "* __restrict__ outp, mf_u64 out_stride, unsigned* __restrict__ status, unsigned long long max_tries) {\n";
+      << "* __restrict__ outp, mf_u64 out_stride, unsigned* __restrict__ status, unsigned long long max_tries,"
+      << " unsigned long long splitmix_seed) {\n";
     s << "  const unsigned t = blockIdx.x * MF_BLOCK + threadIdx.x;\n  if (t >= nseeds) return;\n";
-    s << "  unsigned st[4];\n#pragma unroll\n  for (int k = 0; k < 4; k++) st[k] = seeds[(mf_u64)k * nseeds + t];\n";
+    // the stream's xoshiro128++ state: from the seed table, or (seeds null)
+    // made here as mf_splitmix_seed_rows makes row t: the upper halves of four
+    // SplitMix64 outputs (Steele, Lea and Flood, OOPSLA 2014) from
+    // (seed mod 2^32) * 2^32 + t
+    s << "  unsigned st[4];\n"
+      << "  if (seeds) {\n#pragma unroll\n    for (int k = 0; k < 4; k++) st[k] = seeds[(mf_u64)k * nseeds + t];\n"
+      << "  } else {\n    unsigned long long sm = (splitmix_seed & 0xffffffffull) * 4294967296ull + t;\n"
+      << "#pragma unroll\n    for (int k = 0; k < 4; k++) {\n"
+      << "      unsigned long long z = (sm += 0x9e3779b97f4a7c15ull);\n"
+      << "      z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;\n"
+      << "      z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;\n"
+      << "      st[k] = (unsigned)((z ^ (z >> 31)) >> 32);\n    }\n  }\n";
     emit_params_and_uniform(s, "P.v");
     // The reference prints min, max-min and maxprob with "%.15e" into its
     // generate kernel (compute_llvm.hh:466-478,485-489) and evaluates

@@ -2340,10 +2340,12 @@ int mf_kernel_store_async(mf_kernel* k, const mf_buffer* in, uint64_t in_stride,
   return kernel_store(k, in, in_stride, n, params, n_params, out, out_stride, false);
 }
 
+// seeds null: every stream seeded on the device from `splitmix_seed` (the
+// state mf_splitmix_seed_rows gives its row), no seed table copied.
 static int kernel_generate(mf_kernel* k, const uint32_t* seeds, uint32_t nseeds, uint64_t n, uint64_t nper,
                            const double* params, uint32_t n_params, mf_buffer* out, uint64_t out_stride,
-                           uint64_t max_tries, bool sync) {
-  if (!k || !seeds || !out) return fail(MF_ERR_INVALID, "null argument");
+                           uint64_t max_tries, bool sync, uint64_t splitmix_seed = 0) {
+  if (!k || !out) return fail(MF_ERR_INVALID, "null argument");
   if (k->kind != MF_KERNEL_GENERATE) return fail(MF_ERR_INVALID, "kernel is not a GENERATE kernel");
   if (n_params != k->n_params || (n_params && !params)) return fail(MF_ERR_INVALID, "parameter count mismatch");
   if (nseeds == 0 || nper == 0) return fail(MF_ERR_INVALID, "no generator threads");
@@ -2353,19 +2355,22 @@ static int kernel_generate(mf_kernel* k, const uint32_t* seeds, uint32_t nseeds,
   if (n == 0) return MF_OK;
   mf_context* c = k->ctx;
   MF_CUDA_TRY(cudaSetDevice(c->device));
-  int rc = ensure_stage(c, size_t(nseeds) * 4 * sizeof(uint32_t));
-  if (rc) return rc;
-  MF_CUDA_TRY(cudaMemcpyAsync(c->stage_dev, seeds, size_t(nseeds) * 4 * sizeof(uint32_t), cudaMemcpyHostToDevice,
-                              c->stream));
+  if (seeds) {
+    int rc = ensure_stage(c, size_t(nseeds) * 4 * sizeof(uint32_t));
+    if (rc) return rc;
+    MF_CUDA_TRY(cudaMemcpyAsync(c->stage_dev, seeds, size_t(nseeds) * 4 * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                                c->stream));
+  }
   if (sync) *c->status_host = 0u;
   std::vector<double> pv(std::max<uint32_t>(1, k->n_params), 0.0);
   if (k->n_params) std::memcpy(pv.data(), params, k->n_params * sizeof(double));
-  const unsigned* sd = static_cast<const unsigned*>(c->stage_dev);
+  const unsigned* sd = seeds ? static_cast<const unsigned*>(c->stage_dev) : nullptr;
   void* outp = out->ptr;
   out->gen++;
   unsigned* status = c->status;
   unsigned long long mt = max_tries ? max_tries : 1000000000ULL;
-  void* args[] = {&sd, &nseeds, &n, &nper, pv.data(), &outp, &out_stride, &status, &mt};
+  unsigned long long sms = splitmix_seed;
+  void* args[] = {&sd, &nseeds, &n, &nper, pv.data(), &outp, &out_stride, &status, &mt, &sms};
   const unsigned grid = (nseeds + k->lowered.block - 1) / k->lowered.block;
   res_yield(k->ctx);
   MF_CUDA_TRY(cudaLaunchKernel(reinterpret_cast<const void*>(k->fn), dim3(grid), dim3(k->lowered.block), args, 0,
@@ -2381,12 +2386,20 @@ static int kernel_generate(mf_kernel* k, const uint32_t* seeds, uint32_t nseeds,
 int mf_kernel_generate(mf_kernel* k, const uint32_t* seeds, uint32_t nseeds, uint64_t n, uint64_t nper,
                        const double* params, uint32_t n_params, mf_buffer* out, uint64_t out_stride,
                        uint64_t max_tries) {
+  if (!seeds) return fail(MF_ERR_INVALID, "null argument");
   return kernel_generate(k, seeds, nseeds, n, nper, params, n_params, out, out_stride, max_tries, true);
+}
+
+int mf_kernel_generate_splitmix_async(mf_kernel* k, uint64_t seed, uint32_t nstreams, uint64_t n, uint64_t nper,
+                                      const double* params, uint32_t n_params, mf_buffer* out, uint64_t out_stride,
+                                      uint64_t max_tries) {
+  return kernel_generate(k, nullptr, nstreams, n, nper, params, n_params, out, out_stride, max_tries, false, seed);
 }
 
 int mf_kernel_generate_async(mf_kernel* k, const uint32_t* seeds, uint32_t nseeds, uint64_t n, uint64_t nper,
                              const double* params, uint32_t n_params, mf_buffer* out, uint64_t out_stride,
                              uint64_t max_tries) {
+  if (!seeds) return fail(MF_ERR_INVALID, "null argument");
   return kernel_generate(k, seeds, nseeds, n, nper, params, n_params, out, out_stride, max_tries, false);
 }
 

@@ -33,7 +33,7 @@ import numpy as np
 
 from . import _lib as L
 from .backend import CUDABackend, CUDABlock, DeviceColumns
-from .workloads import Likelihood, load_spec, splitmix_seed_rows
+from .workloads import Likelihood, load_spec
 
 
 MODEL_LIMITS = {
@@ -167,11 +167,11 @@ class ModelRuntime:
         (hoisted by the precompute where the model has one)."""
         pre = self.template.pre
         nseeds = int(min(65536, n))
-        self.gen.CopyToSeedBuffer(splitmix_seed_rows(nseeds, seed))
         self.gen.SetNevents(n)
+        # streams seeded on the device (no seed table built or copied);
         # enqueued without a host wait (a thread that gives up is reported by
         # the next synchronous call); the precompute follows in stream order
-        self.gen.SubmitKernelAsync(-(-n // nseeds))
+        self.gen.SubmitGenerateSplitmixAsync(seed, nseeds, -(-n // nseeds))
         raw = self.gen.output
         self.gen.output = DeviceColumns(self.backend, self.gen.elem)
         if not self.template.has_precompute:
@@ -257,13 +257,10 @@ class FitServer:
         self.f_noise = 2e-7 if np.dtype(kernelT) == np.float32 else 1e-13
 
     def _hess(self, rt: ModelRuntime, s: np.ndarray) -> np.ndarray:
-        h = np.zeros((rt.npar, rt.npar))
-        k = 0
-        for i in range(rt.npar):
-            for j in range(i + 1):
-                h[i, j] = h[j, i] = -2.0 * s[k]
-                k += 1
-        return h
+        """-2 x the Hessian kernel's sums (lower triangle, row by row) as the
+        full symmetric matrix: one gather through a flat index map."""
+        from .toystudy import _unpack_hessian
+        return _unpack_hessian(np.asarray(s)[None, : rt.npar * (rt.npar + 1) // 2], rt.npar)[0]
 
     def run(self, requests, realtime: bool = True) -> ServerStats:
         """Serves ``requests`` (arrival times relative to the start); with

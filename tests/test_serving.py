@@ -57,3 +57,21 @@ def test_admission_respects_the_budget(server):
     ref = {o.id: o for o in server.run(_requests(), realtime=False).outcomes}
     for o in st.outcomes:
         assert np.array_equal(o.values, ref[o.id].values)
+
+
+@pytest.mark.parametrize("model,n", [("mass", 70001), ("spwave", 5000)])
+def test_device_seeded_generation_equals_seed_table(server, model, n):
+    """A request's dataset is generated with its streams seeded on the device
+    (mf_kernel_generate_splitmix_async): the events equal, bit for bit, those
+    generated from the seed table splitmix_seed_rows builds on the host."""
+    from morefit_gb300.workloads import splitmix_seed_rows
+    gen = server.models[model].gen
+    nseeds = int(min(65536, n))
+    gen.SetNevents(n)
+    gen.SubmitGenerateSplitmixAsync(99, nseeds, -(-n // nseeds))
+    a = gen.output.download()
+    gen.CopyToSeedBuffer(splitmix_seed_rows(nseeds, 99))
+    gen.SetNevents(n)
+    gen.SubmitKernelAsync(-(-n // nseeds))
+    b = gen.output.download()
+    assert a.shape == b.shape and np.array_equal(a, b)
