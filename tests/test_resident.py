@@ -23,11 +23,11 @@ def _warm(backend, like, theta, timeout=120.0):
     assert backend.resident_stats()["state"] == 2, backend.resident_stats()
 
 
-def _pair(spec, kernelT, n, seed=11):
+def _pair(spec, kernelT, n, seed=11, idle_us=2000):
     from morefit_gb300.backend import CUDABackend
     from morefit_gb300.workloads import Likelihood, generate_events
     out = []
-    for idle in (0, 2000):
+    for idle in (0, idle_us):
         b = CUDABackend(0, resident_idle_us=idle)
         lk = Likelihood(b, spec, kernelT)
         lk.set_device_data(generate_events(b, spec, n, seed=seed))
@@ -44,15 +44,16 @@ def test_resident_sums_equal_launches(workload, kernelT, n):
     from morefit_gb300.workloads import load_spec
     spec = load_spec(workload)
     truth = np.array(spec["truth"])
-    (b0, l0), (b1, l1) = _pair(spec, kernelT, n)
+    # idle time far above any pause between the calls below (a garbage
+    # collection, a busy host): every call is served by the same grid
+    (b0, l0), (b1, l1) = _pair(spec, kernelT, n, idle_us=500000)
     calls = [(kern, truth * (1.0 + 1e-3 * np.sin(np.arange(truth.size) + j)))
              for j in range(30) for kern in ("lh_grad_kernel", "lh_kernel", "lh_kernel")]
     try:
         launched = [l0.sums(kern, th).copy() for kern, th in calls]  # sums() returns a reused array
         _warm(b1, l1, truth)
         time.sleep(0.03)  # past the hold after the other context's launches
-        # the grid left while idle: this call launches, the next one starts a grid
-        l1.sums("lh_kernel", truth)
+        l1.sums("lh_kernel", truth)  # starts the grid if none is up
         before = b1.resident_stats()["served"]
         served = [l1.sums(kern, th).copy() for kern, th in calls]
         st = b1.resident_stats()
