@@ -77,13 +77,14 @@ def test_resident_grid_makes_room_and_leaves_when_idle():
     from morefit_gb300.workloads import generate_events, load_spec
     spec = load_spec("pwave")
     truth = np.array(spec["truth"])
-    (b0, l0), (b1, l1) = _pair(spec, np.float64, 200000)
+    # idle_us 50 ms: above any host pause between back-to-back calls, below the sleeps
+    (b0, l0), (b1, l1) = _pair(spec, np.float64, 200000, idle_us=50000)
     other = CUDABackend(0, resident_idle_us=0)
     try:
         ref = l0.sums("lh_grad_kernel", truth)
         _warm(b1, l1, truth)
-        time.sleep(0.03)
-        l1.sums("lh_kernel", truth)  # the grid left while idle: this call launches, the next start one
+        time.sleep(0.03)  # past the hold after the other context's launches
+        l1.sums("lh_kernel", truth)  # starts the grid if none is up
         s0 = b1.resident_stats()
         for _ in range(3):
             assert np.array_equal(l1.sums("lh_grad_kernel", truth), ref)
@@ -101,7 +102,7 @@ def test_resident_grid_makes_room_and_leaves_when_idle():
         s2 = b1.resident_stats()
         assert s2["grids"] > s1["grids"] and s2["served"] > s1["served"], (s1, s2)
         # idle for longer than idle_us: the grid leaves by itself
-        time.sleep(0.02)
+        time.sleep(0.1)
         for _ in range(3):
             assert np.array_equal(l1.sums("lh_grad_kernel", truth), ref)
         s3 = b1.resident_stats()
