@@ -115,6 +115,8 @@ namespace mfi {
 int columns_sum_launch(const void* data, int elem, uint64_t stride, uint64_t n, uint32_t ncols, void* partials,
                        unsigned* counter, double* out, cudaStream_t stream, int num_sms) {
   const int grid = grid_for(n, num_sms);
+  int dev = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess) resident_yield_device(dev);
   if (elem == MF_F32)
     columns_sum_kernel<float><<<grid, kThreads, 0, stream>>>(static_cast<const float*>(data), stride, n, ncols,
                                                              static_cast<float2*>(partials), counter, out);
@@ -298,6 +300,8 @@ template <typename T>
 int histogram_launch(const void* data, const void* weights, uint64_t n, double lo, double width, uint32_t nbins,
                      double* y, double* y2, unsigned long long* outside, cudaStream_t st, int grid) {
   const T* x = static_cast<const T*>(data);
+  int dev = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess) mfi::resident_yield_device(dev);
   const T* w = static_cast<const T*>(weights);
   if (w) {
     if (nbins <= kHistSharedWeight)

@@ -19,6 +19,10 @@ int columns_sum_launch(const void* data, int elem, uint64_t stride, uint64_t n, 
                        unsigned* counter, double* out, cudaStream_t stream, int num_sms);
 // Number of partial rows (blocks) the column-sum kernel uses for n events.
 int columns_sum_partials(uint64_t n, int num_sms);
+// Asks a resident evaluation grid on `device` (mf_context_set_resident), if
+// one is up, to leave once idle, so that a launch that follows is not held
+// back; no allocation, no synchronization.
+void resident_yield_device(int device);
 }  // namespace mfi
 
 #endif

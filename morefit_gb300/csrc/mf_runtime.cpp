@@ -1651,10 +1651,9 @@ int64_t steady_ns() {
       .count();
 }
 
-// Asks the grid up on c's device (whichever context owns it) to exit once
+// Asks the grid up on device d (whichever context owns it) to exit once
 // idle; called before every other launch of this library on the device.
-void res_yield(mf_context* c) {
-  const int d = c->device;
+void res_yield_device(int d) {
   if (d < 0 || d >= 64 || !g_res_up[d].load(std::memory_order_acquire)) return;
   std::lock_guard<std::mutex> lk(g_res_mu);
   mf_context* o = g_res_owner[d];
@@ -1662,6 +1661,8 @@ void res_yield(mf_context* c) {
   __atomic_store_n(&o->res->mail->stop, 1u, __ATOMIC_RELEASE);
   o->res->hold_until.store(steady_ns() + kResHoldNs);
 }
+
+void res_yield(mf_context* c) { res_yield_device(c->device); }
 
 // After the grid left (or was asked to leave) its loop: wait for it and
 // release the device.
@@ -2061,6 +2062,10 @@ int res_reduce(mf_kernel* k, const mf_buffer* in, uint64_t stride, uint64_t n, c
 }
 
 }  // namespace
+
+namespace mfi {
+void resident_yield_device(int device) { res_yield_device(device); }
+}  // namespace mfi
 
 extern "C" {
 
