@@ -792,6 +792,24 @@ def variants(args):
                 host_us.append((time.perf_counter() - t0) * 1e6)
             row["sync_call_us_median"] = statistics.median(host_us)
             row["sync_call_us_p10"] = sorted(host_us)[len(host_us) // 10]
+        if args.lone_async:
+            # single evaluations without the synchronous path's completion
+            # signalling: mf_kernel_reduce_async (sums to device memory, no
+            # system-scope fence or mapped-memory word), each followed by a
+            # stream synchronize; the launch alone on the device, as ncu times it
+            ob = L.c_buf()
+            L.check(L.lib.mf_buffer_alloc(backend.handle, kern.nout * 8, C.byref(ob)))
+            pvc = np.ascontiguousarray(pv)
+            host_us = []
+            for i in range(args.lone_calls):
+                blk = sets[i % nsets].blocks[kname]
+                t0 = time.perf_counter()
+                L.check(L.lib.mf_kernel_reduce_async(kern.handle, blk.input.buf, blk.input.stride, n, L.dptr(pvc),
+                                                     len(pvc), ob, 0))
+                backend.synchronize()
+                host_us.append((time.perf_counter() - t0) * 1e6)
+            L.lib.mf_buffer_free(ob)
+            row["async_call_us_median"] = statistics.median(host_us)
         print(json.dumps(row), flush=True)
         del sets
 
@@ -1014,6 +1032,8 @@ def main():
     ap.add_argument("--sets", type=int, default=5)
     ap.add_argument("--lone", action="store_true", help="with --variants: also time synchronous single evaluations")
     ap.add_argument("--lone-calls", type=int, default=200)
+    ap.add_argument("--lone-async", action="store_true",
+                    help="with --variants: also time asynchronous single evaluations, one at a time")
     ap.add_argument("--model", default="pwave", help="with --variants: the model (a spec in morefit_gb300/specs)")
     ap.add_argument("--kernel", default="lh_grad_kernel", help="with --variants: the REDUCE kernel timed")
     args = ap.parse_args()

@@ -1149,10 +1149,14 @@ LoweredKernel lower(const std::string& name, Kind kind, Elem elem, const std::ve
   s << "#define MF_BOUNDS __launch_bounds__(MF_BLOCK)\n";
   // partial blocks each last-block thread loads per round (bounded register use)
   // combine of block partial rows: MF_CC outputs at a time, MF_Q rows of each in flight per thread
-  s << "#define MF_CC " << std::min(M, 8) << "\n";
-  // (many-output kernels, whose grids of small blocks leave thousands of
-  // partial rows to the last block, keep four times as many loads in flight)
-  s << "#define MF_Q " << (M > kAccRegMax ? 4 : std::max(1, 8 / std::max(1, std::min(M, 8)))) << "\n";
+  // (up to 16 outputs and up to four rows of each, about 32 values per thread
+  // in flight: a grid of two blocks per SM leaves each thread of the last
+  // block one or two rows, so its loads go out in one round; many-output
+  // kernels, whose grids of small blocks leave thousands of partial rows, take
+  // eight outputs and four rows at a time)
+  const int cc = M > kAccRegMax ? 8 : std::min(M, 16);
+  s << "#define MF_CC " << cc << "\n";
+  s << "#define MF_Q " << (M > kAccRegMax ? 4 : std::max(1, std::min(4, 32 / cc))) << "\n";
   // outputs per block-reduction chunk (one warp each)
   s << "#define MF_RC " << std::max(1, std::min(8, out.block / 32)) << "\n";
   s << "struct mf_par { double v[MF_NPAR]; };\n";
