@@ -50,6 +50,22 @@ def test_null_arguments_rejected():
     assert L.lib.mf_kernel_reduce(None, None, 0, 0, None, 0, None) == L.MF_ERR_INVALID
     assert L.lib.mf_buffer_h2d(None, 0, None, 8) == L.MF_ERR_INVALID
     assert L.lib.mf_context_create(0, 0, None) == L.MF_ERR_INVALID
+    assert L.lib.mf_kernel_reduce_segments_chunked(None, None, 0, 1, None, None, None, 0, 0, None) == L.MF_ERR_INVALID
+    assert L.lib.mf_kernel_generate_splitmix_async(None, 1, 16, 100, 7, None, 0, None, 128, 0) == L.MF_ERR_INVALID
+    assert L.lib.mf_context_set_resident(None, 2000) == L.MF_ERR_INVALID
+    assert L.lib.mf_context_resident_stats(None, None, None, None, None) == L.MF_ERR_INVALID
+    assert L.lib.mf_compile_check_resident(None, 1, None, None, None, 0) == L.MF_ERR_INVALID
+
+
+def test_device_properties_without_a_device():
+    import ctypes as C
+    from morefit_gb300 import _lib as L
+    n = C.c_int(-1)
+    assert L.lib.mf_device_count(C.byref(n)) == 0
+    if n.value > 0:
+        pytest.skip("a GPU is visible")
+    name = C.create_string_buffer(64)
+    assert L.lib.mf_device_properties(0, name, 64, None, None, None) == L.MF_ERR_NO_DEVICE
 
 
 @pytest.mark.parametrize("workload,kernel", [("pwave", "lh_grad_kernel"), ("mass", "lh_hessian_kernel")])
