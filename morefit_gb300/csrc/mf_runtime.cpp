@@ -1633,8 +1633,10 @@ struct ResState {
   float2* partials = nullptr;
   unsigned* counter = nullptr;
   cudaStream_t stream = nullptr;
-  // the grid (alive and the device's owner table change under g_res_mu)
-  bool alive = false;
+  // the grid (alive and the device's owner table change under g_res_mu;
+  // the owning thread also reads alive without it, and another context's
+  // start may clear it, hence atomic)
+  std::atomic<bool> alive{false};
   unsigned posted = 0;
   std::atomic<int64_t> hold_until{0};
   uint64_t served = 0, grids = 0;
