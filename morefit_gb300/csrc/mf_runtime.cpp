@@ -2680,7 +2680,13 @@ void coal_execute(mf_coalescer* co, std::vector<CoalReq*>& batch) {
   for (auto& [img, idx] : groups) {
     for (size_t j = 0; j < idx.size(); j++) out_off[idx[j]] = ooff + j * batch[idx[0]]->k->n_outputs;
     const int rc = mfi::launch_multi(c, items[g][0].k, items[g], co->tables + toff, co->out_dev + ooff);
-    if (rc) return coal_fail_all(batch, mf_last_error());
+    if (rc) {
+      // the groups launched before this one still write the mapped results:
+      // let them finish before the next tick reuses that memory
+      const std::string msg = mf_last_error();
+      cudaStreamSynchronize(c->stream);
+      return coal_fail_all(batch, msg);
+    }
     toff += mfi::round16(mfi::multi_table_bytes(items[g][0].k, items[g]));
     ooff += idx.size() * batch[idx[0]]->k->n_outputs;
     g++;
