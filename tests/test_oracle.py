@@ -42,10 +42,11 @@ def _inputs_for(g, events, spec_name):
     return events
 
 
-@pytest.mark.parametrize("workload", ["pwave", "mass", "mass_w", "cbpoly"])
-def test_spec_kernel_reproduces_reference_sums(oracle_lib, workload):
-    g = load_golden(f"{workload}_n1000.json")
-    ev = golden_events(workload, 1000)
+@pytest.mark.parametrize("workload,n", [("pwave", 1000), ("mass", 1000), ("mass_w", 1000), ("cbpoly", 1000),
+                                        ("spwave", 2000)])
+def test_spec_kernel_reproduces_reference_sums(oracle_lib, workload, n):
+    g = load_golden(f"{workload}_n{n}.json")
+    ev = golden_events(workload, n)
     names = [k["name"] for k in g["kernels"] if k["name"].startswith("lh_")]
     assert ("lh_fisher_kernel" in names) == (workload == "mass_w")
     for name in names:
