@@ -113,6 +113,29 @@ def test_all_kernels_compile_without_spills(workload, elem):
         assert info["spill_bytes"] <= limit, (k["name"], info)
 
 
+def test_spwave_kernels_compile_without_spills_in_double_float():
+    """S+P wave (14 parameters): every double-float kernel, the 105-output
+    Hessian included (partials beyond MF_NREG in shared memory), compiles
+    without spilling; in FP32 only the Hessian spills (a Likelihood then
+    evaluates it in register-only parts)."""
+    from morefit_gb300 import _lib as L
+    from morefit_gb300.backend import compile_check
+    g = load_golden("spwave_n2000.json")
+    for elem in (L.MF_F64, L.MF_F32):
+        for k in g["kernels"]:
+            gen = None
+            if k.get("generate"):
+                kind = L.MF_KERNEL_GENERATE
+                gen = (k["outputs"], k["lo"], k["hi"], k["maxprob"])
+            elif k["name"] == "precompute_kernel":
+                kind = L.MF_KERNEL_STORE
+            else:
+                kind = L.MF_KERNEL_REDUCE
+            info = compile_check(k["name"], kind, elem, k["inputs"], k["params"], k["exprs"], gen)
+            if elem == L.MF_F64 or k["name"] != "lh_hessian_kernel":
+                assert info["spill_bytes"] == 0, (elem, k["name"], info)
+
+
 def test_parse_error_is_reported():
     from morefit_gb300 import _lib as L
     from morefit_gb300.backend import lower_source
