@@ -117,27 +117,29 @@ def _unpack_hessian(s: np.ndarray, npar: int) -> np.ndarray:
     return (-2.0 * np.asarray(s))[:, flat].reshape(len(s), npar, npar)
 
 
-def _spd_solve(h: np.ndarray, g: np.ndarray | None):
+def _spd_solve(h: np.ndarray, g: np.ndarray | None, want_diag: bool = True):
     """Cholesky solves of a batch of symmetric matrices h (n, p, p) in the
-    library (mf_spd_solve_batch): (x = h^-1 g or None, diag(h^-1), ok)."""
+    library (mf_spd_solve_batch): (x = h^-1 g or None, diag(h^-1) or None
+    when not wanted, ok)."""
     h = np.ascontiguousarray(h, dtype=np.float64)
     n, p, _ = h.shape
     ok = np.zeros(n, dtype=np.uint8)
-    dinv = np.zeros((n, p))
+    dinv = np.zeros((n, p)) if want_diag else None
     x = None
     gp = xp = None
     if g is not None:
         g = np.ascontiguousarray(g, dtype=np.float64)
         x = np.zeros((n, p))
         gp, xp = L.dptr(g), L.dptr(x)
-    L.check(L.lib.mf_spd_solve_batch(n, p, L.dptr(h), gp, xp, L.dptr(dinv), ok.ctypes.data_as(C.POINTER(C.c_uint8))))
+    dp = L.dptr(dinv) if want_diag else None
+    L.check(L.lib.mf_spd_solve_batch(n, p, L.dptr(h), gp, xp, dp, ok.ctypes.data_as(C.POINTER(C.c_uint8))))
     return x, dinv, ok.astype(bool)
 
 
 def _newton_steps(h: np.ndarray, g: np.ndarray) -> np.ndarray:
     """-H^-1 g per toy: Cholesky where H is positive definite, LAPACK's
     pivoted solve for the others."""
-    x, _, ok = _spd_solve(h, g)
+    x, _, ok = _spd_solve(h, g, want_diag=False)  # the inverse's diagonal is not needed here
     step = -x
     bad = np.nonzero(~ok)[0]
     if bad.size:
